@@ -1,0 +1,435 @@
+// C ABI: contexts, device clouds, trees, stages and the whole-path run.
+//
+// Reference entry points replaced (CPP-TBB-CPU/include/optim3_func.hpp:73-93,
+// driven by CPP-TBB-CPU/application/owm_optim3.cpp):
+//   readXYZfile -> owm_xyz_read + owm_cloud_create
+//   parallel_qtree + storeMinAndNumPoints -> owm_tree_build
+//   stage1 / stage2 / grid + stage3 -> owm_stage1 / owm_stage2 / owm_stage3
+//   the driver's loop body -> owm_run
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "owm_ctx.cuh"
+
+namespace owm {
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+thread_local std::string g_last_error;
+}  // namespace
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+  g_last_error = buf;
+  cudaGetLastError();  // clear sticky-free errors so the context stays usable
+}
+
+void count_launch(int64_t* ctx_counter, int64_t k) {
+  g_launches.fetch_add(k, std::memory_order_relaxed);
+  if (ctx_counter) *ctx_counter += k;
+}
+
+int64_t total_launches() { return g_launches.load(); }
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int DeviceBuffer::reserve(size_t bytes, cudaStream_t s) {
+  if (bytes <= cap) return OWM_OK;
+  if (ptr) {
+    cudaFreeAsync(ptr, s);
+    ptr = nullptr;
+    cap = 0;
+  }
+  size_t want = bytes + bytes / 8 + 4096;
+  cudaError_t e = cudaMallocAsync(&ptr, want, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ptr = nullptr;
+    return OWM_ENOMEM;
+  }
+  cap = want;
+  return OWM_OK;
+}
+
+void DeviceBuffer::release(cudaStream_t s) {
+  if (ptr) cudaFreeAsync(ptr, s);
+  ptr = nullptr;
+  cap = 0;
+}
+
+int tree_alloc(TreeStore* t, DeviceBuffer* mem, int64_t n, const owm_tree_cfg& cfg, cudaStream_t s) {
+  int64_t ncap = tree_node_cap(n, cfg);
+  size_t bytes = 0;
+  auto sz = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  bytes += 3 * sz((size_t)n * 8) + sz((size_t)n * 4) + sz((size_t)ncap * sizeof(Node));
+  int rc = mem->reserve(bytes, s);
+  if (rc) return rc;
+  char* p = static_cast<char*>(mem->ptr);
+  t->xk = (int64_t*)p;
+  p += sz((size_t)n * 8);
+  t->yk = (int64_t*)p;
+  p += sz((size_t)n * 8);
+  t->zk = (int64_t*)p;
+  p += sz((size_t)n * 8);
+  t->pid = (uint32_t*)p;
+  p += sz((size_t)n * 4);
+  t->nodes = (Node*)p;
+  t->point_cap = n;
+  t->node_cap = ncap;
+  return OWM_OK;
+}
+
+int validate_tree_cfg(const owm_tree_cfg* cfg) {
+  if (!cfg) return OWM_EINVAL;
+  if (cfg->policy == OWM_TREE_MAX_NUMBER) {
+    int m = cfg->max_number;
+    if (m < 1 || m > 256 || (m & (m - 1)) != 0) return OWM_EINVAL;
+    return OWM_OK;
+  }
+  if (cfg->policy == OWM_TREE_MIN_RADIUS) return cfg->min_radius > 0.0f && std::isfinite(cfg->min_radius) ? OWM_OK : OWM_EINVAL;
+  return OWM_EINVAL;
+}
+
+}  // namespace owm
+
+using namespace owm;
+
+struct owm_cloud {
+  owm_ctx* ctx;
+  DeviceBuffer mem;
+  int64_t n;
+  owm_bbox bbox;
+};
+
+struct owm_tree {
+  owm_ctx* ctx;
+  DeviceBuffer mem;
+  TreeStore t;
+  const double* d_xyz;  // borrowed from the cloud (stage 3 reads LLP coordinates)
+  owm_bbox bbox;
+  owm_tree_cfg cfg;
+};
+
+extern "C" {
+
+int owm_ctx_create(int device, owm_ctx** out) {
+  if (!out) return OWM_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return OWM_ECUDA;
+  }
+  OWM_CUDA_TRY(cudaSetDevice(device));
+  owm_ctx* c = new owm_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return OWM_ECUDA;
+  }
+  // keep freed pool memory cached: repeated runs then allocate nothing new
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  cudaGetLastError();
+  if (cudaMalloc(&c->d_small, 4096) != cudaSuccess || cudaMallocHost(&c->h_small, 4096) != cudaSuccess ||
+      cudaMalloc(&c->d_job, 4 * sizeof(QueryJob)) != cudaSuccess) {
+    cudaGetLastError();
+    owm_ctx_destroy(c);
+    return OWM_ENOMEM;
+  }
+  cudaMemset(c->d_small, 0, 4096);
+  for (auto& e : c->ev) cudaEventCreate(&e);
+  cudaStreamSynchronize(c->stream);
+  *out = c;
+  return OWM_OK;
+}
+
+int owm_ctx_destroy(owm_ctx* c) {
+  if (!c) return OWM_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->scratch.release(c->stream);
+  c->tree_mem.release(c->stream);
+  c->input.release(c->stream);
+  c->outbuf.release(c->stream);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->d_small) cudaFree(c->d_small);
+  if (c->d_job) cudaFree(c->d_job);
+  if (c->h_small) cudaFreeHost(c->h_small);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  cudaGetLastError();
+  delete c;
+  return OWM_OK;
+}
+
+int owm_ctx_sync(owm_ctx* c) {
+  if (!c) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return OWM_OK;
+}
+
+void* owm_ctx_stream(owm_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int64_t owm_ctx_launches(const owm_ctx* c) { return c ? c->launches : owm::total_launches(); }
+
+int owm_ctx_device_status(owm_ctx* c, int32_t* status) {
+  if (!c || !status) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small + kStatusSlot, 4, cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  *status = (int32_t)c->h_small[0];
+  return OWM_OK;
+}
+
+int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, owm_cloud** out) {
+  if (!c || !xyz || !out || n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
+  *out = nullptr;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  owm_bbox bb;
+  if (bbox) {
+    bb = *bbox;
+  } else if (is_device_ptr(xyz)) {
+    int rc = device_bbox(c, xyz, n, &bb);
+    if (rc) return rc;
+  } else {
+    owm_bbox_of(xyz, n, &bb);
+  }
+  if (!std::isfinite(bb.min_x) || !std::isfinite(bb.max_x) || !std::isfinite(bb.min_y) ||
+      !std::isfinite(bb.max_y) || bb.max_x < bb.min_x || bb.max_y < bb.min_y)
+    return OWM_EINVAL;
+  owm_cloud* cl = new owm_cloud();
+  cl->ctx = c;
+  cl->n = n;
+  cl->bbox = bb;
+  if (cl->mem.reserve((size_t)n * 24, c->stream) != OWM_OK) {
+    delete cl;
+    return OWM_ENOMEM;
+  }
+  cudaError_t e = cudaMemcpyAsync(cl->mem.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "cloud copy", __FILE__, __LINE__);
+    cl->mem.release(c->stream);
+    delete cl;
+    return OWM_ECUDA;
+  }
+  *out = cl;
+  return OWM_OK;
+}
+
+int owm_cloud_destroy(owm_cloud* cl) {
+  if (!cl) return OWM_OK;
+  cudaSetDevice(cl->ctx->device);
+  cl->mem.release(cl->ctx->stream);
+  cudaStreamSynchronize(cl->ctx->stream);
+  delete cl;
+  return OWM_OK;
+}
+
+int64_t owm_cloud_size(const owm_cloud* cl) { return cl ? cl->n : 0; }
+
+int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm_tree** out) {
+  if (!c || !cl || !out || validate_tree_cfg(cfg) != OWM_OK) return OWM_EINVAL;
+  *out = nullptr;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  owm_tree* tr = new owm_tree();
+  tr->ctx = c;
+  tr->cfg = *cfg;
+  tr->d_xyz = static_cast<const double*>(cl->mem.ptr);
+  tr->bbox = cl->bbox;
+  int rc = tree_alloc(&tr->t, &tr->mem, cl->n, *cfg, c->stream);
+  if (!rc) rc = c->scratch.reserve(tree_scratch_bytes(cl->n), c->stream);
+  if (!rc) rc = clear_status(c);
+  if (!rc)
+    rc = build_tree(tr->d_xyz, cl->n, cl->bbox, *cfg, &tr->t, c->scratch.ptr, c->scratch.cap,
+                    c->d_small + kStatusSlot, c->stream, &c->launches);
+  if (!rc) rc = check_input_status(c);
+  if (rc) {
+    tr->mem.release(c->stream);
+    cudaStreamSynchronize(c->stream);
+    delete tr;
+    return rc;
+  }
+  *out = tr;
+  return OWM_OK;
+}
+
+int owm_tree_get_info(owm_ctx* c, const owm_tree* tr, owm_tree_info* info) {
+  if (!c || !tr || !info) return OWM_EINVAL;
+  std::memset(info, 0, sizeof(*info));
+  info->npoints = tr->t.n;
+  info->nleaves = tr->t.nleaves;
+  info->nnodes = 2 * (int64_t)tr->t.nleaves - 1;
+  info->key_bits = tr->t.key_bits;
+  info->max_leaf = tr->t.max_leaf;
+  Node root;
+  OWM_CUDA_TRY(cudaMemcpyAsync(&root, tr->t.nodes + tr->t.root, sizeof(Node), cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  info->root_count = root.count;
+  info->root_min_id = root.min_id;
+  return OWM_OK;
+}
+
+int owm_tree_check(owm_ctx* c, const owm_tree* tr) {
+  if (!c || !tr) return OWM_EINVAL;
+  int32_t bad = 0;
+  int rc = check_tree(&tr->t, reinterpret_cast<int32_t*>(c->d_small + kCheckSlot), c->stream, &c->launches, &bad);
+  if (rc) return rc;
+  Node root;
+  OWM_CUDA_TRY(cudaMemcpyAsync(&root, tr->t.nodes + tr->t.root, sizeof(Node), cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (bad != 0 || (int64_t)root.count != tr->t.n) return OWM_EINVAL;
+  return OWM_OK;
+}
+
+int owm_tree_destroy(owm_tree* tr) {
+  if (!tr) return OWM_OK;
+  cudaSetDevice(tr->ctx->device);
+  tr->mem.release(tr->ctx->stream);
+  cudaStreamSynchronize(tr->ctx->stream);
+  delete tr;
+  return OWM_OK;
+}
+
+int owm_stage1(owm_ctx* c, const owm_tree* tr, const owm_params* p, int64_t* win_min) {
+  if (!c || !tr || !p || !win_min || p->ncells <= 0) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  const int64_t nc = p->ncells;
+  size_t need = 2 * sizeof(Edge) * 65536 + (size_t)nc * 4 + (size_t)nc * 8 + 4096;
+  int rc = c->outbuf.reserve(need, c->stream);
+  if (rc) return rc;
+  char* base = static_cast<char*>(c->outbuf.ptr);
+  Edge* ex = (Edge*)base;
+  Edge* ey = ex + 65536;
+  uint32_t* win = (uint32_t*)(ey + 65536);
+  int64_t* w64 = (int64_t*)(((uintptr_t)(win + nc) + 255) & ~(uintptr_t)255);
+  rc = run_stage1(c, tr->t, *p, ex, ey, win);
+  if (rc) return rc;
+  bool dev = is_device_ptr(win_min);
+  rc = u32_to_i64_ids(win, nullptr, nc, dev ? win_min : w64, c->stream, &c->launches);
+  if (rc) return rc;
+  if (!dev) OWM_CUDA_TRY(cudaMemcpyAsync(win_min, w64, (size_t)nc * 8, cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return OWM_OK;
+}
+
+int owm_stage2(owm_ctx* c, int64_t* win_min, int64_t ncells, double overlap, int64_t* n_llp) {
+  if (!c || !win_min || !n_llp || ncells <= 0 || !(overlap >= 0.0 && overlap < 1.0) || ncells >= 0x7FFFFFFFLL)
+    return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  size_t need = (size_t)ncells * 8 + 2 * (size_t)ncells * 4 + 4096;
+  int rc = c->outbuf.reserve(need, c->stream);
+  if (!rc) rc = c->scratch.reserve(stage2_scratch_bytes(ncells), c->stream);
+  if (rc) return rc;
+  char* base = static_cast<char*>(c->outbuf.ptr);
+  int64_t* w64 = (int64_t*)base;
+  uint32_t* win = (uint32_t*)(((uintptr_t)(w64 + ncells) + 255) & ~(uintptr_t)255);
+  uint32_t* llp = (uint32_t*)(((uintptr_t)(win + ncells) + 255) & ~(uintptr_t)255);
+  uint32_t* d_cnt = c->d_small + kCountSlot;
+  OWM_CUDA_TRY(cudaMemcpyAsync(w64, win_min, (size_t)ncells * 8, cudaMemcpyDefault, c->stream));
+  rc = i64_to_u32_ids(w64, ncells, win, c->stream, &c->launches);
+  if (!rc)
+    rc = run_stage2(win, ncells, 0xFFFFFFFELL, overlap, llp, d_cnt, c->scratch.ptr, c->scratch.cap, c->stream,
+                    &c->launches);
+  if (rc) return rc;
+  rc = u32_to_i64_ids(llp, d_cnt, ncells, w64, c->stream, &c->launches);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  int64_t m = c->h_small[0];
+  if (m > 0) OWM_CUDA_TRY(cudaMemcpyAsync(win_min, w64, (size_t)m * 8, cudaMemcpyDefault, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  *n_llp = m;
+  return OWM_OK;
+}
+
+int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_t* llp, int64_t n_llp, int64_t* out,
+               int64_t cap, int64_t* n_out) {
+  if (!c || !tr || !p || (!llp && n_llp > 0) || n_llp < 0 || !n_out || (!out && cap > 0)) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  *n_out = 0;
+  if (p->bsize == 0 || p->ngrid <= 0) return OWM_OK;
+  const int64_t ng = p->ngrid;
+  const int64_t m = std::max<int64_t>(n_llp, 1);
+  size_t need = (size_t)m * 8 + (size_t)m * 4 + (size_t)ng * 4 + (size_t)ng * 8 + 8192;
+  int rc = c->outbuf.reserve(need, c->stream);
+  if (!rc) rc = c->scratch.reserve(stage3_scratch_bytes(ng), c->stream);
+  if (rc) return rc;
+  char* base = static_cast<char*>(c->outbuf.ptr);
+  auto al = [](void* q) { return (char*)(((uintptr_t)q + 255) & ~(uintptr_t)255); };
+  int64_t* l64 = (int64_t*)base;
+  uint32_t* l32 = (uint32_t*)al(l64 + m);
+  uint32_t* s3 = (uint32_t*)al(l32 + m);
+  int64_t* s64 = (int64_t*)al(s3 + ng);
+  uint32_t* d_nllp = c->d_small + kLlpSlot;
+  uint32_t* d_cnt = c->d_small + kCountSlot;
+  c->h_small[1] = (uint32_t)n_llp;
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_nllp, &c->h_small[1], 4, cudaMemcpyHostToDevice, c->stream));
+  if (n_llp > 0) {
+    OWM_CUDA_TRY(cudaMemcpyAsync(l64, llp, (size_t)n_llp * 8, cudaMemcpyDefault, c->stream));
+    rc = i64_to_u32_ids(l64, n_llp, l32, c->stream, &c->launches);
+    if (rc) return rc;
+  }
+  rc = run_stage3(tr->t.view(), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
+                  c->d_job, c->stream, &c->launches);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small + 2, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  int64_t k = c->h_small[2];
+  *n_out = k;
+  if (k > cap) return OWM_ERANGE;
+  if (k > 0) {
+    rc = u32_to_i64_ids(s3, nullptr, k, s64, c->stream, &c->launches);
+    if (rc) return rc;
+    OWM_CUDA_TRY(cudaMemcpyAsync(out, s64, (size_t)k * 8, cudaMemcpyDefault, c->stream));
+    OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  return OWM_OK;
+}
+
+int owm_run(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int64_t* seeds, int64_t cap, int64_t* n_seeds,
+            owm_run_info* info) {
+  if (!c || !cl || !cfg || !n_seeds || (!seeds && cap > 0)) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  return run_pipeline(c, static_cast<const double*>(cl->mem.ptr), cl->n, cl->bbox, *cfg, seeds, cap, n_seeds, info);
+}
+
+int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, const owm_run_cfg* cfg,
+                 int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
+  if (!c || !xyz || !cfg || !n_seeds || n <= 0 || n >= 0x7FFFFFFFLL || (!seeds && cap > 0)) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  owm_bbox bb;
+  if (bbox) {
+    bb = *bbox;
+  } else if (is_device_ptr(xyz)) {
+    int rc = device_bbox(c, xyz, n, &bb);
+    if (rc) return rc;
+  } else {
+    owm_bbox_of(xyz, n, &bb);
+  }
+  int rc = c->input.reserve((size_t)n * 24, c->stream);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaMemcpyAsync(c->input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
+  return run_pipeline(c, static_cast<const double*>(c->input.ptr), n, bb, *cfg, seeds, cap, n_seeds, info);
+}
+
+}  // extern "C"

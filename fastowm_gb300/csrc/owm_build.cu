@@ -1,0 +1,525 @@
+// Spatial index build on the device: the GB300 replacement of the reference's
+// parallel_qtree + storeMinAndNumPoints (CPP-TBB-CPU/src/optim3_func.cpp:
+// 220-307).
+//
+//   k_morton          quantise (x, y) on the square root domain, interleave
+//                     (2D Morton / quadtree order), one 32-bit key per point
+//   radix_sort        stable LSD sort of (key, input position)
+//   k_gather_leaves   permute the points into sorted order as exact
+//                     order-preserving int64 keys + 1-based id, and reduce each
+//                     leaf of L points (count, outward float box, (z,id)-min)
+//                     with warp shuffles -- one pass over the points
+//   k_leaf_starts /   leaves = quadtree cells of half-side <= min_radius
+//   k_leaf_reduce     (min-radius policy) or any other leaf partition
+//   k_karras          binary radix hierarchy over the leaves (Karras 2012) on
+//                     64-bit (leaf Morton key, leaf index) codes
+//   k_escapes         depth-first "escape" link of every node, so that queries
+//                     walk the tree without a stack
+//   k_refit           bottom-up atomic refit: internal count, box and
+//                     (z, id)-min -- the reference's O3 memo (storeMinAndNumPoints)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "owm_build.cuh"
+
+namespace owm {
+
+namespace {
+
+__device__ __forceinline__ uint32_t spread_bits16(uint32_t x) {
+  x &= 0x0000ffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+// Quadtree order key: x bit above y bit at each level, like the
+// reference's quadrant index (x >= cx) << 1 | (y >= cy) (optim3_func.cpp:92-100).
+__global__ void k_morton(const double* __restrict__ xyz, int64_t n, double ox, double oy, double scale,
+                         int bits, uint32_t* __restrict__ keys) {
+  const float qmax = (float)((1u << bits) - 1u);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double x = __ldg(xyz + 3 * i), y = __ldg(xyz + 3 * i + 1);
+    float fx = (float)((x - ox) * scale), fy = (float)((y - oy) * scale);
+    fx = fminf(fmaxf(fx, 0.0f), qmax);
+    fy = fminf(fmaxf(fy, 0.0f), qmax);
+    keys[i] = (spread_bits16((uint32_t)fx) << 1) | spread_bits16((uint32_t)fy);
+  }
+}
+
+struct LeafAcc {
+  int64_t xmin, xmax, ymin, ymax, zmin;
+  uint32_t idmin, posmin, count;
+  __device__ __forceinline__ void init() {
+    xmin = ymin = 0x7FFFFFFFFFFFFFFFll;
+    xmax = ymax = (int64_t)0x8000000000000000ull;
+    zmin = 0x7FFFFFFFFFFFFFFFll;
+    idmin = 0xFFFFFFFFu;
+    posmin = 0xFFFFFFFFu;
+    count = 0;
+  }
+  __device__ __forceinline__ void add(int64_t x, int64_t y, int64_t z, uint32_t id, uint32_t pos) {
+    xmin = min(xmin, x);
+    xmax = max(xmax, x);
+    ymin = min(ymin, y);
+    ymax = max(ymax, y);
+    if (zid_less(z, id, zmin, idmin)) {
+      zmin = z;
+      idmin = id;
+      posmin = pos;
+    }
+    ++count;
+  }
+  // reduce with lanes lane^o for o in [1, width)
+  __device__ __forceinline__ void reduce(int width) {
+    for (int o = width >> 1; o >= 1; o >>= 1) {
+      int64_t a = __shfl_xor_sync(0xffffffffu, xmin, o);
+      int64_t b = __shfl_xor_sync(0xffffffffu, xmax, o);
+      int64_t c = __shfl_xor_sync(0xffffffffu, ymin, o);
+      int64_t d = __shfl_xor_sync(0xffffffffu, ymax, o);
+      int64_t z = __shfl_xor_sync(0xffffffffu, zmin, o);
+      uint32_t id = __shfl_xor_sync(0xffffffffu, idmin, o);
+      uint32_t ps = __shfl_xor_sync(0xffffffffu, posmin, o);
+      uint32_t ct = __shfl_xor_sync(0xffffffffu, count, o);
+      xmin = min(xmin, a);
+      xmax = max(xmax, b);
+      ymin = min(ymin, c);
+      ymax = max(ymax, d);
+      if (zid_less(z, id, zmin, idmin)) {
+        zmin = z;
+        idmin = id;
+        posmin = ps;
+      }
+      count += ct;
+    }
+  }
+};
+
+__device__ __forceinline__ void write_leaf(Node* nd, const LeafAcc& a, int32_t first, double ox, double oy) {
+  Node n;
+  n.x0 = __double2float_rd(__dsub_rd(dkey_inv(a.xmin), ox));
+  n.y0 = __double2float_rd(__dsub_rd(dkey_inv(a.ymin), oy));
+  n.x1 = __double2float_ru(__dsub_ru(dkey_inv(a.xmax), ox));
+  n.y1 = __double2float_ru(__dsub_ru(dkey_inv(a.ymax), oy));
+  n.zmin = a.zmin;
+  n.min_id = a.idmin;
+  n.min_pos = a.posmin;
+  n.count = a.count;
+  n.left = first;
+  n.escape = kEnd;
+  n.right = -1;
+  *nd = n;
+}
+
+// Loads one input point as order keys; returns false if a coordinate is not
+// finite (the reference's comparisons are undefined there: such input is
+// rejected through the context's status word).
+__device__ __forceinline__ bool load_point(const double* __restrict__ xyz, uint32_t src, int64_t& x, int64_t& y,
+                                           int64_t& z) {
+  const double* p = xyz + 3 * (int64_t)src;
+  const double dx = __ldg(p), dy = __ldg(p + 1), dz = __ldg(p + 2);
+  x = dkey(dx);
+  y = dkey(dy);
+  z = dkey(dz);
+  const uint64_t e = 0x7FF0000000000000ull;
+  return ((__double_as_longlong(dx) & e) != e) & ((__double_as_longlong(dy) & e) != e) &
+         ((__double_as_longlong(dz) & e) != e);
+}
+
+// One warp per unit of max(L, 32) sorted positions.  L in {1,2,4,...,1024}.
+template <int L>
+__global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict__ xyz, const uint32_t* __restrict__ perm,
+                                                       int64_t n, int32_t nleaves, double ox, double oy,
+                                                       int64_t* __restrict__ xk, int64_t* __restrict__ yk,
+                                                       int64_t* __restrict__ zk, uint32_t* __restrict__ pid,
+                                                       Node* __restrict__ leaves, uint32_t* __restrict__ status) {
+  constexpr int kUnit = L < 32 ? 32 : L;
+  bool finite = true;
+  constexpr int kSeg = L < 32 ? L : 32;
+  const int lane = threadIdx.x & 31;
+  const int64_t nunits = (n + kUnit - 1) / kUnit;
+  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits;
+       u += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    LeafAcc acc;
+    acc.init();
+#pragma unroll
+    for (int c = 0; c < kUnit; c += 32) {
+      int64_t pos = u * kUnit + c + lane;
+      if (pos < n) {
+        uint32_t src = __ldg(perm + pos);
+        int64_t x, y, z;
+        finite &= load_point(xyz, src, x, y, z);
+        xk[pos] = x;
+        yk[pos] = y;
+        zk[pos] = z;
+        pid[pos] = src + 1;
+        acc.add(x, y, z, src + 1, (uint32_t)pos);
+      }
+    }
+    acc.reduce(kSeg);
+    if ((lane & (kSeg - 1)) == 0) {
+      int64_t first = u * kUnit + lane;  // L < 32: segment start; else lane 0
+      if (first < n) {
+        int64_t li = first / L;
+        write_leaf(leaves + li, acc, (int32_t)first, ox, oy);
+      }
+    }
+  }
+  if (!finite) atomicOr(status, 1u);
+}
+
+__global__ void k_gather(const double* __restrict__ xyz, const uint32_t* __restrict__ perm, int64_t n,
+                         int64_t* __restrict__ xk, int64_t* __restrict__ yk, int64_t* __restrict__ zk,
+                         uint32_t* __restrict__ pid, uint32_t* __restrict__ status) {
+  bool finite = true;
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t src = __ldg(perm + pos);
+    int64_t x, y, z;
+    finite &= load_point(xyz, src, x, y, z);
+    xk[pos] = x;
+    yk[pos] = y;
+    zk[pos] = z;
+    pid[pos] = src + 1;
+  }
+  if (!finite) atomicOr(status, 1u);
+}
+
+// flag[pos] = 1 where a new leaf starts: the quadtree cell (key >> cell_shift)
+// changes, or the current run reached max_leaf points from its cell start.
+__global__ void k_leaf_flags(const uint32_t* __restrict__ keys, int64_t n, int cell_shift,
+                             uint32_t* __restrict__ flags) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t f = 1;
+    if (pos > 0) {
+      uint32_t a = cell_shift >= 32 ? 0u : keys[pos] >> cell_shift;
+      uint32_t b = cell_shift >= 32 ? 0u : keys[pos - 1] >> cell_shift;
+      f = a != b;
+    }
+    flags[pos] = f;
+  }
+}
+
+__global__ void k_leaf_starts(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ scan, int64_t n,
+                              int32_t* __restrict__ starts) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    if (flags[pos]) starts[scan[pos]] = (int32_t)pos;
+  }
+}
+
+// One warp per leaf of any size; starts has nleaves+1 entries (last = n).
+__global__ void k_leaf_reduce(const int64_t* __restrict__ xk, const int64_t* __restrict__ yk,
+                              const int64_t* __restrict__ zk, const uint32_t* __restrict__ pid,
+                              const int32_t* __restrict__ starts, int32_t nleaves, double ox, double oy,
+                              Node* __restrict__ leaves) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t li = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < nleaves;
+       li += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    int32_t b = starts[li], e = starts[li + 1];
+    LeafAcc acc;
+    acc.init();
+    for (int32_t p = b + lane; p < e; p += 32) acc.add(xk[p], yk[p], zk[p], pid[p], (uint32_t)p);
+    acc.reduce(32);
+    if (lane == 0) write_leaf(leaves + li, acc, b, ox, oy);
+  }
+}
+
+__device__ __forceinline__ int32_t leaf_first(int32_t li, int32_t L, const int32_t* starts) {
+  return starts ? starts[li] : li * L;
+}
+
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ mk, int32_t L, const int32_t* __restrict__ starts,
+                                     int32_t nl, int32_t i, int32_t j) {
+  if (j < 0 || j >= nl) return -1;
+  uint64_t a = ((uint64_t)__ldg(mk + leaf_first(i, L, starts)) << 32) | (uint32_t)i;
+  uint64_t b = ((uint64_t)__ldg(mk + leaf_first(j, L, starts)) << 32) | (uint32_t)j;
+  return __clzll((long long)(a ^ b));
+}
+
+// Karras (2012), Sec. 4: internal node i covers leaves [min(i,j), max(i,j)]
+// and splits after gamma.  Internal nodes are 0..nl-2, leaf li is nl-1+li.
+__global__ void k_karras(const uint32_t* __restrict__ mk, int32_t L, const int32_t* __restrict__ starts, int32_t nl,
+                         Node* __restrict__ nodes, int32_t* __restrict__ parent, int32_t* __restrict__ right_of,
+                         int32_t* __restrict__ last_of) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nl - 1) return;
+  int d = delta(mk, L, starts, nl, i, i + 1) - delta(mk, L, starts, nl, i, i - 1) > 0 ? 1 : -1;
+  int dmin = delta(mk, L, starts, nl, i, i - d);
+  int32_t lmax = 2;
+  while (delta(mk, L, starts, nl, i, i + lmax * d) > dmin) lmax <<= 1;
+  int32_t l = 0;
+  for (int32_t t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(mk, L, starts, nl, i, i + (l + t) * d) > dmin) l += t;
+  int32_t j = i + l * d;
+  int dnode = delta(mk, L, starts, nl, i, j);
+  int32_t s = 0;
+  for (int32_t div = 2;; div <<= 1) {
+    int32_t t = (l + div - 1) / div;
+    if (delta(mk, L, starts, nl, i, i + (s + t) * d) > dnode) s += t;
+    if (t <= 1) break;
+  }
+  int32_t gamma = i + s * d + (d < 0 ? -1 : 0);
+  int32_t lo = min(i, j), hi = max(i, j);
+  int32_t left = (lo == gamma) ? (nl - 1 + gamma) : gamma;
+  int32_t right = (hi == gamma + 1) ? (nl - 1 + gamma + 1) : gamma + 1;
+  nodes[i].left = left;
+  nodes[i].right = right;
+  parent[left] = i;
+  parent[right] = i;
+  right_of[gamma] = right;
+  last_of[i] = hi;
+}
+
+// escape(node covering leaves [a, b]) = right child of the split after b
+// (the unique internal node whose left subtree ends at b), or end.
+__global__ void k_escapes(Node* __restrict__ nodes, const int32_t* __restrict__ right_of,
+                          const int32_t* __restrict__ last_of, int32_t nl) {
+  int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 2 * nl - 1) return;
+  int32_t last = k < nl - 1 ? last_of[k] : k - (nl - 1);
+  nodes[k].escape = last >= nl - 1 ? kEnd : right_of[last];
+}
+
+__device__ __forceinline__ void load_summary(const Node* p, float4& box, int64_t& z, uint32_t& id, uint32_t& pos,
+                                             uint32_t& cnt) {
+  // L2 loads: the sibling's summary was written by another thread of this grid
+  box = __ldcg(reinterpret_cast<const float4*>(p));
+  z = __ldcg(&p->zmin);
+  id = __ldcg(&p->min_id);
+  pos = __ldcg(&p->min_pos);
+  cnt = __ldcg(&p->count);
+}
+
+__global__ void k_refit(Node* __restrict__ nodes, const int32_t* __restrict__ parent, int32_t* __restrict__ flags,
+                        int32_t nl) {
+  int32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+  if (li >= nl) return;
+  int32_t n = parent[nl - 1 + li];
+  while (n >= 0) {
+    __threadfence();
+    if (atomicAdd(&flags[n], 1) == 0) return;  // sibling not done yet
+    __threadfence();
+    const Node* a = nodes + __ldcg(&nodes[n].left);
+    const Node* b = nodes + __ldcg(&nodes[n].right);
+    float4 ba, bb;
+    int64_t za, zb;
+    uint32_t ia, ib, pa, pb, ca, cb;
+    load_summary(a, ba, za, ia, pa, ca);
+    load_summary(b, bb, zb, ib, pb, cb);
+    Node* o = nodes + n;
+    float4 box = make_float4(fminf(ba.x, bb.x), fminf(ba.y, bb.y), fmaxf(ba.z, bb.z), fmaxf(ba.w, bb.w));
+    __stcg(reinterpret_cast<float4*>(o), box);
+    bool bl = zid_less(zb, ib, za, ia);
+    __stcg(&o->zmin, bl ? zb : za);
+    __stcg(&o->min_id, bl ? ib : ia);
+    __stcg(&o->min_pos, bl ? pb : pa);
+    __stcg(&o->count, ca + cb);
+    n = parent[n];
+  }
+}
+
+// Sum of children == count for every internal node (checkNumPoints).
+__global__ void k_check_counts(const Node* __restrict__ nodes, int32_t nl, int32_t* __restrict__ bad) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nl - 1) return;
+  const Node& n = nodes[i];
+  const Node& a = nodes[n.left];
+  const Node& b = nodes[n.right];
+  bool ok = n.count == a.count + b.count;
+  bool zok = !zid_less(a.zmin, a.min_id, n.zmin, n.min_id) && !zid_less(b.zmin, b.min_id, n.zmin, n.min_id);
+  bool box_ok = n.x0 <= a.x0 && n.x0 <= b.x0 && n.y0 <= a.y0 && n.y0 <= b.y0 && n.x1 >= a.x1 && n.x1 >= b.x1 &&
+                n.y1 >= a.y1 && n.y1 >= b.y1;
+  if (!(ok && zok && box_ok)) atomicAdd(bad, 1);
+}
+
+int grid_for(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  if (g > 152 * 32) g = 152 * 32;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+template <int L>
+void launch_gather_leaves(const double* xyz, const uint32_t* perm, int64_t n, int32_t nl, double ox, double oy,
+                          TreeStore* t, uint32_t* status, cudaStream_t s) {
+  constexpr int kUnit = L < 32 ? 32 : L;
+  int64_t nunits = (n + kUnit - 1) / kUnit;
+  int64_t warps = nunits;
+  int64_t blocks = (warps * 32 + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_gather_leaves<L><<<(unsigned)blocks, 256, 0, s>>>(xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid,
+                                                      t->nodes + (nl - 1), status);
+}
+
+}  // namespace
+
+int choose_key_bits(int64_t n, int policy, double side, float min_radius) {
+  int b = n <= (1 << 18) ? 8 : 12;
+  if (policy == OWM_TREE_MIN_RADIUS && min_radius > 0.0f) {
+    // quadtree depth where half-side <= 2*min_radius (insertPoint's split
+    // rule, optim3_func.cpp:107: split while radius*0.5 > minRadius)
+    double r = side * 0.5;
+    int d = 0;
+    while (r * 0.5 > (double)min_radius && d < 16) {
+      r *= 0.5;
+      ++d;
+    }
+    if (d > b) b = d <= 12 ? 12 : 16;
+  }
+  return 2 * b;
+}
+
+size_t tree_scratch_bytes(int64_t n) {
+  size_t a = 0;
+  auto add = [&](size_t bytes) { a += (bytes + 255) & ~(size_t)255; };
+  add((size_t)n * 4);  // keys0
+  add((size_t)n * 4);  // keys1
+  add((size_t)n * 4);  // vals0
+  add((size_t)n * 4);  // vals1
+  add(radix_sort_temp_bytes(n));
+  add((size_t)(n + 1) * 4);  // leaf starts
+  add((size_t)(2 * n + 2) * 4);  // parent
+  add((size_t)(n + 1) * 4);      // flags / right_of
+  add((size_t)(n + 1) * 4);      // right_of
+  add((size_t)(n + 1) * 4);      // last_of
+  add(scan_temp_bytes(n) + 64);
+  return a + 1024;
+}
+
+int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
+               void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches) {
+  if (n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
+  if (scratch_bytes < tree_scratch_bytes(n)) return OWM_ENOMEM;
+  char* sp = static_cast<char*>(scratch);
+  auto take = [&](size_t bytes) {
+    void* p = sp;
+    sp += (bytes + 255) & ~(size_t)255;
+    return p;
+  };
+  uint32_t* k0 = (uint32_t*)take((size_t)n * 4);
+  uint32_t* k1 = (uint32_t*)take((size_t)n * 4);
+  uint32_t* v0 = (uint32_t*)take((size_t)n * 4);
+  uint32_t* v1 = (uint32_t*)take((size_t)n * 4);
+  size_t sort_bytes = radix_sort_temp_bytes(n);
+  void* sort_tmp = take(sort_bytes);
+  int32_t* starts = (int32_t*)take((size_t)(n + 1) * 4);
+  int32_t* parent = (int32_t*)take((size_t)(2 * n + 2) * 4);
+  int32_t* flags = (int32_t*)take((size_t)(n + 1) * 4);
+  int32_t* right_of = (int32_t*)take((size_t)(n + 1) * 4);
+  int32_t* last_of = (int32_t*)take((size_t)(n + 1) * 4);
+  void* scan_tmp = take(scan_temp_bytes(n) + 64);
+
+  // Square root domain like the reference's quadtree (getRadius/getCenter,
+  // optim3_func.cpp:6-26): centre of the bbox, half-side = max half-extent.
+  double rx = (bb.max_x - bb.min_x) * 0.5, ry = (bb.max_y - bb.min_y) * 0.5;
+  double R = rx >= ry ? rx : ry;
+  if (!(R > 0.0)) R = 0.5;
+  double ox = bb.min_x + rx - R, oy = bb.min_y + ry - R;
+  int key_bits = choose_key_bits(n, cfg.policy, 2.0 * R, cfg.min_radius);
+  int bits_axis = key_bits / 2;
+  double scale = (double)(1u << bits_axis) / (2.0 * R);
+  t->ox = bb.min_x;  // float boxes are offsets from the bbox corner
+  t->oy = bb.min_y;
+  t->key_bits = key_bits;
+  t->n = n;
+
+  k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0);
+  count_launch(launches);
+  bool alt = false;
+  OWM_CUDA_TRY(radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches));
+  const uint32_t* mk = alt ? k1 : k0;
+  const uint32_t* perm = alt ? v1 : v0;
+
+  int32_t L = cfg.max_number;
+  int32_t nl;
+  const int32_t* lstarts = nullptr;
+  bool fixed = cfg.policy == OWM_TREE_MAX_NUMBER;
+  if (fixed) {
+    nl = (int32_t)((n + L - 1) / L);
+  } else {
+    // min-radius leaves: runs of equal cell key at the leaf depth
+    double r = R;
+    int d = 0;
+    while (r * 0.5 > (double)cfg.min_radius && d < bits_axis) {
+      r *= 0.5;
+      ++d;
+    }
+    int cell_shift = 2 * (bits_axis - d);
+    uint32_t* fl = reinterpret_cast<uint32_t*>(flags);  // reuse as scratch, [n]
+    uint32_t* sc = reinterpret_cast<uint32_t*>(parent);  // [n] + total
+    k_leaf_flags<<<grid_for(n, 256), 256, 0, s>>>(mk, n, cell_shift, fl);
+    count_launch(launches);
+    OWM_CUDA_TRY(exclusive_scan_u32(fl, sc, n, sc + n, scan_tmp, scan_temp_bytes(n) + 64, s, launches));
+    k_leaf_starts<<<grid_for(n, 256), 256, 0, s>>>(fl, sc, n, starts);
+    count_launch(launches);
+    uint32_t h_nl = 0;
+    OWM_CUDA_TRY(cudaMemcpyAsync(&h_nl, sc + n, 4, cudaMemcpyDeviceToHost, s));
+    OWM_CUDA_TRY(cudaStreamSynchronize(s));
+    nl = (int32_t)h_nl;
+    OWM_CUDA_TRY(cudaMemcpyAsync(starts + nl, &n, 4, cudaMemcpyHostToDevice, s));  // n < 2^31
+    OWM_CUDA_TRY(cudaStreamSynchronize(s));
+    lstarts = starts;
+    L = 0;
+  }
+  int64_t nnodes = 2 * (int64_t)nl - 1;
+  if (t->node_cap < nnodes || t->point_cap < n) return OWM_ENOMEM;
+  t->nleaves = nl;
+  t->root = 0;
+
+  if (fixed) {
+    switch (L) {
+      case 1: launch_gather_leaves<1>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 2: launch_gather_leaves<2>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 4: launch_gather_leaves<4>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 8: launch_gather_leaves<8>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 16: launch_gather_leaves<16>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 32: launch_gather_leaves<32>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 64: launch_gather_leaves<64>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 128: launch_gather_leaves<128>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 256: launch_gather_leaves<256>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      default:
+        return OWM_EINVAL;  // the API only admits powers of two up to 256
+    }
+    count_launch(launches);
+  } else {
+    k_gather<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status);
+    count_launch(launches);
+    int64_t blocks = ((int64_t)nl * 32 + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_leaf_reduce<<<(unsigned)blocks, 256, 0, s>>>(t->xk, t->yk, t->zk, t->pid, lstarts, nl, t->ox, t->oy,
+                                                    t->nodes + (nl - 1));
+    count_launch(launches);
+  }
+
+  if (nl > 1) {
+    OWM_CUDA_TRY(cudaMemsetAsync(parent, 0xFF, (size_t)nnodes * 4, s));
+    OWM_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)nl * 4, s));
+    k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, t->nodes, parent, right_of, last_of);
+    k_escapes<<<(unsigned)((nnodes + 255) / 256), 256, 0, s>>>(t->nodes, right_of, last_of, nl);
+    k_refit<<<(nl + 255) / 256, 256, 0, s>>>(t->nodes, parent, flags, nl);
+    count_launch(launches, 3);
+  }
+  t->max_leaf = fixed ? L : -1;
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int check_tree(const TreeStore* t, int32_t* d_bad, cudaStream_t s, int64_t* launches, int32_t* h_bad) {
+  OWM_CUDA_TRY(cudaMemsetAsync(d_bad, 0, 4, s));
+  if (t->nleaves > 1) {
+    k_check_counts<<<(t->nleaves - 1 + 255) / 256, 256, 0, s>>>(t->nodes, t->nleaves, d_bad);
+    count_launch(launches);
+  }
+  OWM_CUDA_TRY(cudaMemcpyAsync(h_bad, d_bad, 4, cudaMemcpyDeviceToHost, s));
+  OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  return OWM_OK;
+}
+
+}  // namespace owm

@@ -1,0 +1,54 @@
+// Tree storage and build entry points shared by the API, batch and server.
+#pragma once
+
+#include "owm_internal.cuh"
+
+namespace owm {
+
+// Device storage of one tree.  Point arrays hold `point_cap` entries, nodes
+// `node_cap` (>= 2*nleaves-1).
+struct TreeStore {
+  int64_t* xk = nullptr;
+  int64_t* yk = nullptr;
+  int64_t* zk = nullptr;
+  uint32_t* pid = nullptr;
+  Node* nodes = nullptr;
+  int64_t point_cap = 0, node_cap = 0;
+  int64_t n = 0;
+  int32_t nleaves = 0, root = 0, key_bits = 0, max_leaf = 0;
+  double ox = 0, oy = 0;
+
+  TreeView view() const {
+    TreeView v;
+    v.xk = xk;
+    v.yk = yk;
+    v.zk = zk;
+    v.pid = pid;
+    v.nodes = nodes;
+    v.nleaves = nleaves;
+    v.root = root;
+    v.ox = ox;
+    v.oy = oy;
+    return v;
+  }
+};
+
+// Node slots needed for n points under a tree configuration.
+inline int64_t tree_node_cap(int64_t n, const owm_tree_cfg& cfg) {
+  int64_t nl = cfg.policy == OWM_TREE_MAX_NUMBER ? (n + cfg.max_number - 1) / cfg.max_number : n;
+  return 2 * nl - 1;
+}
+
+size_t tree_scratch_bytes(int64_t n);
+int choose_key_bits(int64_t n, int policy, double side, float min_radius);
+
+// Builds the tree of n device points (AoS xyz) into t (whose arrays must be
+// allocated with enough capacity).  Scratch is caller-provided.
+// Non-finite input coordinates set bit 0 of *status (device word).
+int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bbox, const owm_tree_cfg& cfg, TreeStore* t,
+               void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches);
+
+// Structural self-check (checkNumPoints); *h_bad = number of bad nodes.
+int check_tree(const TreeStore* t, int32_t* d_bad, cudaStream_t s, int64_t* launches, int32_t* h_bad);
+
+}  // namespace owm

@@ -1,0 +1,130 @@
+// Internal device/host definitions shared by the OWM CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cstdio>
+
+#include "owm_gb300.h"
+
+namespace owm {
+
+// ---------------------------------------------------------------------------
+// Order-preserving integer keys for IEEE doubles.
+//
+// For finite doubles a, b (with -0.0 folded to +0.0):  a < b  <=>
+// key(a) < key(b) as signed int64.  Every containment and minimum test of the
+// path is done on these keys, so the decisions equal the reference's FP64
+// comparisons bit for bit while running on the integer pipes (GB300's FP64
+// rate is low).
+__host__ __device__ __forceinline__ int64_t dkey(double d) {
+  int64_t b;
+#ifdef __CUDA_ARCH__
+  b = __double_as_longlong(d);
+#else
+  __builtin_memcpy(&b, &d, 8);
+#endif
+  if (b == (int64_t)0x8000000000000000ull) b = 0;  // -0.0 -> +0.0
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFll);
+}
+__host__ __device__ __forceinline__ double dkey_inv(int64_t k) {
+  int64_t b = k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFll);
+  double d;
+#ifdef __CUDA_ARCH__
+  d = __longlong_as_double(b);
+#else
+  __builtin_memcpy(&d, &b, 8);
+#endif
+  return d;
+}
+
+// key(DBL_MAX): z of the reference's sentinel point 0 (optim3_func.cpp:708).
+constexpr int64_t kZSentinel = 0x7FEFFFFFFFFFFFFFll;
+constexpr int32_t kEnd = -1;  // end of a stackless walk
+
+// (z, id) lexicographic "less": the reference's strict `<` on z plus a
+// deterministic tie rule on the point id.
+__host__ __device__ __forceinline__ bool zid_less(int64_t za, uint32_t ia, int64_t zb, uint32_t ib) {
+  return za < zb || (za == zb && ia < ib);
+}
+
+// ---------------------------------------------------------------------------
+// Hierarchy node (48 B = three 16-byte words, loaded as such by queries).
+// Boxes are float offsets from the tree origin, rounded outward, so "fully
+// inside" / "disjoint" decisions taken on them are always right and anything
+// unsure falls to an exact per-point test.
+struct __align__(16) Node {
+  float x0, y0, x1, y1;  // outward-rounded box, relative to origin
+  int64_t zmin;          // dkey of the minimum z under the node
+  uint32_t min_id;       // 1-based id of that point
+  uint32_t min_pos;      // its position in the sorted point arrays
+  uint32_t count;        // points under the node
+  int32_t left;          // internal: left child node; leaf: first point
+  int32_t escape;        // next node of a depth-first walk after this subtree
+  int32_t right;         // internal: right child; leaf: -1
+};
+static_assert(sizeof(Node) == 48, "Node must stay 48 bytes");
+
+// Window / cell edge along one axis: exact keys for point tests, and the
+// float offsets rounded down / up for node tests.
+struct __align__(16) Edge {
+  int64_t lo_k, hi_k;
+  float lo_dn, lo_up, hi_dn, hi_up;
+};
+static_assert(sizeof(Edge) == 32, "Edge must stay 32 bytes");
+
+// Device view of one tree (also one tile of a batch).
+struct TreeView {
+  const int64_t* xk;  // sorted point keys
+  const int64_t* yk;
+  const int64_t* zk;
+  const uint32_t* pid;  // 1-based ids
+  const Node* nodes;    // [2*nleaves-1]: internal 0..nl-2, leaves nl-1..
+  int32_t nleaves;
+  int32_t root;
+  double ox, oy;        // origin of the float boxes
+};
+
+// ---------------------------------------------------------------------------
+// Error plumbing.
+#define OWM_CUDA_TRY(expr)                                                          \
+  do {                                                                              \
+    cudaError_t _e = (expr);                                                        \
+    if (_e != cudaSuccess) {                                                        \
+      owm::set_last_cuda_error(_e, #expr, __FILE__, __LINE__);                      \
+      return OWM_ECUDA;                                                             \
+    }                                                                               \
+  } while (0)
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+
+// Library-wide kernel launch counter (every launch of this library's kernels
+// goes through count_launch) and the per-context one.
+void count_launch(int64_t* ctx_counter, int64_t k = 1);
+
+// ---------------------------------------------------------------------------
+// Primitives (owm_sort.cu).
+struct SortTemp {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+// Temp bytes for sorting n keys (pairs or keys-only) and for scanning n ints.
+size_t radix_sort_temp_bytes(int64_t n);
+size_t scan_temp_bytes(int64_t n);
+
+// LSD radix sort of uint32 keys (and optional uint32 values) on bits
+// [0, end_bit).  Data ping-pongs between (k0,v0) and (k1,v1); *in_alt tells
+// where the result is.  If iota_vals, the values of the first pass are the
+// positions 0..n-1 (v0 is not read).  Stable.
+cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int64_t n, int end_bit,
+                       bool iota_vals, void* temp, size_t temp_bytes, cudaStream_t s, bool* in_alt,
+                       int64_t* launches);
+
+// Exclusive scan of n uint32 (in place allowed); *total (device) gets the sum
+// when non-null.
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total,
+                               void* temp, size_t temp_bytes, cudaStream_t s, int64_t* launches);
+
+}  // namespace owm

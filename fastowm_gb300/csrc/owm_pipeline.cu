@@ -1,0 +1,190 @@
+// The whole OWM path of one cloud on the device, as the reference driver
+// runs it per loop iteration (CPP-TBB-CPU/application/owm_optim3.cpp:77-230):
+// tree build, stage 1, sort + stage 2, LLP grid + stage 3, and the result
+// (stage-3 ids followed by the LLPs).  Intermediates never leave the device;
+// the host sees two small count words and the final seed list.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "owm_ctx.cuh"
+
+namespace owm {
+
+namespace {
+
+__global__ void k_bbox(const double* __restrict__ xyz, int64_t n, long long* __restrict__ out) {
+  long long x0 = 0x7FFFFFFFFFFFFFFFll, y0 = 0x7FFFFFFFFFFFFFFFll;
+  long long x1 = (long long)0x8000000000000000ull, y1 = (long long)0x8000000000000000ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    long long x = dkey(xyz[3 * i]), y = dkey(xyz[3 * i + 1]);
+    x0 = min(x0, x);
+    x1 = max(x1, x);
+    y0 = min(y0, y);
+    y1 = max(y1, y);
+  }
+  for (int o = 16; o >= 1; o >>= 1) {
+    x0 = min(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+    x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+    y0 = min(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+    y1 = max(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(out + 0, x0);
+    atomicMin(out + 1, y0);
+    atomicMax(out + 2, x1);
+    atomicMax(out + 3, y1);
+  }
+}
+
+// seeds = s3[0..ns3) ++ llp[0..nllp) as int64 ids (-1 never occurs here).
+__global__ void k_assemble(const uint32_t* __restrict__ s3, const uint32_t* __restrict__ ns3,
+                           const uint32_t* __restrict__ llp, const uint32_t* __restrict__ nllp, int64_t cap,
+                           int64_t* __restrict__ seeds) {
+  const int64_t a = *ns3, b = *nllp;
+  const int64_t tot = min(a + b, cap);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x)
+    seeds[i] = i < a ? (int64_t)s3[i] : (int64_t)llp[i - a];
+}
+
+size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int clear_status(owm_ctx* c) {
+  OWM_CUDA_TRY(cudaMemsetAsync(c->d_small + kStatusSlot, 0, 4, c->stream));
+  return OWM_OK;
+}
+
+int check_input_status(owm_ctx* c) {
+  OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small + kStatusSlot, c->d_small + kStatusSlot, 4, cudaMemcpyDeviceToHost,
+                               c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return (c->h_small[kStatusSlot] & 1u) ? OWM_EINVAL : OWM_OK;
+}
+
+int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out) {
+  long long init[4] = {0x7FFFFFFFFFFFFFFFll, 0x7FFFFFFFFFFFFFFFll, (long long)0x8000000000000000ull,
+                       (long long)0x8000000000000000ull};
+  long long* d = reinterpret_cast<long long*>(c->d_small + kBboxSlot);
+  long long* h = reinterpret_cast<long long*>(c->h_small + kBboxSlot);
+  std::memcpy(h, init, sizeof(init));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d, h, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+  int64_t g = std::min<int64_t>((n + 255) / 256, 152 * 8);
+  k_bbox<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, c->stream>>>(d_xyz, n, d);
+  count_launch(&c->launches);
+  OWM_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(init), cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  out->min_x = dkey_inv(h[0]);
+  out->min_y = dkey_inv(h[1]);
+  out->max_x = dkey_inv(h[2]);
+  out->max_y = dkey_inv(h[3]);
+  return OWM_OK;
+}
+
+int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Edge* ey, uint32_t* d_win) {
+  int rc = compute_edges(p, t.ox, t.oy, false, ex, ey, c->stream, &c->launches);
+  if (rc) return rc;
+  QueryJob j;
+  j.tree = t.view();
+  j.ex = ex;
+  j.ey = ey;
+  j.ncols = (int32_t)p.ncols;
+  j.nrows = (int32_t)p.nrows;
+  j.thr = p.min_num_points;
+  j.cell_order = 0;
+  j.skip = nullptr;
+  j.out = d_win;
+  j.warp_begin = 0;
+  return run_query(j, c->d_job, c->stream, &c->launches);
+}
+
+int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+                 int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
+  if (validate_tree_cfg(&cfg.tree) != OWM_OK) return OWM_EINVAL;
+  owm_params p;
+  int rc = owm_params_compute(&bb, n, cfg.wsize, cfg.overlap, cfg.bsize, &p);
+  if (rc) return rc;
+  const int64_t nc = p.ncells, ng = std::max<int64_t>(p.ngrid, 0);
+  rc = tree_alloc(&c->tree, &c->tree_mem, n, cfg.tree, c->stream);
+  if (rc) return rc;
+  size_t sbytes = std::max(tree_scratch_bytes(n), std::max(stage2_scratch_bytes(nc), stage3_scratch_bytes(ng)));
+  rc = c->scratch.reserve(sbytes, c->stream);
+  if (rc) return rc;
+  size_t obytes = 2 * al(65536 * sizeof(Edge)) + 2 * al((size_t)nc * 4) + al((size_t)std::max<int64_t>(ng, 1) * 4) +
+                  al((size_t)(nc + ng + 1) * 8) + 1024;
+  rc = c->outbuf.reserve(obytes, c->stream);
+  if (rc) return rc;
+  char* op = static_cast<char*>(c->outbuf.ptr);
+  auto take = [&](size_t b) {
+    void* q = op;
+    op += al(b);
+    return q;
+  };
+  Edge* ex = (Edge*)take(65536 * sizeof(Edge));
+  Edge* ey = (Edge*)take(65536 * sizeof(Edge));
+  uint32_t* win = (uint32_t*)take((size_t)nc * 4);
+  uint32_t* llp = (uint32_t*)take((size_t)nc * 4);
+  uint32_t* s3 = (uint32_t*)take((size_t)std::max<int64_t>(ng, 1) * 4);
+  int64_t* s64 = (int64_t*)take((size_t)(nc + ng + 1) * 8);
+  uint32_t* d_nllp = c->d_small + kLlpSlot;
+  uint32_t* d_ns3 = c->d_small + kS3Slot;
+
+  cudaStream_t s = c->stream;
+  OWM_CUDA_TRY(cudaEventRecord(c->ev[0], s));
+  rc = clear_status(c);
+  if (!rc)
+    rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, c->scratch.cap, c->d_small + kStatusSlot, s,
+                    &c->launches);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaEventRecord(c->ev[1], s));
+  rc = run_stage1(c, c->tree, p, ex, ey, win);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaEventRecord(c->ev[2], s));
+  rc = run_stage2(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
+  rc = run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, c->scratch.ptr, c->scratch.cap, c->d_job, s,
+                  &c->launches);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));
+  const int64_t room = nc + ng + 1;
+  k_assemble<<<(unsigned)std::min<int64_t>((room + 255) / 256, 152 * 8), 256, 0, s>>>(s3, d_ns3, llp, d_nllp, room,
+                                                                                       s64);
+  count_launch(&c->launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small, 32, cudaMemcpyDeviceToHost, s));
+  OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (c->h_small[kStatusSlot] & 1u) return OWM_EINVAL;
+  const int64_t nllp = c->h_small[kLlpSlot], ns3 = c->h_small[kS3Slot];
+  const int64_t total = nllp + ns3;
+  *n_seeds = total;
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    info->n_llp = nllp;
+    info->n_stage3 = ns3;
+    info->n_seeds = total;
+    info->params = p;
+  }
+  if (total > cap) return OWM_ERANGE;
+  if (total > 0) OWM_CUDA_TRY(cudaMemcpyAsync(seeds, s64, (size_t)total * 8, cudaMemcpyDefault, s));
+  OWM_CUDA_TRY(cudaEventRecord(c->ev[5], s));
+  OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (info) {
+    float a = 0, b = 0, d = 0, e = 0, f = 0;
+    cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&d, c->ev[2], c->ev[3]);
+    cudaEventElapsedTime(&e, c->ev[3], c->ev[4]);
+    cudaEventElapsedTime(&f, c->ev[0], c->ev[5]);
+    info->ms_tree = a;
+    info->ms_stage1 = b;
+    info->ms_stage2 = d;
+    info->ms_stage3 = e;
+    info->ms_total = f;
+  }
+  return OWM_OK;
+}
+
+}  // namespace owm

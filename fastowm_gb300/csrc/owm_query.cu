@@ -1,0 +1,485 @@
+// OWM stages on the device.
+//
+// Stage 1 / stage 3 boxes (reference: stage1, optim3_func.cpp:541-561, and
+// stage3, :627-662) are answered by one traversal kernel:
+//   * one thread owns one box; a warp owns a 4 x 8 patch of neighbouring
+//     boxes, so its lanes walk nearly the same nodes (broadcast loads);
+//   * the walk is stackless (escape links) and runs in two phases:
+//       A  nodes strictly inside the box give their memoised count and
+//          (z, id)-min at once (the reference's O3 memo); partial leaves are
+//          left for later;
+//       B  partial nodes are revisited only while they can still matter:
+//          once the count reached the threshold, a node whose memoised min is
+//          not below the current best is skipped (min-z pruning); a partial
+//          leaf whose min point lies inside the box needs no scan for the
+//          min (optim3_func.cpp:437-445);
+//   * remaining leaf scans are done by the whole warp together: 32 lanes
+//     test 32 points of one lane's leaf and a shuffle reduction hands the
+//     count and the (z, id)-min back to the owner.
+// All point tests are strict and run on exact int64 keys of the FP64
+// coordinates; node tests run on outward-rounded float boxes and only decide
+// "inside"/"outside" when that is certain.
+//
+// Stage 2 (owm_optim3.cpp:160,173; optim3_func.cpp:610-625): radix sort of
+// the window results, then ids with run length >= 2, ascending.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "owm_query.cuh"
+
+namespace owm {
+
+namespace {
+
+constexpr int kQBlock = 128;
+
+__device__ __forceinline__ Edge make_edge(double lo, double hi, double o) {
+  Edge e;
+  e.lo_k = dkey(lo);
+  e.hi_k = dkey(hi);
+  e.lo_dn = __double2float_rd(__dsub_rd(lo, o));
+  e.lo_up = __double2float_ru(__dsub_ru(lo, o));
+  e.hi_dn = __double2float_rd(__dsub_rd(hi, o));
+  e.hi_up = __double2float_ru(__dsub_ru(hi, o));
+  return e;
+}
+
+// Stage-1 windows (optim3_func.cpp:544-555, makeBox :318-324):
+//   init = (min - (double)(Wsize/2)) + Displace;  c = init + i*Displace;
+//   box  = c -/+ (double)(float)(Wsize/2)
+// Stage-3 cells (optim3_func.cpp:630-651, makeBox :310-316):
+//   init = min + (double)(Bsize/2);  c = init + (double)(i*Bsize);
+//   box  = c -/+ (double)(float)(Bsize/2)
+// Every operation is a separately rounded IEEE op (no contraction).
+__global__ void k_edges(double min_x, double min_y, double step, int32_t half, int cells, int32_t ncols,
+                        int32_t nrows, int32_t bsize, double ox, double oy, Edge* __restrict__ ex,
+                        Edge* __restrict__ ey) {
+  int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  double r = (double)(float)half;
+  if (t < ncols) {
+    double c;
+    if (cells) {
+      double init = __dadd_rn(min_x, (double)half);
+      c = __dadd_rn(init, (double)(t * bsize));
+    } else {
+      double init = __dadd_rn(__dsub_rn(min_x, (double)half), step);
+      c = __dadd_rn(init, __dmul_rn((double)t, step));
+    }
+    ex[t] = make_edge(__dsub_rn(c, r), __dadd_rn(c, r), ox);
+  }
+  if (t < nrows) {
+    double c;
+    if (cells) {
+      double init = __dadd_rn(min_y, (double)half);
+      c = __dadd_rn(init, (double)(t * bsize));
+    } else {
+      double init = __dadd_rn(__dsub_rn(min_y, (double)half), step);
+      c = __dadd_rn(init, __dmul_rn((double)t, step));
+    }
+    ey[t] = make_edge(__dsub_rn(c, r), __dadd_rn(c, r), oy);
+  }
+}
+
+__device__ __forceinline__ int find_job(const QueryJob* __restrict__ jobs, int32_t njobs, int64_t warp) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&jobs[mid].warp_begin) <= warp) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int64_t shfl64(int64_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+__global__ void __launch_bounds__(kQBlock) k_query(const QueryJob* __restrict__ jobs, int32_t njobs,
+                                                   int64_t total_warps) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * kQBlock + threadIdx.x) >> 5;
+  if (warp >= total_warps) return;  // warp-uniform
+  const QueryJob& J = jobs[njobs > 1 ? find_job(jobs, njobs, warp) : 0];
+  const TreeView T = J.tree;
+  const int64_t lw = warp - J.warp_begin;
+  const int32_t gx = (J.ncols + 3) >> 2;
+  const int32_t ii = (int32_t)(lw % gx) * 4 + (lane & 3);
+  const int32_t jj = (int32_t)(lw / gx) * 8 + (lane >> 2);
+  bool active = ii < J.ncols && jj < J.nrows;
+  int64_t oidx = 0;
+  Edge ex, ey;
+  if (active) {
+    oidx = J.cell_order ? (int64_t)jj * J.ncols + ii : (int64_t)ii * J.nrows + jj;
+    ex = J.ex[ii];
+    ey = J.ey[jj];
+    if (J.skip && J.skip[oidx]) {
+      J.out[oidx] = kNone;
+      active = false;
+    }
+  } else {
+    ex.lo_k = ex.hi_k = ey.lo_k = ey.hi_k = 0;
+  }
+  const uint32_t thr = J.thr;
+  const int32_t first_leaf = T.nleaves - 1;
+  int64_t bz = kZSentinel;
+  uint32_t bid = 0, cnt = 0;
+  int phase = 0;
+  int32_t nodei = active ? T.root : kEnd;
+  bool done = !active;
+  int32_t scan_leaf = -1;
+
+  for (;;) {
+    int steps = 0;
+    while (!done && scan_leaf < 0 && steps < 64) {
+      ++steps;
+      if (nodei == kEnd) {
+        if (phase == 0) {
+          phase = 1;
+          nodei = T.root;
+          continue;
+        }
+        done = true;
+        break;
+      }
+      // 48-byte node = three aligned 16-byte words:
+      //   [x0 y0 x1 y1] [zmin.lo zmin.hi min_id min_pos] [count left escape right]
+      const uint4* np = reinterpret_cast<const uint4*>(T.nodes + nodei);
+      const float4 b = __ldg(reinterpret_cast<const float4*>(np));
+      const uint4 mw = __ldg(np + 1);
+      const uint4 cw = __ldg(np + 2);
+      const int64_t nz = (int64_t)(((uint64_t)mw.y << 32) | mw.x);
+      const uint32_t nid = mw.z, npos = mw.w, ncount = cw.x;
+      const int32_t nleft = (int32_t)cw.y, esc = (int32_t)cw.z;
+      const bool out = b.z <= ex.lo_dn || b.x >= ex.hi_up || b.w <= ey.lo_dn || b.y >= ey.hi_up;
+      const bool in = !out && b.x > ex.lo_up && b.z < ex.hi_dn && b.y > ey.lo_up && b.w < ey.hi_dn;
+      const bool leaf = nodei >= first_leaf;
+      const bool improve = zid_less(nz, nid, bz, bid);
+      if (phase == 0) {
+        if (in) {
+          cnt += ncount;
+          if (improve) {
+            bz = nz;
+            bid = nid;
+          }
+          nodei = esc;
+        } else if (out || leaf || (cnt >= thr && !improve)) {
+          nodei = esc;
+        } else {
+          nodei = nleft;
+        }
+      } else {
+        if (in || out || (cnt >= thr && !improve)) {
+          nodei = esc;
+        } else if (!leaf) {
+          nodei = nleft;
+        } else {
+          bool min_inside = false;
+          if (improve) {
+            int64_t mx = __ldg(T.xk + npos), my = __ldg(T.yk + npos);
+            min_inside = mx > ex.lo_k && mx < ex.hi_k && my > ey.lo_k && my < ey.hi_k;
+            if (min_inside) {
+              bz = nz;
+              bid = nid;
+            }
+          }
+          if (cnt < thr || (improve && !min_inside)) scan_leaf = nodei;
+          nodei = esc;
+        }
+      }
+    }
+    uint32_t want = __ballot_sync(0xffffffffu, scan_leaf >= 0);
+    if (want == 0) {
+      if (__all_sync(0xffffffffu, done)) break;
+      continue;
+    }
+    while (want) {
+      const int src = __ffs(want) - 1;
+      want &= want - 1;
+      const int32_t leafi = __shfl_sync(0xffffffffu, scan_leaf, src);
+      const int64_t lx = shfl64(ex.lo_k, src), hx = shfl64(ex.hi_k, src);
+      const int64_t ly = shfl64(ey.lo_k, src), hy = shfl64(ey.hi_k, src);
+      const Node* np = T.nodes + leafi;
+      const int32_t first = __ldg(&np->left);
+      const uint32_t c = __ldg(&np->count);
+      uint32_t in_cnt = 0;
+      int64_t mz = 0x7FFFFFFFFFFFFFFFll;
+      uint32_t mid = 0xFFFFFFFFu;
+      for (uint32_t o = 0; o < c; o += 32) {
+        bool inside = false;
+        if (o + lane < c) {
+          const int64_t p = (int64_t)first + o + lane;
+          const int64_t x = __ldg(T.xk + p), y = __ldg(T.yk + p);
+          inside = x > lx && x < hx && y > ly && y < hy;
+          if (inside) {
+            const int64_t z = __ldg(T.zk + p);
+            const uint32_t id = __ldg(T.pid + p);
+            if (zid_less(z, id, mz, mid)) {
+              mz = z;
+              mid = id;
+            }
+          }
+        }
+        in_cnt += __popc(__ballot_sync(0xffffffffu, inside));
+      }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        int64_t z2 = shfl64(mz, lane ^ o);
+        uint32_t i2 = __shfl_xor_sync(0xffffffffu, mid, o);
+        if (zid_less(z2, i2, mz, mid)) {
+          mz = z2;
+          mid = i2;
+        }
+      }
+      if (lane == src) {
+        cnt += in_cnt;
+        if (zid_less(mz, mid, bz, bid)) {
+          bz = mz;
+          bid = mid;
+        }
+        scan_leaf = -1;
+      }
+    }
+  }
+  if (active) J.out[oidx] = cnt >= thr ? bid : kNone;
+}
+
+// ---- stage 2 -----------------------------------------------------------------
+__global__ void k_s2_keys(const uint32_t* __restrict__ win, int64_t n, uint32_t none_key, uint32_t* __restrict__ keys) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t v = win[i];
+    keys[i] = v == kNone ? none_key : v;
+  }
+}
+
+// Sorted keys -> flag of the first element of every run of length >= 2
+// (overlap > 0), or of every valid run (overlap == 0).
+__global__ void k_s2_flags(const uint32_t* __restrict__ keys, int64_t n, uint32_t none_key, int need_dup,
+                           uint32_t* __restrict__ flags) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t k = keys[i];
+    bool f = k != none_key && (i == 0 || keys[i - 1] != k);
+    if (need_dup) f = f && (i + 1 < n && keys[i + 1] == k);
+    flags[i] = f ? 1u : 0u;
+  }
+}
+
+__global__ void k_compact(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ flags,
+                          const uint32_t* __restrict__ pos, int64_t n, uint32_t* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (flags[i]) out[pos[i]] = vals[i];
+}
+
+__global__ void k_flag_valid(const uint32_t* __restrict__ v, int64_t n, uint32_t* __restrict__ flags) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    flags[i] = v[i] != kNone ? 1u : 0u;
+}
+
+// ---- stage 3 -----------------------------------------------------------------
+// LLP grid (owm_optim3.cpp:192-197 + countNeighbors, optim3_func.cpp:503-539):
+// a cell is occupied when an LLP lies strictly inside its box.
+__global__ void k_s3_mark(const double* __restrict__ xyz, const uint32_t* __restrict__ llp,
+                          const uint32_t* __restrict__ nllp, int64_t cap, const Edge* __restrict__ ex,
+                          const Edge* __restrict__ ey, int32_t ncols, int32_t nrows, double min_x, double min_y,
+                          double bsize, uint8_t* __restrict__ mark) {
+  const int64_t n = min((int64_t)*nllp, cap);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t id = llp[k];
+    double x = 0.0, y = 0.0;  // id 0 is the sentinel point {0, 0, DBL_MAX}
+    if (id > 0) {
+      x = xyz[3 * (int64_t)(id - 1)];
+      y = xyz[3 * (int64_t)(id - 1) + 1];
+    }
+    const int64_t xk = dkey(x), yk = dkey(y);
+    // candidate cells around floor((v - min)/B); the exact test decides
+    double fi = floor((x - min_x) / bsize), fj = floor((y - min_y) / bsize);
+    if (!(fi > -4.0 && fi < (double)ncols + 4.0 && fj > -4.0 && fj < (double)nrows + 4.0)) continue;
+    int32_t ic = (int32_t)fi, jc = (int32_t)fj;
+    for (int32_t jj = max(jc - 1, 0); jj <= min(jc + 1, nrows - 1); ++jj) {
+      if (!(yk > ey[jj].lo_k && yk < ey[jj].hi_k)) continue;
+      for (int32_t ii = max(ic - 1, 0); ii <= min(ic + 1, ncols - 1); ++ii)
+        if (xk > ex[ii].lo_k && xk < ex[ii].hi_k) mark[(int64_t)jj * ncols + ii] = 1;
+    }
+  }
+}
+
+__global__ void k_u32_to_i64(const uint32_t* __restrict__ in, const uint32_t* __restrict__ count, int64_t cap,
+                             int64_t* __restrict__ out) {
+  const int64_t n = count ? min((int64_t)*count, cap) : cap;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t v = in[i];
+    out[i] = v == kNone ? -1 : (int64_t)v;
+  }
+}
+
+__global__ void k_i64_to_u32(const int64_t* __restrict__ in, int64_t n, uint32_t* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t v = in[i];
+    out[i] = (v < 0 || v >= (int64_t)kNone) ? kNone : (uint32_t)v;
+  }
+}
+
+int grid1d(int64_t n, int block = 256) {
+  int64_t g = (n + block - 1) / block;
+  if (g > 152 * 32) g = 152 * 32;
+  return (int)std::max<int64_t>(g, 1);
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int compute_edges(const owm_params& p, double ox, double oy, bool cells, Edge* d_ex, Edge* d_ey, cudaStream_t s,
+                  int64_t* launches) {
+  int32_t nc = cells ? (int32_t)p.ncols_grid : (int32_t)p.ncols;
+  int32_t nr = cells ? (int32_t)p.nrows_grid : (int32_t)p.nrows;
+  int32_t m = std::max(nc, nr);
+  if (m <= 0) return OWM_OK;
+  uint16_t w16 = (uint16_t)p.wsize, b16 = (uint16_t)p.bsize;
+  int32_t half = cells ? b16 / 2 : w16 / 2;  // integer division of a ushort
+  double step = p.displace;
+  k_edges<<<(m + 127) / 128, 128, 0, s>>>(p.bbox.min_x, p.bbox.min_y, step, half, cells ? 1 : 0, nc, nr, (int32_t)b16,
+                                         ox, oy, d_ex, d_ey);
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int64_t job_warps(int32_t ncols, int32_t nrows) {
+  if (ncols <= 0 || nrows <= 0) return 0;
+  return (int64_t)((ncols + 3) / 4) * ((nrows + 7) / 8);
+}
+
+int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches) {
+  if (total_warps <= 0) return OWM_OK;
+  int64_t blocks = (total_warps * 32 + kQBlock - 1) / kQBlock;
+  k_query<<<(unsigned)blocks, kQBlock, 0, s>>>(d_jobs, njobs, total_warps);
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches) {
+  QueryJob j = job;
+  j.warp_begin = 0;
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_job_slot, &j, sizeof(QueryJob), cudaMemcpyHostToDevice, s));
+  return launch_query(d_job_slot, 1, job_warps(j.ncols, j.nrows), s, launches);
+}
+
+size_t stage2_scratch_bytes(int64_t n) {
+  return 4 * align256((size_t)n * 4) + align256(radix_sort_temp_bytes(n)) + align256(scan_temp_bytes(n)) + 1024;
+}
+
+int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
+               uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches) {
+  if (n <= 0) {
+    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+    return OWM_OK;
+  }
+  if (scratch_bytes < stage2_scratch_bytes(n)) return OWM_ENOMEM;
+  char* sp = static_cast<char*>(scratch);
+  auto take = [&](size_t b) {
+    void* p = sp;
+    sp += align256(b);
+    return p;
+  };
+  uint32_t* k0 = (uint32_t*)take((size_t)n * 4);
+  uint32_t* k1 = (uint32_t*)take((size_t)n * 4);
+  uint32_t* flags = (uint32_t*)take((size_t)n * 4);
+  uint32_t* pos = (uint32_t*)take((size_t)n * 4);
+  size_t sb = radix_sort_temp_bytes(n);
+  void* st = take(sb);
+  size_t cb = scan_temp_bytes(n);
+  void* ct = take(cb);
+  // ids are <= npoints < none_key, so `bits` key bits order them with "none" last
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)npoints + 1) ++bits;
+  uint32_t none_key = bits >= 32 ? 0xFFFFFFFFu : (uint32_t)(((uint64_t)1 << bits) - 1);
+  k_s2_keys<<<grid1d(n), 256, 0, s>>>(d_win, n, none_key, k0);
+  count_launch(launches);
+  bool alt = false;
+  OWM_CUDA_TRY(radix_sort(k0, nullptr, k1, nullptr, n, bits, false, st, sb, s, &alt, launches));
+  const uint32_t* sk = alt ? k1 : k0;
+  k_s2_flags<<<grid1d(n), 256, 0, s>>>(sk, n, none_key, overlap > 0.0 ? 1 : 0, flags);
+  count_launch(launches);
+  OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, n, d_count, ct, cb, s, launches));
+  k_compact<<<grid1d(n), 256, 0, s>>>(sk, flags, pos, n, d_llp);
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+size_t stage3_scratch_bytes(int64_t ngrid) {
+  int64_t m = std::max<int64_t>(ngrid, 1);
+  return align256((size_t)m) + 3 * align256((size_t)m * 4) + 2 * align256((size_t)65536 * sizeof(Edge)) +
+         align256(scan_temp_bytes(m)) + 1024;
+}
+
+int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
+               const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
+               size_t scratch_bytes, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches) {
+  int64_t ng = p.ngrid;
+  if (p.bsize == 0 || ng <= 0) {
+    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+    return OWM_OK;
+  }
+  if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
+  char* sp = static_cast<char*>(scratch);
+  auto take = [&](size_t b) {
+    void* q = sp;
+    sp += align256(b);
+    return q;
+  };
+  uint8_t* mark = (uint8_t*)take((size_t)ng);
+  uint32_t* cellmin = (uint32_t*)take((size_t)ng * 4);
+  uint32_t* flags = (uint32_t*)take((size_t)ng * 4);
+  uint32_t* pos = (uint32_t*)take((size_t)ng * 4);
+  Edge* ex = (Edge*)take((size_t)65536 * sizeof(Edge));
+  Edge* ey = (Edge*)take((size_t)65536 * sizeof(Edge));
+  size_t cb = scan_temp_bytes(ng);
+  void* ct = take(cb);
+  int rc = compute_edges(p, t.ox, t.oy, true, ex, ey, s, launches);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaMemsetAsync(mark, 0, (size_t)ng, s));
+  if (llp_cap > 0) {
+    k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, ex, ey, (int32_t)p.ncols_grid,
+                                             (int32_t)p.nrows_grid, p.bbox.min_x, p.bbox.min_y, (double)p.bsize, mark);
+    count_launch(launches);
+  }
+  QueryJob j;
+  j.tree = t;
+  j.ex = ex;
+  j.ey = ey;
+  j.ncols = (int32_t)p.ncols_grid;
+  j.nrows = (int32_t)p.nrows_grid;
+  j.thr = 1;
+  j.cell_order = 1;
+  j.skip = mark;
+  j.out = cellmin;
+  j.warp_begin = 0;
+  rc = run_query(j, d_job_slot, s, launches);
+  if (rc) return rc;
+  k_flag_valid<<<grid1d(ng), 256, 0, s>>>(cellmin, ng, flags);
+  count_launch(launches);
+  OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, ng, d_count, ct, cb, s, launches));
+  k_compact<<<grid1d(ng), 256, 0, s>>>(cellmin, flags, pos, ng, d_out);
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int u32_to_i64_ids(const uint32_t* in, const uint32_t* d_count, int64_t cap, int64_t* out, cudaStream_t s,
+                   int64_t* launches) {
+  if (cap <= 0) return OWM_OK;
+  k_u32_to_i64<<<grid1d(cap), 256, 0, s>>>(in, d_count, cap, out);
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int i64_to_u32_ids(const int64_t* in, int64_t n, uint32_t* out, cudaStream_t s, int64_t* launches) {
+  if (n <= 0) return OWM_OK;
+  k_i64_to_u32<<<grid1d(n), 256, 0, s>>>(in, n, out);
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+}  // namespace owm

@@ -1,0 +1,54 @@
+// Query-side entry points (stages 1-3) shared by the API, batch and server.
+#pragma once
+
+#include "owm_build.cuh"
+
+namespace owm {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;  // "no minimum" (-1) in uint32 outputs
+
+// One grid of query boxes (stage-1 windows or stage-3 cells) over one tree.
+struct QueryJob {
+  TreeView tree;
+  const Edge* ex;       // [ncols]
+  const Edge* ey;       // [nrows]
+  int32_t ncols, nrows;
+  uint32_t thr;         // minimum number of points strictly inside
+  int32_t cell_order;   // 0: out[ii*nrows + jj] (stage 1); 1: out[jj*ncols + ii]
+  const uint8_t* skip;  // optional [ncols*nrows] in out order: box not queried
+  uint32_t* out;        // id of the (z,id)-min point, or kNone
+  int64_t warp_begin;   // first warp index of this job in a multi-job launch
+};
+
+// Edge tables of the stage-1 windows (cells == false) or of the stage-3 cells
+// (cells == true) of params p, float offsets relative to (ox, oy).
+int compute_edges(const owm_params& p, double ox, double oy, bool cells, Edge* d_ex, Edge* d_ey, cudaStream_t s,
+                  int64_t* launches);
+
+// Number of warps a job needs (4 x 8 boxes per warp).
+int64_t job_warps(int32_t ncols, int32_t nrows);
+
+// Runs jobs[0..njobs) (device array) whose warp ranges tile [0, total_warps).
+int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches);
+// Single job convenience (job staged through a small device buffer).
+int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches);
+
+// Stage 2 on n uint32 window results (kNone = no min): LLPs ascending into
+// llp, their number into *d_count (device).  keys/alt/temp are scratch.
+size_t stage2_scratch_bytes(int64_t n);
+int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
+               uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
+
+// Stage 3: mark cells holding an LLP (x, y read from the input cloud), query
+// the rest, compact in cell order.  d_out gets the ids, *d_count their number.
+size_t stage3_scratch_bytes(int64_t ngrid);
+int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
+               const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
+               size_t scratch_bytes, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches);
+
+// Device kernels used by the API's conversions.
+int u32_to_i64_ids(const uint32_t* in, const uint32_t* d_count, int64_t cap, int64_t* out, cudaStream_t s,
+                   int64_t* launches);
+int i64_to_u32_ids(const int64_t* in, int64_t n, uint32_t* out, cudaStream_t s, int64_t* launches);
+
+}  // namespace owm
