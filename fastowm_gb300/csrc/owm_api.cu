@@ -322,7 +322,9 @@ int owm_stage1(owm_ctx* c, const owm_tree* tr, const owm_params* p, int64_t* win
   Edge* ey = ex + 65536;
   uint32_t* win = (uint32_t*)(ey + 65536);
   int64_t* w64 = (int64_t*)(((uintptr_t)(win + nc) + 255) & ~(uintptr_t)255);
-  rc = run_stage1(c, tr->t, *p, ex, ey, win);
+  rc = clear_status(c);
+  if (!rc) rc = run_stage1(c, tr->t, *p, ex, ey, win);
+  if (!rc) rc = check_input_status(c);
   if (rc) return rc;
   bool dev = is_device_ptr(win_min);
   rc = u32_to_i64_ids(win, nullptr, nc, dev ? win_min : w64, c->stream, &c->launches);
@@ -389,8 +391,11 @@ int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_
     rc = i64_to_u32_ids(l64, n_llp, l32, c->stream, &c->launches);
     if (rc) return rc;
   }
-  rc = run_stage3(tr->t.view(), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
-                  c->d_job, c->stream, &c->launches);
+  rc = clear_status(c);
+  if (!rc)
+    rc = run_stage3(tr->t.view(), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
+                    c->d_job, c->d_small + kStatusSlot, c->stream, &c->launches);
+  if (!rc) rc = check_input_status(c);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small + 2, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream));
   OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));

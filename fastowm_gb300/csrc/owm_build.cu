@@ -302,7 +302,8 @@ __global__ void k_refit(Node* __restrict__ nodes, const int32_t* __restrict__ pa
   int32_t li = blockIdx.x * blockDim.x + threadIdx.x;
   if (li >= nl) return;
   int32_t n = parent[nl - 1 + li];
-  while (n >= 0) {
+  // a root path has at most nl-1 internal nodes; the bound guards corruption
+  for (int32_t guard = 0; n >= 0 && guard < nl; ++guard) {
     __threadfence();
     if (atomicAdd(&flags[n], 1) == 0) return;  // sibling not done yet
     __threadfence();

@@ -61,7 +61,10 @@ int check_input_status(owm_ctx* c) {
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small + kStatusSlot, c->d_small + kStatusSlot, 4, cudaMemcpyDeviceToHost,
                                c->stream));
   OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  return (c->h_small[kStatusSlot] & 1u) ? OWM_EINVAL : OWM_OK;
+  uint32_t st = c->h_small[kStatusSlot];
+  if (st & kStatusNonFinite) return OWM_EINVAL;
+  if (st & kStatusWalkBound) return OWM_ETIMEOUT;
+  return OWM_OK;
 }
 
 int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out) {
@@ -96,6 +99,7 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   j.cell_order = 0;
   j.skip = nullptr;
   j.out = d_win;
+  j.status = c->d_small + kStatusSlot;
   j.warp_begin = 0;
   return run_query(j, c->d_job, c->stream, &c->launches);
 }
@@ -145,8 +149,8 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   rc = run_stage2(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
-  rc = run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, c->scratch.ptr, c->scratch.cap, c->d_job, s,
-                  &c->launches);
+  rc = run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, c->scratch.ptr, c->scratch.cap, c->d_job,
+                  c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));
   const int64_t room = nc + ng + 1;
@@ -156,7 +160,8 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   OWM_CUDA_TRY(cudaGetLastError());
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small, 32, cudaMemcpyDeviceToHost, s));
   OWM_CUDA_TRY(cudaStreamSynchronize(s));
-  if (c->h_small[kStatusSlot] & 1u) return OWM_EINVAL;
+  if (c->h_small[kStatusSlot] & kStatusNonFinite) return OWM_EINVAL;
+  if (c->h_small[kStatusSlot] & kStatusWalkBound) return OWM_ETIMEOUT;
   const int64_t nllp = c->h_small[kLlpSlot], ns3 = c->h_small[kS3Slot];
   const int64_t total = nllp + ns3;
   *n_seeds = total;

@@ -125,11 +125,21 @@ __global__ void __launch_bounds__(kQBlock) k_query(const QueryJob* __restrict__ 
   int32_t nodei = active ? T.root : kEnd;
   bool done = !active;
   int32_t scan_leaf = -1;
+  // A well-formed depth-first walk visits each node at most once per phase;
+  // the bound only guards against a corrupted hierarchy (then: status bit,
+  // stop, no hang).
+  const int64_t step_bound = 4 * (int64_t)T.nleaves + 16;
+  int64_t walked = 0;
 
   for (;;) {
     int steps = 0;
     while (!done && scan_leaf < 0 && steps < 64) {
       ++steps;
+      if (++walked > step_bound) {
+        atomicOr(J.status, kStatusWalkBound);
+        done = true;
+        break;
+      }
       if (nodei == kEnd) {
         if (phase == 0) {
           phase = 1;
@@ -414,7 +424,7 @@ size_t stage3_scratch_bytes(int64_t ngrid) {
 
 int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
                const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
-               size_t scratch_bytes, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches) {
+               size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches) {
   int64_t ng = p.ngrid;
   if (p.bsize == 0 || ng <= 0) {
     OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
@@ -453,6 +463,7 @@ int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, cons
   j.cell_order = 1;
   j.skip = mark;
   j.out = cellmin;
+  j.status = status;
   j.warp_begin = 0;
   rc = run_query(j, d_job_slot, s, launches);
   if (rc) return rc;

@@ -17,8 +17,13 @@ struct QueryJob {
   int32_t cell_order;   // 0: out[ii*nrows + jj] (stage 1); 1: out[jj*ncols + ii]
   const uint8_t* skip;  // optional [ncols*nrows] in out order: box not queried
   uint32_t* out;        // id of the (z,id)-min point, or kNone
+  uint32_t* status;     // device status word: kStatusWalkBound set if a walk overran
   int64_t warp_begin;   // first warp index of this job in a multi-job launch
 };
+
+// Status bits of the context's device status word.
+constexpr uint32_t kStatusNonFinite = 1u;  // non-finite input coordinate
+constexpr uint32_t kStatusWalkBound = 2u;  // a tree walk exceeded its step bound
 
 // Edge tables of the stage-1 windows (cells == false) or of the stage-3 cells
 // (cells == true) of params p, float offsets relative to (ox, oy).
@@ -44,7 +49,7 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
 size_t stage3_scratch_bytes(int64_t ngrid);
 int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
                const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
-               size_t scratch_bytes, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches);
+               size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches);
 
 // Device kernels used by the API's conversions.
 int u32_to_i64_ids(const uint32_t* in, const uint32_t* d_count, int64_t cap, int64_t* out, cudaStream_t s,
