@@ -1,0 +1,361 @@
+"""Benchmark of the OWM ground-seed path on GB300.
+
+One step = the whole path (tree build + stage 1 + stage 2 + stage 3 + seed
+copy-out) over one cloud.  Default workload: the single large cloud
+(100,000,000 FP64 points, 2 km x 2 km, Wsize 12, overlap 0.8, Bsize 20,
+leaf 32), inputs resident in HBM for `value`; `e2e` runs the same step
+through owm_run_host from pinned host memory (host->device copy of the
+points and device->host copy of the seeds inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU (torchrun): every rank runs an independent replica of the
+workload (the path has no exchange step); value = all ranks' points / max
+rank time.  --impl reference times the reference's own CPU path (compiled
+from its sources when present, else the CPU restatement) on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpts/s build+OWM (bit-exact seeds), batched vs per-tile GPU; p50/p99 tile ms"
+UNIT = "Mpts/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks / throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def rd():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(",")])
+
+        self.th = threading.Thread(target=rd, daemon=True)
+        self.th.start()
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, ws: int, device: str) -> float:
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(config: int, n_override: int | None):
+    import fastowm_gb300 as F
+
+    spec, W, Ov, B, mn, seed = F.synth_config(config)
+    if n_override:
+        # same density and terrain, smaller square area
+        dens = spec.n / ((spec.x1 - spec.x0) * (spec.y1 - spec.y0))
+        side = float(np.sqrt(n_override / dens))
+        spec.n = int(n_override)
+        spec.x1 = spec.x0 + side
+        spec.y1 = spec.y0 + side
+    return spec, W, Ov, B, mn, seed
+
+
+def kernel_bytes(name: str, n: int, p, nleaves: int) -> float | None:
+    """Algorithmic bytes per launch of the main kernels (per-unit figures x units)."""
+    if name == "k_query_s1":  # read sorted points once, node summaries, one result per window
+        return 24.0 * n + 48.0 * nleaves + 8.0 * p.ncells
+    if name.startswith("k_gather_leaves"):  # perm + xyz in, keyed points + id + leaf out
+        return (4 + 24 + 24 + 4) * n + 48.0 * nleaves
+    if name == "k_rs_downsweep":
+        return 16.0 * n
+    if name == "k_morton":
+        return 28.0 * n
+    return None
+
+
+def cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads: int):
+    """The reference's CPU path on the given sample: (Mpts/s, kind, seconds)."""
+    from oracle import oracle as O
+
+    n = xyz.shape[0]
+    if O.ref_available():
+        _, _, _, res = O.ref_run(xyz, bb, W, Ov, B, policy=1, max_number=mn, level=5, nthreads=threads,
+                                 want_win=False)
+        t = res.t_tree + res.t_owm
+        return n / t / 1e6, "reference", t
+    O.build(ref=False)
+    t0 = time.perf_counter()
+    O.run(xyz, bb, W, Ov, B, nthreads=threads)
+    t = time.perf_counter() - t0
+    return n / t / 1e6, "port", t
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import fastowm_gb300 as F
+
+    n_sample = args.cpu_sample
+    spec, W, Ov, B, mn, seed = workload(args.config, n_sample)
+    xyz, bb = F.synth_cloud(spec, seed)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads)
+    vals, secs, kind = [], [], "port"
+    for _ in range(args.steps):
+        v, kind, t = cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads)
+        vals.append(v)
+        secs.append(t)
+    tot = sum(secs)
+    value = spec.n * len(secs) / tot / 1e6
+    sample = (f"{spec.n} pts of the {args.config == 2 and '2 km x 2 km' or 'config'} workload generator at the same "
+              f"density ({spec.x1 - spec.x0:.0f} m square), W={W} O={Ov} B={B}")
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * tot / len(secs), 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"config {args.config} sample", "points": spec.n, "wsize": W, "overlap": Ov,
+                       "bsize": B, "leaf_max_number": mn},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--n", type=int, default=None, help="override point count (same density)")
+    ap.add_argument("--cpu-sample", type=int, default=16_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        barrier(ws)
+        return
+
+    import torch
+
+    import fastowm_gb300 as F
+    from fastowm_gb300 import RunInfo
+
+    torch.cuda.set_device(local)
+    spec, W, Ov, B, mn, seed = workload(args.config, args.n)
+    # pinned host buffer for the e2e leg; generated in place
+    host = torch.empty((spec.n, 3), dtype=torch.float64, pin_memory=True)
+    xyz = host.numpy()
+    xyz, bb = F.synth_cloud(spec, seed, out=xyz)
+    ctx = F.Context(local)
+    cloud = ctx.cloud(xyz, bb)
+    cfg = F.run_cfg(W, Ov, B, mn)
+    p = F.params(bb, spec.n, W, Ov, B)
+    stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
+    info = RunInfo()
+
+    for _ in range(args.warmup):
+        seeds = ctx.run(cloud, cfg, info)
+    tree_leaves = (spec.n + mn - 1) // mn
+
+    # ---- value: device-resident inputs, per-kernel events on ---------------------------------
+    clocks = Clocks(local)
+    F.lib().owm_ctx_set_profiling(ctx.handle, 1)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = ctx.launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    phase = np.zeros(4)
+    for _ in range(args.steps):
+        seeds = ctx.run(cloud, cfg, info)
+        phase += [info.ms_tree, info.ms_stage1, info.ms_stage2, info.ms_stage3]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    barrier(ws)
+    ktimes = kernel_times(F, ctx)
+    F.lib().owm_ctx_set_profiling(ctx.handle, 0)
+    ms_max = max_over_ranks(ms, ws, f"cuda:{local}")
+    value = ws * spec.n * args.steps / (ms_max / 1e3) / 1e6
+
+    # ---- e2e: pinned host points in, seeds out, through owm_run_host ---------------------------
+    e2e = None
+    if not args.no_e2e:
+        out = np.empty(p.ncells + p.ngrid + 1, dtype=np.int64)
+        for _ in range(max(1, args.warmup // 2)):
+            ctx.run_host(xyz, bb, cfg, info, out)
+        barrier(ws)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        nseed = 0
+        for _ in range(args.steps):
+            r = ctx.run_host(xyz, bb, cfg, info, out)
+            nseed = len(r)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ems = max_over_ranks(max(e0.elapsed_time(e1), 1e3 * wall), ws, f"cuda:{local}")
+        e2e = {"value": round(ws * spec.n * args.steps / (ems / 1e3) / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(spec.n * 24), "d2h_bytes_per_step": int(nseed * 8 + 32),
+               "ms_per_step": round(ems / args.steps, 3)}
+
+    # ---- roofline of the dominant kernel --------------------------------------------------------
+    peak, peak_kind = peaks()
+    roof = None
+    if ktimes:
+        name, (kms, calls) = max(ktimes.items(), key=lambda kv: kv[1][0])
+        per_launch_ms = kms / calls
+        bytes_alg = kernel_bytes(name, spec.n, p, tree_leaves)
+        achieved = bytes_alg / (per_launch_ms / 1e3) / 1e9 if bytes_alg else None
+        roof = {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,
+                "ms_per_launch": round(per_launch_ms, 4), "bytes_per_launch": bytes_alg}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        sspec, sW, sO, sB, smn, sseed = workload(args.config, args.cpu_sample)
+        sxyz, sbb = F.synth_cloud(sspec, sseed)
+        threads = os.cpu_count() or 1
+        v, kind, t = cpu_baseline_run(sxyz, sbb, sW, sO, sB, smn, threads)
+        cpu = {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{sspec.n} pts, same generator and density ({sspec.x1 - sspec.x0:.0f} m square), "
+                         f"W={sW} O={sO} B={sB}, build+OWM once ({t:.2f} s)"}
+    if rank == 0:
+        tot_k = sum(v[0] for v in ktimes.values()) or 1.0
+        line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"config {args.config}: {spec.n} FP64 points "
+                                       f"{spec.x1 - spec.x0:.0f} x {spec.y1 - spec.y0:.0f} m, plain GPU path "
+                                       f"(one cloud per launch sequence)",
+                           "wsize": W, "overlap": Ov, "bsize": B, "leaf_max_number": mn,
+                           "windows": int(p.ncells), "cells": int(p.ngrid), "seeds": int(len(seeds)),
+                           "l2": "inputs (2.4 GB at 100M points) larger than L2; no flush",
+                           "parallelism": f"replicas x{ws}"},
+                "phases_ms": {"tree": round(phase[0] / args.steps, 4), "stage1": round(phase[1] / args.steps, 4),
+                              "stage2": round(phase[2] / args.steps, 4), "stage3": round(phase[3] / args.steps, 4)},
+                "kernels": {k: {"ms": round(v[0] / args.steps, 4), "share": round(v[0] / tot_k, 4),
+                                "launches_per_step": v[1] / args.steps} for k, v in
+                            sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    cloud.close()
+    ctx.close()
+    barrier(ws)
+
+
+def kernel_times(F, ctx):
+    import ctypes as C
+
+    cap = 64
+    names = (C.c_char * 64 * cap)()
+    ms = (C.c_double * cap)()
+    calls = (C.c_int64 * cap)()
+    n = C.c_int32()
+    F.lib().owm_ctx_kernel_times(ctx.handle, cap, C.cast(names, C.c_void_p), ms, calls, C.byref(n))
+    out = {}
+    for k in range(min(n.value, cap)):
+        out[bytes(names[k]).split(b"\0")[0].decode()] = (ms[k], calls[k])
+    return out
+
+
+if __name__ == "__main__":
+    main()

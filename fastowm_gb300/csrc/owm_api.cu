@@ -38,6 +38,44 @@ void count_launch(int64_t* ctx_counter, int64_t k) {
 
 int64_t total_launches() { return g_launches.load(); }
 
+Profiler*& tls_profiler() {
+  static thread_local Profiler* p = nullptr;
+  return p;
+}
+
+cudaEvent_t Profiler::take() {
+  if (!pool.empty()) {
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void Profiler::clear() {
+  for (auto& r : recs) {
+    pool.push_back(r.a);
+    pool.push_back(r.b);
+  }
+  recs.clear();
+}
+
+void prof_begin(const char* name, cudaStream_t s) {
+  Profiler* p = tls_profiler();
+  p->pending = name;
+  p->pending_ev = p->take();
+  cudaEventRecord(p->pending_ev, s);
+}
+
+void prof_end(cudaStream_t s) {
+  Profiler* p = tls_profiler();
+  cudaEvent_t b = p->take();
+  cudaEventRecord(b, s);
+  p->recs.push_back({p->pending, p->pending_ev, b});
+}
+
 bool is_device_ptr(const void* p) {
   if (!p) return false;
   cudaPointerAttributes a;
@@ -171,6 +209,9 @@ int owm_ctx_destroy(owm_ctx* c) {
   c->input.release(c->stream);
   c->outbuf.release(c->stream);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  c->prof.clear();
+  for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
+  c->prof.pool.clear();
   if (c->d_small) cudaFree(c->d_small);
   if (c->d_job) cudaFree(c->d_job);
   if (c->h_small) cudaFreeHost(c->h_small);
@@ -200,7 +241,54 @@ int owm_ctx_device_status(owm_ctx* c, int32_t* status) {
   return OWM_OK;
 }
 
+int owm_ctx_set_profiling(owm_ctx* c, int on) {
+  if (!c) return OWM_EINVAL;
+  if (!on) {
+    cudaStreamSynchronize(c->stream);
+    c->prof.clear();
+  }
+  c->profiling = on != 0;
+  return OWM_OK;
+}
+
+int owm_ctx_kernel_times(owm_ctx* c, int32_t cap, char (*names)[64], double* ms, int64_t* calls, int32_t* n) {
+  if (!c || !n || cap < 0) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  std::vector<std::string> nm;
+  std::vector<double> tot;
+  std::vector<int64_t> cnt;
+  for (auto& r : c->prof.recs) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    size_t k = 0;
+    while (k < nm.size() && nm[k] != r.name) ++k;
+    if (k == nm.size()) {
+      nm.push_back(r.name);
+      tot.push_back(0);
+      cnt.push_back(0);
+    }
+    tot[k] += t;
+    cnt[k] += 1;
+  }
+  c->prof.clear();
+  int32_t m = (int32_t)nm.size();
+  *n = m;
+  for (int32_t k = 0; k < m && k < cap; ++k) {
+    if (names) {
+      std::strncpy(names[k], nm[k].c_str(), 63);
+      names[k][63] = 0;
+    }
+    if (ms) ms[k] = tot[k];
+    if (calls) calls[k] = cnt[k];
+  }
+  return m > cap ? OWM_ERANGE : OWM_OK;
+}
+
 int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, owm_cloud** out) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !xyz || !out || n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
   *out = nullptr;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
@@ -248,6 +336,7 @@ int owm_cloud_destroy(owm_cloud* cl) {
 int64_t owm_cloud_size(const owm_cloud* cl) { return cl ? cl->n : 0; }
 
 int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm_tree** out) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !cl || !out || validate_tree_cfg(cfg) != OWM_OK) return OWM_EINVAL;
   *out = nullptr;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
@@ -290,6 +379,7 @@ int owm_tree_get_info(owm_ctx* c, const owm_tree* tr, owm_tree_info* info) {
 }
 
 int owm_tree_check(owm_ctx* c, const owm_tree* tr) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !tr) return OWM_EINVAL;
   int32_t bad = 0;
   int rc = check_tree(&tr->t, reinterpret_cast<int32_t*>(c->d_small + kCheckSlot), c->stream, &c->launches, &bad);
@@ -311,6 +401,7 @@ int owm_tree_destroy(owm_tree* tr) {
 }
 
 int owm_stage1(owm_ctx* c, const owm_tree* tr, const owm_params* p, int64_t* win_min) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !tr || !p || !win_min || p->ncells <= 0) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
   const int64_t nc = p->ncells;
@@ -335,6 +426,7 @@ int owm_stage1(owm_ctx* c, const owm_tree* tr, const owm_params* p, int64_t* win
 }
 
 int owm_stage2(owm_ctx* c, int64_t* win_min, int64_t ncells, double overlap, int64_t* n_llp) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !win_min || !n_llp || ncells <= 0 || !(overlap >= 0.0 && overlap < 1.0) || ncells >= 0x7FFFFFFFLL)
     return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
@@ -366,6 +458,7 @@ int owm_stage2(owm_ctx* c, int64_t* win_min, int64_t ncells, double overlap, int
 
 int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_t* llp, int64_t n_llp, int64_t* out,
                int64_t cap, int64_t* n_out) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !tr || !p || (!llp && n_llp > 0) || n_llp < 0 || !n_out || (!out && cap > 0)) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
   *n_out = 0;
@@ -413,6 +506,7 @@ int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_
 
 int owm_run(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int64_t* seeds, int64_t cap, int64_t* n_seeds,
             owm_run_info* info) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !cl || !cfg || !n_seeds || (!seeds && cap > 0)) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
   return run_pipeline(c, static_cast<const double*>(cl->mem.ptr), cl->n, cl->bbox, *cfg, seeds, cap, n_seeds, info);
@@ -420,6 +514,7 @@ int owm_run(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int64_t* se
 
 int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, const owm_run_cfg* cfg,
                  int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !xyz || !cfg || !n_seeds || n <= 0 || n >= 0x7FFFFFFFLL || (!seeds && cap > 0)) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
   owm_bbox bb;

@@ -355,8 +355,8 @@ void launch_gather_leaves(const double* xyz, const uint32_t* perm, int64_t n, in
   int64_t warps = nunits;
   int64_t blocks = (warps * 32 + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_gather_leaves<L><<<(unsigned)blocks, 256, 0, s>>>(xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid,
-                                                      t->nodes + (nl - 1), status);
+  OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L><<<(unsigned)blocks, 256, 0, s>>>(xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid,
+                                                      t->nodes + (nl - 1), status));
 }
 
 }  // namespace
@@ -431,7 +431,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   t->key_bits = key_bits;
   t->n = n;
 
-  k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0);
+  OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
   count_launch(launches);
   bool alt = false;
   OWM_CUDA_TRY(radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches));
@@ -455,10 +455,10 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     int cell_shift = 2 * (bits_axis - d);
     uint32_t* fl = reinterpret_cast<uint32_t*>(flags);  // reuse as scratch, [n]
     uint32_t* sc = reinterpret_cast<uint32_t*>(parent);  // [n] + total
-    k_leaf_flags<<<grid_for(n, 256), 256, 0, s>>>(mk, n, cell_shift, fl);
+    OWM_LAUNCH("k_leaf_flags", s, k_leaf_flags<<<grid_for(n, 256), 256, 0, s>>>(mk, n, cell_shift, fl));
     count_launch(launches);
     OWM_CUDA_TRY(exclusive_scan_u32(fl, sc, n, sc + n, scan_tmp, scan_temp_bytes(n) + 64, s, launches));
-    k_leaf_starts<<<grid_for(n, 256), 256, 0, s>>>(fl, sc, n, starts);
+    OWM_LAUNCH("k_leaf_starts", s, k_leaf_starts<<<grid_for(n, 256), 256, 0, s>>>(fl, sc, n, starts));
     count_launch(launches);
     uint32_t h_nl = 0;
     OWM_CUDA_TRY(cudaMemcpyAsync(&h_nl, sc + n, 4, cudaMemcpyDeviceToHost, s));
@@ -490,21 +490,21 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     }
     count_launch(launches);
   } else {
-    k_gather<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status);
+    OWM_LAUNCH("k_gather", s, k_gather<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status));
     count_launch(launches);
     int64_t blocks = ((int64_t)nl * 32 + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_leaf_reduce<<<(unsigned)blocks, 256, 0, s>>>(t->xk, t->yk, t->zk, t->pid, lstarts, nl, t->ox, t->oy,
-                                                    t->nodes + (nl - 1));
+    OWM_LAUNCH("k_leaf_reduce", s, k_leaf_reduce<<<(unsigned)blocks, 256, 0, s>>>(t->xk, t->yk, t->zk, t->pid, lstarts, nl, t->ox, t->oy,
+                                                    t->nodes + (nl - 1)));
     count_launch(launches);
   }
 
   if (nl > 1) {
     OWM_CUDA_TRY(cudaMemsetAsync(parent, 0xFF, (size_t)nnodes * 4, s));
     OWM_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)nl * 4, s));
-    k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, t->nodes, parent, right_of, last_of);
-    k_escapes<<<(unsigned)((nnodes + 255) / 256), 256, 0, s>>>(t->nodes, right_of, last_of, nl);
-    k_refit<<<(nl + 255) / 256, 256, 0, s>>>(t->nodes, parent, flags, nl);
+    OWM_LAUNCH("k_karras", s, k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, t->nodes, parent, right_of, last_of));
+    OWM_LAUNCH("k_escapes", s, k_escapes<<<(unsigned)((nnodes + 255) / 256), 256, 0, s>>>(t->nodes, right_of, last_of, nl));
+    OWM_LAUNCH("k_refit", s, k_refit<<<(nl + 255) / 256, 256, 0, s>>>(t->nodes, parent, flags, nl));
     count_launch(launches, 3);
   }
   t->max_leaf = fixed ? L : -1;

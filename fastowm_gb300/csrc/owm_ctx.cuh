@@ -1,6 +1,8 @@
 // Context object and the whole-path pipeline shared by API, batch and server.
 #pragma once
 
+#include <vector>
+
 #include "owm_query.cuh"
 
 namespace owm {
@@ -28,7 +30,32 @@ int validate_tree_cfg(const owm_tree_cfg* cfg);
 
 }  // namespace owm
 
+namespace owm {
+// Event pairs recorded around kernels while profiling is on.
+struct Profiler {
+  struct Rec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  const char* pending = nullptr;
+  cudaEvent_t pending_ev = nullptr;
+  cudaEvent_t take();
+  void clear();
+};
+// Sets the calling thread's active profiler for one API call.
+struct ProfScope {
+  Profiler* prev;
+  explicit ProfScope(Profiler* p) : prev(tls_profiler()) { tls_profiler() = p; }
+  ~ProfScope() { tls_profiler() = prev; }
+};
+}  // namespace owm
+
 struct owm_ctx {
+  owm::Profiler prof;
+  bool profiling = false;
+  owm::Profiler* active_prof() { return profiling ? &prof : nullptr; }
   int device = 0;
   cudaStream_t stream = nullptr;
   int64_t launches = 0;

@@ -104,6 +104,21 @@ void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int 
 // goes through count_launch) and the per-context one.
 void count_launch(int64_t* ctx_counter, int64_t k = 1);
 
+// Per-kernel CUDA-event timing.  Every launch site is wrapped in OWM_LAUNCH;
+// when the calling thread has an active profiler (set for the duration of an
+// API call on a context with profiling on), an event pair is recorded on the
+// launch stream around the kernel.
+struct Profiler;
+Profiler*& tls_profiler();
+void prof_begin(const char* name, cudaStream_t s);
+void prof_end(cudaStream_t s);
+#define OWM_LAUNCH(name, stream, ...)      \
+  do {                                     \
+    if (owm::tls_profiler()) owm::prof_begin(name, stream); \
+    __VA_ARGS__;                           \
+    if (owm::tls_profiler()) owm::prof_end(stream);         \
+  } while (0)
+
 // ---------------------------------------------------------------------------
 // Primitives (owm_sort.cu).
 struct SortTemp {

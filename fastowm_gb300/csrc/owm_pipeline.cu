@@ -101,7 +101,7 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   j.out = d_win;
   j.status = c->d_small + kStatusSlot;
   j.warp_begin = 0;
-  return run_query(j, c->d_job, c->stream, &c->launches);
+  return run_query(j, c->d_job, c->stream, &c->launches, "k_query_s1");
 }
 
 int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,

@@ -345,8 +345,8 @@ int compute_edges(const owm_params& p, double ox, double oy, bool cells, Edge* d
   uint16_t w16 = (uint16_t)p.wsize, b16 = (uint16_t)p.bsize;
   int32_t half = cells ? b16 / 2 : w16 / 2;  // integer division of a ushort
   double step = p.displace;
-  k_edges<<<(m + 127) / 128, 128, 0, s>>>(p.bbox.min_x, p.bbox.min_y, step, half, cells ? 1 : 0, nc, nr, (int32_t)b16,
-                                         ox, oy, d_ex, d_ey);
+  OWM_LAUNCH("k_edges", s, k_edges<<<(m + 127) / 128, 128, 0, s>>>(p.bbox.min_x, p.bbox.min_y, step, half, cells ? 1 : 0, nc, nr, (int32_t)b16,
+                                         ox, oy, d_ex, d_ey));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
@@ -357,20 +357,21 @@ int64_t job_warps(int32_t ncols, int32_t nrows) {
   return (int64_t)((ncols + 3) / 4) * ((nrows + 7) / 8);
 }
 
-int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches) {
+int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches,
+                 const char* name) {
   if (total_warps <= 0) return OWM_OK;
   int64_t blocks = (total_warps * 32 + kQBlock - 1) / kQBlock;
-  k_query<<<(unsigned)blocks, kQBlock, 0, s>>>(d_jobs, njobs, total_warps);
+  OWM_LAUNCH(name, s, k_query<<<(unsigned)blocks, kQBlock, 0, s>>>(d_jobs, njobs, total_warps));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
 }
 
-int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches) {
+int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches, const char* name) {
   QueryJob j = job;
   j.warp_begin = 0;
   OWM_CUDA_TRY(cudaMemcpyAsync(d_job_slot, &j, sizeof(QueryJob), cudaMemcpyHostToDevice, s));
-  return launch_query(d_job_slot, 1, job_warps(j.ncols, j.nrows), s, launches);
+  return launch_query(d_job_slot, 1, job_warps(j.ncols, j.nrows), s, launches, name);
 }
 
 size_t stage2_scratch_bytes(int64_t n) {
@@ -402,15 +403,15 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
   int bits = 1;
   while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)npoints + 1) ++bits;
   uint32_t none_key = bits >= 32 ? 0xFFFFFFFFu : (uint32_t)(((uint64_t)1 << bits) - 1);
-  k_s2_keys<<<grid1d(n), 256, 0, s>>>(d_win, n, none_key, k0);
+  OWM_LAUNCH("k_s2_keys", s, k_s2_keys<<<grid1d(n), 256, 0, s>>>(d_win, n, none_key, k0));
   count_launch(launches);
   bool alt = false;
   OWM_CUDA_TRY(radix_sort(k0, nullptr, k1, nullptr, n, bits, false, st, sb, s, &alt, launches));
   const uint32_t* sk = alt ? k1 : k0;
-  k_s2_flags<<<grid1d(n), 256, 0, s>>>(sk, n, none_key, overlap > 0.0 ? 1 : 0, flags);
+  OWM_LAUNCH("k_s2_flags", s, k_s2_flags<<<grid1d(n), 256, 0, s>>>(sk, n, none_key, overlap > 0.0 ? 1 : 0, flags));
   count_launch(launches);
   OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, n, d_count, ct, cb, s, launches));
-  k_compact<<<grid1d(n), 256, 0, s>>>(sk, flags, pos, n, d_llp);
+  OWM_LAUNCH("k_compact", s, k_compact<<<grid1d(n), 256, 0, s>>>(sk, flags, pos, n, d_llp));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
@@ -449,8 +450,8 @@ int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, cons
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemsetAsync(mark, 0, (size_t)ng, s));
   if (llp_cap > 0) {
-    k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, ex, ey, (int32_t)p.ncols_grid,
-                                             (int32_t)p.nrows_grid, p.bbox.min_x, p.bbox.min_y, (double)p.bsize, mark);
+    OWM_LAUNCH("k_s3_mark", s, k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, ex, ey, (int32_t)p.ncols_grid,
+                                             (int32_t)p.nrows_grid, p.bbox.min_x, p.bbox.min_y, (double)p.bsize, mark));
     count_launch(launches);
   }
   QueryJob j;
@@ -465,12 +466,12 @@ int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, cons
   j.out = cellmin;
   j.status = status;
   j.warp_begin = 0;
-  rc = run_query(j, d_job_slot, s, launches);
+  rc = run_query(j, d_job_slot, s, launches, "k_query_s3");
   if (rc) return rc;
-  k_flag_valid<<<grid1d(ng), 256, 0, s>>>(cellmin, ng, flags);
+  OWM_LAUNCH("k_flag_valid", s, k_flag_valid<<<grid1d(ng), 256, 0, s>>>(cellmin, ng, flags));
   count_launch(launches);
   OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, ng, d_count, ct, cb, s, launches));
-  k_compact<<<grid1d(ng), 256, 0, s>>>(cellmin, flags, pos, ng, d_out);
+  OWM_LAUNCH("k_compact", s, k_compact<<<grid1d(ng), 256, 0, s>>>(cellmin, flags, pos, ng, d_out));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
@@ -479,7 +480,7 @@ int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, cons
 int u32_to_i64_ids(const uint32_t* in, const uint32_t* d_count, int64_t cap, int64_t* out, cudaStream_t s,
                    int64_t* launches) {
   if (cap <= 0) return OWM_OK;
-  k_u32_to_i64<<<grid1d(cap), 256, 0, s>>>(in, d_count, cap, out);
+  OWM_LAUNCH("k_u32_to_i64", s, k_u32_to_i64<<<grid1d(cap), 256, 0, s>>>(in, d_count, cap, out));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
@@ -487,7 +488,7 @@ int u32_to_i64_ids(const uint32_t* in, const uint32_t* d_count, int64_t cap, int
 
 int i64_to_u32_ids(const int64_t* in, int64_t n, uint32_t* out, cudaStream_t s, int64_t* launches) {
   if (n <= 0) return OWM_OK;
-  k_i64_to_u32<<<grid1d(n), 256, 0, s>>>(in, n, out);
+  OWM_LAUNCH("k_i64_to_u32", s, k_i64_to_u32<<<grid1d(n), 256, 0, s>>>(in, n, out));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;

@@ -34,9 +34,11 @@ int compute_edges(const owm_params& p, double ox, double oy, bool cells, Edge* d
 int64_t job_warps(int32_t ncols, int32_t nrows);
 
 // Runs jobs[0..njobs) (device array) whose warp ranges tile [0, total_warps).
-int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches);
+// `name` labels the launch for the per-kernel profiler.
+int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches,
+                 const char* name);
 // Single job convenience (job staged through a small device buffer).
-int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches);
+int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches, const char* name);
 
 // Stage 2 on n uint32 window results (kNone = no min): LLPs ascending into
 // llp, their number into *d_count (device).  keys/alt/temp are scratch.

@@ -249,9 +249,9 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
   int64_t parts = (n + kScanChunk - 1) / kScanChunk;
   if (parts > (int64_t)kScanChunk || temp_bytes < scan_temp_bytes(n)) return cudaErrorInvalidValue;
   uint32_t* part = static_cast<uint32_t*>(temp);
-  k_scan_reduce<<<(unsigned)parts, kScanBlock, 0, s>>>(in, n, part);
-  k_scan_parts<<<1, kScanBlock, 0, s>>>(part, parts, total);
-  k_scan_down<<<(unsigned)parts, kScanBlock, 0, s>>>(in, out, n, part);
+  OWM_LAUNCH("k_scan_reduce", s, k_scan_reduce<<<(unsigned)parts, kScanBlock, 0, s>>>(in, n, part));
+  OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(part, parts, total));
+  OWM_LAUNCH("k_scan_down", s, k_scan_down<<<(unsigned)parts, kScanBlock, 0, s>>>(in, out, n, part));
   count_launch(launches, 3);
   return cudaGetLastError();
 }
@@ -273,16 +273,16 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   bool alt = false;
   bool first = true;
   for (int shift = 0; shift < end_bit; shift += 8) {
-    k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, hist, ntiles);
+    OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, hist, ntiles));
     cudaError_t e = exclusive_scan_u32(hist, hist, hn, nullptr, stemp, sbytes, s, launches);
     if (e != cudaSuccess) return e;
     if (has_vals) {
       if (first && iota_vals)
-        k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles);
+        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
       else
-        k_rs_downsweep<true, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles);
+        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
     } else {
-      k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles);
+      OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles));
     }
     count_launch(launches, 2);
     first = false;

@@ -128,8 +128,16 @@ int owm_ctx_sync(owm_ctx* ctx);
 void* owm_ctx_stream(owm_ctx* ctx); /* the context's cudaStream_t */
 /* Number of this library's kernel launches issued on the context so far. */
 int64_t owm_ctx_launches(const owm_ctx* ctx);
-/* Device status word of the bounded waits (0 = none expired). */
+/* Device status word: bit 0 non-finite input, bit 1 a bounded tree walk
+ * overran (corrupt hierarchy; the call returned OWM_ETIMEOUT). */
 int owm_ctx_device_status(owm_ctx* ctx, int32_t* status);
+/* Per-kernel CUDA-event timing of this context's launches (1 = on). */
+int owm_ctx_set_profiling(owm_ctx* ctx, int on);
+/* Sums the recorded kernel times by kernel name since the last call (and
+ * clears them): names[k] (NUL-terminated), total ms and launch count;
+ * *n = number of distinct kernels (OWM_ERANGE if more than cap). */
+int owm_ctx_kernel_times(owm_ctx* ctx, int32_t cap, char (*names)[64], double* ms, int64_t* calls,
+                         int32_t* n);
 
 /* ---- device cloud ------------------------------------------------------ */
 typedef struct owm_cloud owm_cloud;
