@@ -24,7 +24,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (OWM_EAGAIN, OWM_OK, OWM_TREE_MAX_NUMBER, OWM_TREE_MIN_RADIUS, Bbox, Params, RunCfg, RunInfo,
+from ._lib import (OWM_EAGAIN, OWM_OK, OWM_TREE_MAX_NUMBER, OWM_TREE_MIN_RADIUS, Bbox, Params, RunCfg, RunInfo,  # noqa: F401
                    ServerCfg, ServerStats, SynthSpec, TileDesc, TreeCfg, TreeInfo)
 
 __all__ = ["OwmError", "round2d", "params", "bbox_of", "read_xyz", "write_xyz_ids", "check_results",

@@ -75,7 +75,8 @@ int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out) {
   std::memcpy(h, init, sizeof(init));
   OWM_CUDA_TRY(cudaMemcpyAsync(d, h, sizeof(init), cudaMemcpyHostToDevice, c->stream));
   int64_t g = std::min<int64_t>((n + 255) / 256, 152 * 8);
-  k_bbox<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, c->stream>>>(d_xyz, n, d);
+  const unsigned gb = (unsigned)std::max<int64_t>(g, 1);
+  OWM_LAUNCH("k_bbox", c->stream, k_bbox<<<gb, 256, 0, c->stream>>>(d_xyz, n, d));
   count_launch(&c->launches);
   OWM_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(init), cudaMemcpyDeviceToHost, c->stream));
   OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -154,8 +155,8 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));
   const int64_t room = nc + ng + 1;
-  k_assemble<<<(unsigned)std::min<int64_t>((room + 255) / 256, 152 * 8), 256, 0, s>>>(s3, d_ns3, llp, d_nllp, room,
-                                                                                       s64);
+  const unsigned ga = (unsigned)std::min<int64_t>((room + 255) / 256, 152 * 8);
+  OWM_LAUNCH("k_assemble", s, k_assemble<<<ga, 256, 0, s>>>(s3, d_ns3, llp, d_nllp, room, s64));
   count_launch(&c->launches);
   OWM_CUDA_TRY(cudaGetLastError());
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small, 32, cudaMemcpyDeviceToHost, s));
