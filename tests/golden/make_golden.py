@@ -76,10 +76,10 @@ def run_case(name, recipe, xyz, bb, W, Ov, B, mn, policy):
         seeds, nllp, win, res = O.ref_run(xyz, bb, W, Ov, B, policy=policy, max_number=mn, nthreads=1)
         llp = np.sort(seeds[len(seeds) - nllp:])
         s3 = seeds[: len(seeds) - nllp]
-        case["reference"] = {"win_min": pack(win), "llp": pack(llp), "stage3": pack(np.sort(s3)),
+        case["reference"] = {"win_min": pack(win), "llp": pack(llp), "stage3": pack(s3),  # cell order (1 thread)
                              "n_llp": int(nllp), "n_stage3": int(len(s3)),
                              "min_num_points": int(res.min_num_points)}
-        same = np.array_equal(win, win_r) and np.array_equal(llp, llp_r) and np.array_equal(np.sort(s3), np.sort(s3_r))
+        same = np.array_equal(win, win_r) and np.array_equal(llp, llp_r) and np.array_equal(s3, s3_r)
         case["reference_equals_restatement"] = bool(same)
         print(f"{name:>14}: n={xyz.shape[0]} windows={p.ncells} llp={nllp} s3={len(s3)} ties={ties} "
               f"reference==restatement: {same}")
