@@ -20,6 +20,7 @@ there is no CPU fallback, and a missing library or device raises.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -145,21 +146,39 @@ def run_cfg(wsize: int, overlap: float, bsize: int, max_number: int = 32, policy
     return RunCfg(wsize, bsize, overlap, tree_cfg(policy, max_number, min_radius))
 
 
-class Cloud:
-    def __init__(self, ctx: "Context", handle: C.c_void_p, n: int, bbox: Bbox):
-        self.ctx, self.handle, self.n, self.bbox = ctx, handle, n, bbox
+class _Child:
+    """A device object owned by a Context: closed before the context is, and
+    never released through a context that is already gone."""
 
     def close(self):
-        if self.handle:
-            lib().owm_cloud_destroy(self.handle)
-            self.handle = None
+        h, self.handle = getattr(self, "handle", None), None
+        ctx = getattr(self, "ctx", None)
+        if h and ctx is not None and getattr(ctx, "handle", None):
+            self._destroy(h)
 
-    __del__ = close
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
-class Tree:
+class Cloud(_Child):
+    def __init__(self, ctx: "Context", handle: C.c_void_p, n: int, bbox: Bbox):
+        self.ctx, self.handle, self.n, self.bbox = ctx, handle, n, bbox
+        ctx._children.add(self)
+
+    def _destroy(self, h):
+        lib().owm_cloud_destroy(h)
+
+
+class Tree(_Child):
     def __init__(self, ctx: "Context", handle: C.c_void_p, cloud: Cloud):
         self.ctx, self.handle, self.cloud = ctx, handle, cloud  # keeps the cloud alive
+        ctx._children.add(self)
+
+    def _destroy(self, h):
+        lib().owm_tree_destroy(h)
 
     def info(self) -> TreeInfo:
         i = TreeInfo()
@@ -169,28 +188,29 @@ class Tree:
     def check(self) -> bool:
         return lib().owm_tree_check(self.ctx.handle, self.handle) == OWM_OK
 
-    def close(self):
-        if self.handle:
-            lib().owm_tree_destroy(self.handle)
-            self.handle = None
-
-    __del__ = close
-
 
 class Context:
-    """One GPU stream and its cached device buffers."""
+    """One GPU stream and its cached device buffers.  Clouds and trees made
+    from it are released before it is."""
 
     def __init__(self, device: int = 0):
+        self._children = weakref.WeakSet()
         h = C.c_void_p()
         _check(lib().owm_ctx_create(device, C.byref(h)), "ctx_create")
         self.handle = h
 
     def close(self):
         if getattr(self, "handle", None):
+            for ch in sorted(list(self._children), key=lambda o: 0 if isinstance(o, Tree) else 1):
+                ch.close()
             lib().owm_ctx_destroy(self.handle)
             self.handle = None
 
-    __del__ = close
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def sync(self):
         _check(lib().owm_ctx_sync(self.handle), "sync")

@@ -149,6 +149,7 @@ using namespace owm;
 
 struct owm_cloud {
   owm_ctx* ctx;
+  int device;  // destroy needs no context (it may already be gone)
   DeviceBuffer mem;
   int64_t n;
   owm_bbox bbox;
@@ -156,6 +157,7 @@ struct owm_cloud {
 
 struct owm_tree {
   owm_ctx* ctx;
+  int device;
   DeviceBuffer mem;
   TreeStore t;
   const double* d_xyz;  // borrowed from the cloud (stage 3 reads LLP coordinates)
@@ -306,6 +308,7 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
     return OWM_EINVAL;
   owm_cloud* cl = new owm_cloud();
   cl->ctx = c;
+  cl->device = c->device;
   cl->n = n;
   cl->bbox = bb;
   if (cl->mem.reserve((size_t)n * 24, c->stream) != OWM_OK) {
@@ -326,9 +329,9 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
 
 int owm_cloud_destroy(owm_cloud* cl) {
   if (!cl) return OWM_OK;
-  cudaSetDevice(cl->ctx->device);
-  cl->mem.release(cl->ctx->stream);
-  cudaStreamSynchronize(cl->ctx->stream);
+  cudaSetDevice(cl->device);
+  if (cl->mem.ptr) cudaFree(cl->mem.ptr);  // synchronising free; no stream or context needed
+  cudaGetLastError();
   delete cl;
   return OWM_OK;
 }
@@ -342,6 +345,7 @@ int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm
   OWM_CUDA_TRY(cudaSetDevice(c->device));
   owm_tree* tr = new owm_tree();
   tr->ctx = c;
+  tr->device = c->device;
   tr->cfg = *cfg;
   tr->d_xyz = static_cast<const double*>(cl->mem.ptr);
   tr->bbox = cl->bbox;
@@ -393,9 +397,9 @@ int owm_tree_check(owm_ctx* c, const owm_tree* tr) {
 
 int owm_tree_destroy(owm_tree* tr) {
   if (!tr) return OWM_OK;
-  cudaSetDevice(tr->ctx->device);
-  tr->mem.release(tr->ctx->stream);
-  cudaStreamSynchronize(tr->ctx->stream);
+  cudaSetDevice(tr->device);
+  if (tr->mem.ptr) cudaFree(tr->mem.ptr);
+  cudaGetLastError();
   delete tr;
   return OWM_OK;
 }

@@ -123,6 +123,7 @@ int owm_synth_cloud(const owm_synth_spec* spec, uint64_t seed, double* xyz, owm_
 /* ---- device context --------------------------------------------------- */
 typedef struct owm_ctx owm_ctx;
 int owm_ctx_create(int device, owm_ctx** out);
+/* Destroy every tree and cloud made on a context before the context. */
 int owm_ctx_destroy(owm_ctx* ctx);
 int owm_ctx_sync(owm_ctx* ctx);
 void* owm_ctx_stream(owm_ctx* ctx); /* the context's cudaStream_t */
