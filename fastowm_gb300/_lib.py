@@ -100,6 +100,7 @@ SIGNATURES = {
     "owm_stage1": (C.c_int, [vp, vp, P(Params), P(i64)]),
     "owm_stage2": (C.c_int, [vp, P(i64), i64, f64, P(i64)]),
     "owm_stage3": (C.c_int, [vp, vp, P(Params), P(i64), i64, P(i64), i64, P(i64)]),
+    "owm_stage2_noalloc": (C.c_int, [vp, vp, i64, f64, i64, vp, P(i64)]),
     "owm_run": (C.c_int, [vp, vp, P(RunCfg), P(i64), i64, P(i64), P(RunInfo)]),
     "owm_run_host": (C.c_int, [vp, P(f64), i64, P(Bbox), P(RunCfg), P(i64), i64, P(i64), P(RunInfo)]),
     "owm_batch_create": (C.c_int, [vp, P(vp)]),

@@ -125,6 +125,8 @@ struct SortTemp {
   void* ptr = nullptr;
   size_t bytes = 0;
 };
+inline size_t align256ul(size_t b) { return (b + 255) & ~(size_t)255; }
+
 // Temp bytes for sorting n keys (pairs or keys-only) and for scanning n ints.
 size_t radix_sort_temp_bytes(int64_t n);
 size_t scan_temp_bytes(int64_t n);

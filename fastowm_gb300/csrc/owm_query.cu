@@ -417,6 +417,36 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
   return OWM_OK;
 }
 
+int run_stage2_into(const uint32_t* d_win, uint32_t* k0, uint32_t* k1, uint32_t* flags, uint32_t* pos, int64_t n,
+                    int64_t npoints, double overlap, uint32_t* d_llp, uint32_t* d_count, void* temp,
+                    size_t temp_bytes, cudaStream_t s, int64_t* launches) {
+  if (n <= 0) {
+    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+    return OWM_OK;
+  }
+  size_t sb = radix_sort_temp_bytes(n);
+  size_t cb = scan_temp_bytes(n);
+  if (temp_bytes < align256(sb) + cb) return OWM_ENOMEM;
+  void* st = temp;
+  void* ct = static_cast<char*>(temp) + align256(sb);
+  // ids are <= npoints < none_key, so `bits` key bits order them with "none" last
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)npoints + 1) ++bits;
+  uint32_t none_key = bits >= 32 ? 0xFFFFFFFFu : (uint32_t)(((uint64_t)1 << bits) - 1);
+  OWM_LAUNCH("k_s2_keys", s, k_s2_keys<<<grid1d(n), 256, 0, s>>>(d_win, n, none_key, k0));
+  count_launch(launches);
+  bool alt = false;
+  OWM_CUDA_TRY(radix_sort(k0, nullptr, k1, nullptr, n, bits, false, st, sb, s, &alt, launches));
+  const uint32_t* sk = alt ? k1 : k0;
+  OWM_LAUNCH("k_s2_flags", s, k_s2_flags<<<grid1d(n), 256, 0, s>>>(sk, n, none_key, overlap > 0.0 ? 1 : 0, flags));
+  count_launch(launches);
+  OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, n, d_count, ct, cb, s, launches));
+  OWM_LAUNCH("k_compact", s, k_compact<<<grid1d(n), 256, 0, s>>>(sk, flags, pos, n, d_llp));
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
 size_t stage3_scratch_bytes(int64_t ngrid) {
   int64_t m = std::max<int64_t>(ngrid, 1);
   return align256((size_t)m) + 3 * align256((size_t)m * 4) + 2 * align256((size_t)65536 * sizeof(Edge)) +

@@ -45,6 +45,12 @@ int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t
 size_t stage2_scratch_bytes(int64_t n);
 int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
                uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
+// Same with explicit working arrays (n uint32 each; d_llp must not alias
+// them) and a temp block of radix_sort_temp_bytes(n) (256-aligned) +
+// scan_temp_bytes(n).  d_win may equal k0.
+int run_stage2_into(const uint32_t* d_win, uint32_t* k0, uint32_t* k1, uint32_t* flags, uint32_t* pos, int64_t n,
+                    int64_t npoints, double overlap, uint32_t* d_llp, uint32_t* d_count, void* temp,
+                    size_t temp_bytes, cudaStream_t s, int64_t* launches);
 
 // Stage 3: mark cells holding an LLP (x, y read from the input cloud), query
 // the rest, compact in cell order.  d_out gets the ids, *d_count their number.

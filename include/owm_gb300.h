@@ -199,6 +199,24 @@ int owm_stage2(owm_ctx* ctx, int64_t* win_min, int64_t ncells, double overlap, i
 int owm_stage3(owm_ctx* ctx, const owm_tree* tree, const owm_params* params, const int64_t* llp,
                int64_t n_llp, int64_t* out, int64_t cap, int64_t* n_out);
 
+/* Stage 2 without any device allocation.  No counterpart in the reference:
+ * it exists for callers of this library that cannot allocate device memory
+ * (a host that owns all GPU memory through its own pool, a plugin whose host
+ * forbids allocation on the streams it lends, a real-time loop where an
+ * allocation and its implicit synchronisation are not allowed).  Same
+ * result as owm_stage2 (LLPs ascending), but d_win_min (int64, -1 = none)
+ * and d_llp (room for ncells ids) are caller-owned DEVICE memory, npoints
+ * bounds the ids, and the work runs on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream), which is synchronised before *n_llp is set.
+ * Working memory is one static device array of about 21.5 MB that every
+ * GPU loading this library holds until exit; at most 1,048,576 windows per
+ * call (OWM_ERANGE above that).  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race,
+ * so serialise them. */
+int owm_stage2_noalloc(void* stream, const int64_t* d_win_min, int64_t ncells, double overlap,
+                       int64_t npoints, int64_t* d_llp, int64_t* n_llp);
+
 /* ---- whole path -------------------------------------------------------- */
 typedef struct {
   uint32_t wsize, bsize;
