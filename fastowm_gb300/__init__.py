@@ -201,7 +201,7 @@ class Context:
 
     def close(self):
         if getattr(self, "handle", None):
-            for ch in sorted(list(self._children), key=lambda o: 0 if isinstance(o, Tree) else 1):
+            for ch in sorted(list(self._children), key=lambda o: 0 if isinstance(o, (Tree, Batch)) else 1):
                 ch.close()
             lib().owm_ctx_destroy(self.handle)
             self.handle = None
@@ -280,20 +280,17 @@ class Context:
         return out[: n.value].copy()
 
 
-class Batch:
+class Batch(_Child):
     """Many tiles built and queried together (one launch per stage)."""
 
     def __init__(self, ctx: Context):
         h = C.c_void_p()
         _check(lib().owm_batch_create(ctx.handle, C.byref(h)), "batch_create")
         self.ctx, self.handle = ctx, h
+        ctx._children.add(self)
 
-    def close(self):
-        if getattr(self, "handle", None):
-            lib().owm_batch_destroy(self.handle)
-            self.handle = None
-
-    __del__ = close
+    def _destroy(self, h):
+        lib().owm_batch_destroy(h)
 
     def set_graphs(self, on: bool):
         _check(lib().owm_batch_set_graphs(self.handle, 1 if on else 0), "set_graphs")

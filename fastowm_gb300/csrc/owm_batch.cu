@@ -1,0 +1,918 @@
+// Batched tiles: many independent clouds (own bbox, Wsize, overlap, Bsize and
+// leaf size) built and queried together with one launch per step instead of
+// one launch sequence per tile.
+//
+//   * all points are sorted once on a (tile, Morton) key, so every tile's
+//     points stay in their own contiguous range;
+//   * leaves, Karras hierarchies, escape links and refits of all tiles are
+//     built by single launches that find their tile by binary search over
+//     per-tile offsets;
+//   * stage 1 and stage 3 are one persistent query launch each: warps pull
+//     4 x 8 window patches of any tile from one work counter, which balances
+//     uneven tiles;
+//   * stage 2 sorts all window results on a (tile, id) key;
+//   * the device part can be captured once into a CUDA graph and replayed
+//     while the tile shapes repeat.
+// Results per tile are exactly those of owm_run on that tile alone (ids are
+// 1-based within the tile).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "owm_batch.cuh"
+#include "owm_devutil.cuh"
+
+namespace owm {
+
+namespace {
+
+// Largest t in [0, ntiles) with off[t] <= x (off has ntiles+1 entries,
+// off[0] = 0, off[ntiles] > x): the tile that owns global index x.
+template <class T>
+__device__ __forceinline__ int tile_of(const T* __restrict__ off, int ntiles, int64_t x) {
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if ((int64_t)__ldg(off + mid) <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_b_morton(const double* __restrict__ xyz, int64_t n, const int64_t* __restrict__ pt_off,
+                           const TileMeta* __restrict__ meta, int ntiles, int mbits, uint32_t* __restrict__ keys) {
+  const float qmax = (float)((1u << mbits) - 1u);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int t = tile_of(pt_off, ntiles, i);
+    const TileMeta& m = meta[t];
+    double x = __ldg(xyz + 3 * i), y = __ldg(xyz + 3 * i + 1);
+    float fx = (float)((x - m.mox) * m.mscale), fy = (float)((y - m.moy) * m.mscale);
+    fx = fminf(fmaxf(fx, 0.0f), qmax);
+    fy = fminf(fmaxf(fy, 0.0f), qmax);
+    keys[i] = ((uint32_t)t << (2 * mbits)) | (spread_bits16((uint32_t)fx) << 1) | spread_bits16((uint32_t)fy);
+  }
+}
+
+// One warp per global leaf: gather its points into sorted order as keys and
+// reduce the leaf summary.
+__global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restrict__ xyz,
+                                                         const uint32_t* __restrict__ perm,
+                                                         const TileMeta* __restrict__ meta,
+                                                         const int32_t* __restrict__ leaf_off, int ntiles,
+                                                         int64_t total_leaves, int64_t* __restrict__ xk,
+                                                         int64_t* __restrict__ yk, int64_t* __restrict__ zk,
+                                                         uint32_t* __restrict__ pid, Node* __restrict__ nodes,
+                                                         uint32_t* __restrict__ status) {
+  const int lane = threadIdx.x & 31;
+  bool finite = true;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total_leaves;
+       g += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int t = tile_of(leaf_off, ntiles, g);
+    const TileMeta& m = meta[t];
+    const int32_t j = (int32_t)(g - m.leaf_off);
+    const int32_t first = j * m.leaf;
+    const int32_t cnt = min(m.leaf, m.n - first);
+    LeafAcc acc;
+    acc.init();
+    for (int32_t c = lane; c < cnt; c += 32) {
+      const int32_t lp = first + c;
+      const int64_t gp = m.pt_off + lp;
+      const uint32_t src = __ldg(perm + gp);
+      int64_t x, y, z;
+      finite &= load_point(xyz, src, x, y, z);
+      const uint32_t id = (uint32_t)((int64_t)src - m.pt_off + 1);
+      xk[gp] = x;
+      yk[gp] = y;
+      zk[gp] = z;
+      pid[gp] = id;
+      acc.add(x, y, z, id, (uint32_t)lp);
+    }
+    acc.reduce(32);
+    if (lane == 0) write_leaf(nodes + m.node_off + (m.nleaves - 1) + j, acc, first, m.ox, m.oy);
+  }
+  if (!finite) atomicOr(status, kStatusNonFinite);
+}
+
+__device__ __forceinline__ int bdelta(const uint32_t* __restrict__ mk, const TileMeta& m, int32_t i, int32_t j) {
+  if (j < 0 || j >= m.nleaves) return -1;
+  uint64_t a = ((uint64_t)__ldg(mk + m.pt_off + (int64_t)i * m.leaf) << 32) | (uint32_t)i;
+  uint64_t b = ((uint64_t)__ldg(mk + m.pt_off + (int64_t)j * m.leaf) << 32) | (uint32_t)j;
+  return __clzll((long long)(a ^ b));
+}
+
+// Karras (2012) per tile; indices stored local to the tile.
+__global__ void k_b_karras(const uint32_t* __restrict__ mk, const TileMeta* __restrict__ meta,
+                           const int32_t* __restrict__ int_off, int ntiles, int64_t total_internal,
+                           Node* __restrict__ nodes, int32_t* __restrict__ parent, int32_t* __restrict__ right_of,
+                           int32_t* __restrict__ last_of) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= total_internal) return;
+  const int t = tile_of(int_off, ntiles, q);
+  const TileMeta& m = meta[t];
+  const int32_t i = (int32_t)(q - m.int_off);
+  const int32_t nl = m.nleaves;
+  int d = bdelta(mk, m, i, i + 1) - bdelta(mk, m, i, i - 1) > 0 ? 1 : -1;
+  int dmin = bdelta(mk, m, i, i - d);
+  int32_t lmax = 2;
+  while (bdelta(mk, m, i, i + lmax * d) > dmin) lmax <<= 1;
+  int32_t l = 0;
+  for (int32_t s = lmax >> 1; s >= 1; s >>= 1)
+    if (bdelta(mk, m, i, i + (l + s) * d) > dmin) l += s;
+  int32_t j = i + l * d;
+  int dnode = bdelta(mk, m, i, j);
+  int32_t s = 0;
+  for (int32_t div = 2;; div <<= 1) {
+    int32_t st = (l + div - 1) / div;
+    if (bdelta(mk, m, i, i + (s + st) * d) > dnode) s += st;
+    if (st <= 1) break;
+  }
+  int32_t gamma = i + s * d + (d < 0 ? -1 : 0);
+  int32_t lo = min(i, j), hi = max(i, j);
+  int32_t left = (lo == gamma) ? (nl - 1 + gamma) : gamma;
+  int32_t right = (hi == gamma + 1) ? (nl - 1 + gamma + 1) : gamma + 1;
+  Node* base = nodes + m.node_off;
+  base[i].left = left;
+  base[i].right = right;
+  parent[m.node_off + left] = i;
+  parent[m.node_off + right] = i;
+  right_of[m.leaf_off + gamma] = right;
+  last_of[m.int_off + i] = hi;
+}
+
+__global__ void k_b_escapes(Node* __restrict__ nodes, const int32_t* __restrict__ right_of,
+                            const int32_t* __restrict__ last_of, const TileMeta* __restrict__ meta,
+                            const int32_t* __restrict__ node_off, int ntiles, int64_t total_nodes) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total_nodes) return;
+  const int t = tile_of(node_off, ntiles, k);
+  const TileMeta& m = meta[t];
+  const int32_t kl = (int32_t)(k - m.node_off), nl = m.nleaves;
+  const int32_t last = kl < nl - 1 ? last_of[m.int_off + kl] : kl - (nl - 1);
+  nodes[k].escape = last >= nl - 1 ? kEnd : right_of[m.leaf_off + last];
+}
+
+__global__ void k_b_refit(Node* __restrict__ nodes, const int32_t* __restrict__ parent, int32_t* __restrict__ flags,
+                          const TileMeta* __restrict__ meta, const int32_t* __restrict__ leaf_off, int ntiles,
+                          int64_t total_leaves) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_leaves) return;
+  const int t = tile_of(leaf_off, ntiles, g);
+  const TileMeta& m = meta[t];
+  Node* base = nodes + m.node_off;
+  const int32_t li = (int32_t)(g - m.leaf_off);
+  int32_t n = parent[m.node_off + m.nleaves - 1 + li];
+  for (int32_t guard = 0; n >= 0 && guard < m.nleaves; ++guard) {
+    __threadfence();
+    if (atomicAdd(&flags[m.int_off + n], 1) == 0) return;
+    __threadfence();
+    const Node* a = base + __ldcg(&base[n].left);
+    const Node* b = base + __ldcg(&base[n].right);
+    float4 ba = __ldcg(reinterpret_cast<const float4*>(a)), bb = __ldcg(reinterpret_cast<const float4*>(b));
+    int64_t za = __ldcg(&a->zmin), zb = __ldcg(&b->zmin);
+    uint32_t ia = __ldcg(&a->min_id), ib = __ldcg(&b->min_id);
+    uint32_t pa = __ldcg(&a->min_pos), pb = __ldcg(&b->min_pos);
+    uint32_t ca = __ldcg(&a->count), cb = __ldcg(&b->count);
+    Node* o = base + n;
+    __stcg(reinterpret_cast<float4*>(o),
+           make_float4(fminf(ba.x, bb.x), fminf(ba.y, bb.y), fmaxf(ba.z, bb.z), fmaxf(ba.w, bb.w)));
+    bool bl = zid_less(zb, ib, za, ia);
+    __stcg(&o->zmin, bl ? zb : za);
+    __stcg(&o->min_id, bl ? ib : ia);
+    __stcg(&o->min_pos, bl ? pb : pa);
+    __stcg(&o->count, ca + cb);
+    n = parent[m.node_off + n];
+  }
+}
+
+__device__ __forceinline__ Edge bedge(double lo, double hi, double o) {
+  Edge e;
+  e.lo_k = dkey(lo);
+  e.hi_k = dkey(hi);
+  e.lo_dn = __double2float_rd(__dsub_rd(lo, o));
+  e.lo_up = __double2float_ru(__dsub_ru(lo, o));
+  e.hi_dn = __double2float_rd(__dsub_rd(hi, o));
+  e.hi_up = __double2float_ru(__dsub_ru(hi, o));
+  return e;
+}
+
+// Edge tables of every tile: kind 0 = stage-1 windows, 1 = stage-3 cells;
+// axis 0 = x, 1 = y.  Same arithmetic as the single-cloud k_edges.
+__global__ void k_b_edges(int kind, int axis, const TileMeta* __restrict__ meta, const int32_t* __restrict__ off,
+                          int ntiles, int64_t total, Edge* __restrict__ out) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= total) return;
+  const int t = tile_of(off, ntiles, e);
+  const TileMeta& m = meta[t];
+  const int32_t i = (int32_t)(e - off[t]);
+  const double mn = axis ? m.min_y : m.min_x;
+  const double o = axis ? m.oy : m.ox;
+  double c, r;
+  if (kind) {
+    r = (double)(float)m.bhalf;
+    c = __dadd_rn(__dadd_rn(mn, (double)m.bhalf), (double)(i * m.bsize));
+  } else {
+    r = (double)(float)m.whalf;
+    double init = __dadd_rn(__dsub_rn(mn, (double)m.whalf), m.displace);
+    c = __dadd_rn(init, __dmul_rn((double)i, m.displace));
+  }
+  out[e] = bedge(__dsub_rn(c, r), __dadd_rn(c, r), o);
+}
+
+__global__ void k_b_s2_keys(const uint32_t* __restrict__ win, int64_t n, const int64_t* __restrict__ win_off,
+                            int ntiles, int idbits, uint32_t none, uint32_t* __restrict__ keys) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (int64_t)gridDim.x * blockDim.x) {
+    int t = tile_of(win_off, ntiles, w);
+    uint32_t v = win[w];
+    keys[w] = ((uint32_t)t << idbits) | (v == kNone ? none : v);
+  }
+}
+
+__global__ void k_b_s2_flags(const uint32_t* __restrict__ keys, int64_t n, int idbits, uint32_t none,
+                             const TileMeta* __restrict__ meta, uint32_t* __restrict__ flags,
+                             uint32_t* __restrict__ tile_count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t k = keys[i];
+    uint32_t t = k >> idbits;
+    bool f = (k & none) != none && (i == 0 || keys[i - 1] != k);
+    if (meta[t].need_dup) f = f && (i + 1 < n && keys[i + 1] == k);
+    flags[i] = f ? 1u : 0u;
+    if (f) atomicAdd(tile_count + t, 1u);
+  }
+}
+
+__global__ void k_b_compact(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ flags,
+                            const uint32_t* __restrict__ pos, int64_t n, uint32_t* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (flags[i]) out[pos[i]] = vals[i];
+}
+
+__global__ void k_b_s3_mark(const double* __restrict__ xyz, const uint32_t* __restrict__ llp,
+                            const uint32_t* __restrict__ nllp, int64_t cap, int idbits,
+                            const TileMeta* __restrict__ meta, const Edge* __restrict__ cell_ex,
+                            const Edge* __restrict__ cell_ey, uint8_t* __restrict__ mark) {
+  const int64_t n = min((int64_t)*nllp, cap);
+  const uint32_t mask = (idbits >= 32) ? 0xFFFFFFFFu : ((1u << idbits) - 1u);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t key = llp[k];
+    const TileMeta& m = meta[key >> idbits];
+    if (m.bsize == 0 || m.ncg <= 0) continue;
+    const uint32_t id = key & mask;
+    double x = 0.0, y = 0.0;  // id 0 = sentinel {0, 0, DBL_MAX}
+    if (id > 0) {
+      x = xyz[3 * (m.pt_off + id - 1)];
+      y = xyz[3 * (m.pt_off + id - 1) + 1];
+    }
+    const int64_t xk = dkey(x), yk = dkey(y);
+    double fi = floor((x - m.min_x) / (double)m.bsize), fj = floor((y - m.min_y) / (double)m.bsize);
+    if (!(fi > -4.0 && fi < (double)m.ncg + 4.0 && fj > -4.0 && fj < (double)m.nrg + 4.0)) continue;
+    const int32_t ic = (int32_t)fi, jc = (int32_t)fj;
+    const Edge* ex = cell_ex + m.cx_off;
+    const Edge* ey = cell_ey + m.cy_off;
+    for (int32_t jj = max(jc - 1, 0); jj <= min(jc + 1, m.nrg - 1); ++jj) {
+      if (!(yk > ey[jj].lo_k && yk < ey[jj].hi_k)) continue;
+      for (int32_t ii = max(ic - 1, 0); ii <= min(ic + 1, m.ncg - 1); ++ii)
+        if (xk > ex[ii].lo_k && xk < ex[ii].hi_k) mark[m.cell_off + (int64_t)jj * m.ncg + ii] = 1;
+    }
+  }
+}
+
+__global__ void k_b_flag_cells(const uint32_t* __restrict__ cellmin, int64_t n, const int64_t* __restrict__ cell_off,
+                               int ntiles, uint32_t* __restrict__ flags, uint32_t* __restrict__ tile_count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    bool f = cellmin[i] != kNone;
+    flags[i] = f ? 1u : 0u;
+    if (f) atomicAdd(tile_count + tile_of(cell_off, ntiles, i), 1u);
+  }
+}
+
+// Per tile t: out[out_off[t] ..] = its stage-3 ids, then its LLPs.
+__global__ void k_b_assemble(const uint32_t* __restrict__ s3, const uint32_t* __restrict__ s3_off,
+                             const uint32_t* __restrict__ llp, const uint32_t* __restrict__ llp_off, int idbits,
+                             int ntiles, int64_t* __restrict__ out, int64_t* __restrict__ out_off) {
+  const uint32_t mask = (idbits >= 32) ? 0xFFFFFFFFu : ((1u << idbits) - 1u);
+  const int64_t n3 = s3_off[ntiles], nl = llp_off[ntiles];
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n3 + nl + ntiles + 1;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    if (k < n3) {
+      int t = tile_of(s3_off, ntiles, k);
+      out[(int64_t)s3_off[t] + llp_off[t] + (k - s3_off[t])] = s3[k];
+    } else if (k < n3 + nl) {
+      int64_t q = k - n3;
+      int t = tile_of(llp_off, ntiles, q);
+      out[(int64_t)s3_off[t + 1] + llp_off[t] + (q - llp_off[t])] = llp[q] & mask;
+    } else {
+      int64_t t = k - n3 - nl;
+      out_off[t] = (int64_t)s3_off[t] + llp_off[t];
+    }
+  }
+}
+
+int gsz(int64_t n, int block = 256) {
+  int64_t g = (n + block - 1) / block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
+}
+
+size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int bits_for(uint64_t v) {  // smallest b with 2^b > v
+  int b = 0;
+  while (b < 64 && ((uint64_t)1 << b) <= v) ++b;
+  return b;
+}
+
+// Everything a batch needs, derived on the host from the tile shapes.
+struct Plan {
+  int32_t ntiles = 0;
+  int64_t npts = 0, nleaves = 0, nnodes = 0, ninternal = 0, nwin = 0, ncell = 0;
+  int64_t ex = 0, ey = 0, cx = 0, cy = 0;
+  int tile_bits = 1, mbits = 8, idbits = 1;
+  std::vector<TileMeta> meta;
+  std::vector<int64_t> pt_off, win_off, cell_off;
+  std::vector<int32_t> leaf_off, node_off, int_off, ex_off, ey_off, cx_off, cy_off;
+  // buffer offsets (bytes) inside the batch buffer
+  size_t o_xyz, o_k0, o_k1, o_v0, o_v1, o_sort, o_xk, o_yk, o_zk, o_pid, o_nodes, o_parent, o_flags, o_right,
+      o_last, o_edges, o_win, o_s2k0, o_s2k1, o_s2f, o_s2p, o_s2t, o_llp, o_mark, o_cmin, o_cf, o_cp, o_ct, o_s3,
+      o_meta, o_jobs1, o_jobs3, o_ptoff, o_leafoff, o_nodeoff, o_intoff, o_exoff, o_eyoff, o_cxoff, o_cyoff,
+      o_winoff, o_celloff, o_cnt2, o_cnt3, o_llpoff, o_s3off, o_out, o_outoff, o_words, total;
+};
+
+int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan* P) {
+  P->ntiles = ntiles;
+  P->meta.resize(ntiles);
+  P->pt_off.assign(ntiles + 1, 0);
+  P->win_off.assign(ntiles + 1, 0);
+  P->cell_off.assign(ntiles + 1, 0);
+  for (auto* v : {&P->leaf_off, &P->node_off, &P->int_off, &P->ex_off, &P->ey_off, &P->cx_off, &P->cy_off})
+    v->assign(ntiles + 1, 0);
+  P->tile_bits = std::max(1, bits_for((uint64_t)ntiles - 1));
+  P->mbits = std::min(16, (32 - P->tile_bits) / 2);
+  int64_t maxn = 0;
+  for (int32_t t = 0; t < ntiles; ++t) {
+    const owm_tile_desc& d = td[t];
+    if (!d.xyz || d.n <= 0 || d.n >= 0x7FFFFFFFLL) return OWM_EINVAL;
+    if (validate_tree_cfg(&d.cfg.tree) != OWM_OK || d.cfg.tree.policy != OWM_TREE_MAX_NUMBER) return OWM_EINVAL;
+    owm_bbox bb = d.bbox;
+    if (!(bb.min_x <= bb.max_x)) {
+      if (is_device_ptr(d.xyz)) return OWM_EINVAL;  // device tiles must carry their bbox
+      owm_bbox_of(d.xyz, d.n, &bb);
+    }
+    owm_params p;
+    int rc = owm_params_compute(&bb, d.n, d.cfg.wsize, d.cfg.overlap, d.cfg.bsize, &p);
+    if (rc) return rc;
+    maxn = std::max<int64_t>(maxn, d.n);
+    TileMeta& m = P->meta[t];
+    std::memset(&m, 0, sizeof(m));
+    m.pt_off = P->npts;
+    m.n = (int32_t)d.n;
+    m.leaf = br.leaf_for(d.n, d.cfg.tree.max_number);
+    int32_t nl = (int32_t)((d.n + m.leaf - 1) / m.leaf);
+    m.leaf_off = (int32_t)P->nleaves;
+    m.nleaves = nl;
+    m.node_off = (int32_t)P->nnodes;
+    m.int_off = (int32_t)P->ninternal;
+    double rx = (bb.max_x - bb.min_x) * 0.5, ry = (bb.max_y - bb.min_y) * 0.5;
+    double R = rx >= ry ? rx : ry;
+    if (!(R > 0.0)) R = 0.5;
+    m.mox = bb.min_x + rx - R;
+    m.moy = bb.min_y + ry - R;
+    m.mscale = (double)(1u << P->mbits) / (2.0 * R);
+    m.ox = bb.min_x;
+    m.oy = bb.min_y;
+    m.min_x = bb.min_x;
+    m.min_y = bb.min_y;
+    m.displace = p.displace;
+    m.ncols = (int32_t)p.ncols;
+    m.nrows = (int32_t)p.nrows;
+    m.ncg = (int32_t)p.ncols_grid;
+    m.nrg = (int32_t)p.nrows_grid;
+    m.whalf = ((uint16_t)p.wsize) / 2;
+    m.bhalf = ((uint16_t)p.bsize) / 2;
+    m.bsize = (uint16_t)p.bsize;
+    m.thr = p.min_num_points;
+    m.need_dup = p.overlap > 0.0 ? 1 : 0;
+    m.win_off = P->nwin;
+    m.cell_off = P->ncell;
+    m.ex_off = (int32_t)P->ex;
+    m.ey_off = (int32_t)P->ey;
+    m.cx_off = (int32_t)P->cx;
+    m.cy_off = (int32_t)P->cy;
+    P->pt_off[t] = P->npts;
+    P->leaf_off[t] = m.leaf_off;
+    P->node_off[t] = m.node_off;
+    P->int_off[t] = m.int_off;
+    P->win_off[t] = P->nwin;
+    P->cell_off[t] = P->ncell;
+    P->ex_off[t] = (int32_t)P->ex;
+    P->ey_off[t] = (int32_t)P->ey;
+    P->cx_off[t] = (int32_t)P->cx;
+    P->cy_off[t] = (int32_t)P->cy;
+    P->npts += d.n;
+    P->nleaves += nl;
+    P->nnodes += 2 * (int64_t)nl - 1;
+    P->ninternal += nl - 1;
+    P->nwin += p.ncells;
+    P->ncell += p.bsize > 0 ? p.ngrid : 0;
+    P->ex += p.ncols;
+    P->ey += p.nrows;
+    P->cx += p.bsize > 0 ? p.ncols_grid : 0;
+    P->cy += p.bsize > 0 ? p.nrows_grid : 0;
+  }
+  P->pt_off[ntiles] = P->npts;
+  P->leaf_off[ntiles] = (int32_t)P->nleaves;
+  P->node_off[ntiles] = (int32_t)P->nnodes;
+  P->int_off[ntiles] = (int32_t)P->ninternal;
+  P->win_off[ntiles] = P->nwin;
+  P->cell_off[ntiles] = P->ncell;
+  P->ex_off[ntiles] = (int32_t)P->ex;
+  P->ey_off[ntiles] = (int32_t)P->ey;
+  P->cx_off[ntiles] = (int32_t)P->cx;
+  P->cy_off[ntiles] = (int32_t)P->cy;
+  if (P->npts >= 0xFFFFFFFFLL || P->nnodes >= 0x7FFFFFFFLL) return OWM_ERANGE;
+  P->idbits = std::max(1, bits_for((uint64_t)maxn + 1));
+  if (P->tile_bits + P->idbits > 32) return OWM_ERANGE;  // split the batch
+
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = o;
+    o += a256(bytes);
+    return r;
+  };
+  const int64_t N = P->npts, NW = std::max<int64_t>(P->nwin, 1), NC = std::max<int64_t>(P->ncell, 1);
+  const int64_t T1 = ntiles + 1;
+  P->o_xyz = take((size_t)N * 24);
+  P->o_k0 = take((size_t)N * 4);
+  P->o_k1 = take((size_t)N * 4);
+  P->o_v0 = take((size_t)N * 4);
+  P->o_v1 = take((size_t)N * 4);
+  P->o_sort = take(radix_sort_temp_bytes(N));
+  P->o_xk = take((size_t)N * 8);
+  P->o_yk = take((size_t)N * 8);
+  P->o_zk = take((size_t)N * 8);
+  P->o_pid = take((size_t)N * 4);
+  P->o_nodes = take((size_t)P->nnodes * sizeof(Node));
+  P->o_parent = take((size_t)P->nnodes * 4);
+  P->o_flags = take((size_t)std::max<int64_t>(P->ninternal, 1) * 4);
+  P->o_right = take((size_t)P->nleaves * 4);
+  P->o_last = take((size_t)std::max<int64_t>(P->ninternal, 1) * 4);
+  P->o_edges = take((size_t)(P->ex + P->ey + P->cx + P->cy + 1) * sizeof(Edge));
+  P->o_win = take((size_t)NW * 4);
+  P->o_s2k0 = take((size_t)NW * 4);
+  P->o_s2k1 = take((size_t)NW * 4);
+  P->o_s2f = take((size_t)NW * 4);
+  P->o_s2p = take((size_t)NW * 4);
+  P->o_s2t = take(a256(radix_sort_temp_bytes(NW)) + scan_temp_bytes(std::max(NW, NC)) + 256);
+  P->o_llp = take((size_t)NW * 4);
+  P->o_mark = take((size_t)NC);
+  P->o_cmin = take((size_t)NC * 4);
+  P->o_cf = take((size_t)NC * 4);
+  P->o_cp = take((size_t)NC * 4);
+  P->o_ct = take(scan_temp_bytes(NC) + 256);
+  P->o_s3 = take((size_t)NC * 4);
+  P->o_meta = take((size_t)ntiles * sizeof(TileMeta));
+  P->o_jobs1 = take((size_t)ntiles * sizeof(QueryJob));
+  P->o_jobs3 = take((size_t)ntiles * sizeof(QueryJob));
+  P->o_ptoff = take((size_t)T1 * 8);
+  P->o_leafoff = take((size_t)T1 * 4);
+  P->o_nodeoff = take((size_t)T1 * 4);
+  P->o_intoff = take((size_t)T1 * 4);
+  P->o_exoff = take((size_t)T1 * 4);
+  P->o_eyoff = take((size_t)T1 * 4);
+  P->o_cxoff = take((size_t)T1 * 4);
+  P->o_cyoff = take((size_t)T1 * 4);
+  P->o_winoff = take((size_t)T1 * 8);
+  P->o_celloff = take((size_t)T1 * 8);
+  P->o_cnt2 = take((size_t)T1 * 4);
+  P->o_cnt3 = take((size_t)T1 * 4);
+  P->o_llpoff = take((size_t)T1 * 4);
+  P->o_s3off = take((size_t)T1 * 4);
+  P->o_out = take((size_t)(NW + NC + 1) * 8);
+  P->o_outoff = take((size_t)T1 * 8);
+  P->o_words = take(256);
+  P->total = o;
+  return OWM_OK;
+}
+
+}  // namespace
+
+int BatchRun::init(int dev, cudaStream_t s) {
+  device = dev;
+  OWM_CUDA_TRY(cudaSetDevice(dev));
+  if (s) {
+    stream = s;
+  } else {
+    OWM_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+  }
+  OWM_CUDA_TRY(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+  return OWM_OK;
+}
+
+void BatchRun::destroy() {
+  cudaSetDevice(device);
+  if (stream) cudaStreamSynchronize(stream);
+  if (graph) cudaGraphExecDestroy(graph);
+  graph = nullptr;
+  mem.release(stream);
+  if (stream) cudaStreamSynchronize(stream);
+  if (h_off) cudaFreeHost(h_off);
+  h_off = nullptr;
+  if (done) cudaEventDestroy(done);
+  done = nullptr;
+  if (own_stream && stream) cudaStreamDestroy(stream);
+  stream = nullptr;
+  cudaGetLastError();
+}
+
+int BatchRun::leaf_for(int64_t n, int32_t requested) const {
+  for (int32_t k = 0; k < nclass; ++k)
+    if (n <= class_bound[k]) return class_leaf[k];
+  return requested;
+}
+
+size_t BatchRun::estimate_bytes(const owm_tile_desc* t, int32_t ntiles) {
+  BatchRun tmp;
+  Plan P;
+  if (make_plan(t, ntiles, tmp, &P) != OWM_OK) return (size_t)-1;
+  return P.total;
+}
+
+int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
+  if (!td || ntiles <= 0) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(device));
+  Plan P;
+  int rc = make_plan(td, ntiles, *this, &P);
+  if (rc) return rc;
+  bytes_needed = P.total;
+  if (P.total > mem.cap && graph) {  // buffers move: the captured graph is stale
+    cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_sig.clear();
+  }
+  rc = mem.reserve(P.total, stream);
+  if (rc) return rc;
+  if (cap_tiles < ntiles + 1) {
+    if (h_off) cudaFreeHost(h_off);
+    h_off = nullptr;
+    OWM_CUDA_TRY(cudaMallocHost(&h_off, (size_t)(ntiles + 1) * 8));
+    cap_tiles = ntiles + 1;
+  }
+  tiles.clear();
+  char* B = static_cast<char*>(mem.ptr);
+  auto at = [&](size_t off) { return B + off; };
+  double* xyz = (double*)at(P.o_xyz);
+  const int64_t N = P.npts;
+  // points in (host or device sources)
+  for (int32_t t = 0; t < ntiles; ++t) {
+    OWM_CUDA_TRY(cudaMemcpyAsync(xyz + 3 * P.pt_off[t], td[t].xyz, (size_t)td[t].n * 24, cudaMemcpyDefault, stream));
+    TileHost th;
+    th.xyz = td[t].xyz;
+    owm_bbox bb = td[t].bbox;
+    if (!(bb.min_x <= bb.max_x)) owm_bbox_of(td[t].xyz, td[t].n, &bb);
+    owm_params_compute(&bb, td[t].n, td[t].cfg.wsize, td[t].cfg.overlap, td[t].cfg.bsize, &th.p);
+    th.tree = td[t].cfg.tree;
+    tiles.push_back(th);
+  }
+  TileMeta* d_meta = (TileMeta*)at(P.o_meta);
+  int64_t* d_ptoff = (int64_t*)at(P.o_ptoff);
+  int32_t* d_leafoff = (int32_t*)at(P.o_leafoff);
+  int32_t* d_nodeoff = (int32_t*)at(P.o_nodeoff);
+  int32_t* d_intoff = (int32_t*)at(P.o_intoff);
+  int32_t* d_exoff = (int32_t*)at(P.o_exoff);
+  int32_t* d_eyoff = (int32_t*)at(P.o_eyoff);
+  int32_t* d_cxoff = (int32_t*)at(P.o_cxoff);
+  int32_t* d_cyoff = (int32_t*)at(P.o_cyoff);
+  int64_t* d_winoff = (int64_t*)at(P.o_winoff);
+  int64_t* d_celloff = (int64_t*)at(P.o_celloff);
+  const size_t T1 = (size_t)ntiles + 1;
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_meta, P.meta.data(), (size_t)ntiles * sizeof(TileMeta), cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_ptoff, P.pt_off.data(), T1 * 8, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_leafoff, P.leaf_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_nodeoff, P.node_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_intoff, P.int_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_exoff, P.ex_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_eyoff, P.ey_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_cxoff, P.cx_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_cyoff, P.cy_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_winoff, P.win_off.data(), T1 * 8, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_celloff, P.cell_off.data(), T1 * 8, cudaMemcpyHostToDevice, stream));
+
+  // query jobs (host-built: pointers are known here)
+  TreeView base_view;
+  int64_t* xk = (int64_t*)at(P.o_xk);
+  int64_t* yk = (int64_t*)at(P.o_yk);
+  int64_t* zk = (int64_t*)at(P.o_zk);
+  uint32_t* pid = (uint32_t*)at(P.o_pid);
+  Node* nodes = (Node*)at(P.o_nodes);
+  Edge* edges = (Edge*)at(P.o_edges);
+  Edge* E_wx = edges;
+  Edge* E_wy = E_wx + P.ex;
+  Edge* E_cx = E_wy + P.ey;
+  Edge* E_cy = E_cx + P.cx;
+  uint32_t* win = (uint32_t*)at(P.o_win);
+  uint8_t* mark = (uint8_t*)at(P.o_mark);
+  uint32_t* cmin = (uint32_t*)at(P.o_cmin);
+  uint32_t* words = (uint32_t*)at(P.o_words);
+  d_status = words;  // [0] status, [1] LLP total, [2] s3 total, [4..5] queue counter (8-byte aligned)
+  unsigned long long* qnext = reinterpret_cast<unsigned long long*>(words + 4);
+  std::vector<QueryJob> j1(ntiles), j3(ntiles);
+  int64_t w1 = 0, w3 = 0;
+  for (int32_t t = 0; t < ntiles; ++t) {
+    const TileMeta& m = P.meta[t];
+    TreeView v;
+    v.xk = xk + m.pt_off;
+    v.yk = yk + m.pt_off;
+    v.zk = zk + m.pt_off;
+    v.pid = pid + m.pt_off;
+    v.nodes = nodes + m.node_off;
+    v.nleaves = m.nleaves;
+    v.root = 0;
+    v.ox = m.ox;
+    v.oy = m.oy;
+    QueryJob& a = j1[t];
+    a.tree = v;
+    a.ex = E_wx + m.ex_off;
+    a.ey = E_wy + m.ey_off;
+    a.ncols = m.ncols;
+    a.nrows = m.nrows;
+    a.thr = m.thr;
+    a.cell_order = 0;
+    a.skip = nullptr;
+    a.out = win + m.win_off;
+    a.status = words;
+    a.warp_begin = w1;
+    w1 += job_warps(m.ncols, m.nrows);
+    QueryJob& b = j3[t];
+    b = a;
+    b.ex = E_cx + m.cx_off;
+    b.ey = E_cy + m.cy_off;
+    b.ncols = m.bsize > 0 ? m.ncg : 0;
+    b.nrows = m.bsize > 0 ? m.nrg : 0;
+    b.thr = 1;
+    b.cell_order = 1;
+    b.skip = mark + m.cell_off;
+    b.out = cmin + m.cell_off;
+    b.warp_begin = w3;
+    w3 += job_warps(b.ncols, b.nrows);
+  }
+  (void)base_view;
+  QueryJob* d_j1 = (QueryJob*)at(P.o_jobs1);
+  QueryJob* d_j3 = (QueryJob*)at(P.o_jobs3);
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_j1, j1.data(), (size_t)ntiles * sizeof(QueryJob), cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(d_j3, j3.data(), (size_t)ntiles * sizeof(QueryJob), cudaMemcpyHostToDevice, stream));
+
+  int64_t* d_out = (int64_t*)at(P.o_out);
+  int64_t* d_outoff = (int64_t*)at(P.o_outoff);
+  this->d_out = d_out;
+  this->d_out_off = d_outoff;
+
+  // ---- device work (graph-capturable: no host sync, fixed shapes) ----
+  std::string sig;
+  if (use_graphs) {
+    sig.assign(reinterpret_cast<const char*>(P.meta.data()), P.meta.size() * sizeof(TileMeta));
+    sig.append(reinterpret_cast<const char*>(&mem.ptr), sizeof(void*));
+    sig.append(reinterpret_cast<const char*>(&P.total), sizeof(P.total));
+  }
+  if (use_graphs && graph && sig == graph_sig) {
+    OWM_CUDA_TRY(cudaGraphLaunch(graph, stream));
+    count_launch(&launches);
+  } else {
+    bool capture = use_graphs;
+    ProfScope no_prof(capture ? nullptr : tls_profiler());
+    if (capture) OWM_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    cudaStream_t s = stream;
+    int64_t* L = &launches;
+    uint32_t* k0 = (uint32_t*)at(P.o_k0);
+    uint32_t* k1 = (uint32_t*)at(P.o_k1);
+    uint32_t* v0 = (uint32_t*)at(P.o_v0);
+    uint32_t* v1 = (uint32_t*)at(P.o_v1);
+    int32_t* parent = (int32_t*)at(P.o_parent);
+    int32_t* flags = (int32_t*)at(P.o_flags);
+    int32_t* right_of = (int32_t*)at(P.o_right);
+    int32_t* last_of = (int32_t*)at(P.o_last);
+    uint32_t* cnt2 = (uint32_t*)at(P.o_cnt2);
+    uint32_t* cnt3 = (uint32_t*)at(P.o_cnt3);
+    uint32_t* llp_off = (uint32_t*)at(P.o_llpoff);
+    uint32_t* s3_off = (uint32_t*)at(P.o_s3off);
+    uint32_t* llp = (uint32_t*)at(P.o_llp);
+    uint32_t* s3 = (uint32_t*)at(P.o_s3);
+    int rc2 = OWM_OK;
+    do {
+      if (cudaMemsetAsync(words, 0, 256, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      const int key_bits = P.tile_bits + 2 * P.mbits;
+      OWM_LAUNCH("k_b_morton", s, k_b_morton<<<gsz(N), 256, 0, s>>>(xyz, N, d_ptoff, d_meta, ntiles, P.mbits, k0));
+      count_launch(L);
+      bool alt = false;
+      if (radix_sort(k0, v0, k1, v1, N, key_bits, true, at(P.o_sort), radix_sort_temp_bytes(N), s, &alt, L) !=
+          cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      const uint32_t* mk = alt ? k1 : k0;
+      const uint32_t* perm = alt ? v1 : v0;
+      {
+        int64_t blocks = std::min<int64_t>((P.nleaves * 32 + 255) / 256, 152 * 16);
+        OWM_LAUNCH("k_b_gather_leaves", s, k_b_gather_leaves<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(
+            xyz, perm, d_meta, d_leafoff, ntiles, P.nleaves, xk, yk, zk, pid, nodes, words));
+        count_launch(L);
+      }
+      if (cudaMemsetAsync(parent, 0xFF, (size_t)P.nnodes * 4, s) != cudaSuccess ||
+          cudaMemsetAsync(flags, 0, (size_t)std::max<int64_t>(P.ninternal, 1) * 4, s) != cudaSuccess) {
+        rc2 = OWM_ECUDA;
+        break;
+      }
+      if (P.ninternal > 0) {
+        OWM_LAUNCH("k_b_karras", s, k_b_karras<<<(unsigned)((P.ninternal + 255) / 256), 256, 0, s>>>(
+            mk, d_meta, d_intoff, ntiles, P.ninternal, nodes, parent, right_of, last_of));
+        count_launch(L);
+      }
+      OWM_LAUNCH("k_b_escapes", s, k_b_escapes<<<(unsigned)((P.nnodes + 255) / 256), 256, 0, s>>>(
+          nodes, right_of, last_of, d_meta, d_nodeoff, ntiles, P.nnodes));
+      OWM_LAUNCH("k_b_refit", s, k_b_refit<<<(unsigned)((P.nleaves + 255) / 256), 256, 0, s>>>(
+          nodes, parent, flags, d_meta, d_leafoff, ntiles, P.nleaves));
+      count_launch(L, 2);
+      // edge tables
+      if (P.ex) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ex + 127) / 128), 128, 0, s>>>(0, 0, d_meta, d_exoff, ntiles, P.ex, E_wx));
+      if (P.ey) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ey + 127) / 128), 128, 0, s>>>(0, 1, d_meta, d_eyoff, ntiles, P.ey, E_wy));
+      if (P.cx) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cx + 127) / 128), 128, 0, s>>>(1, 0, d_meta, d_cxoff, ntiles, P.cx, E_cx));
+      if (P.cy) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cy + 127) / 128), 128, 0, s>>>(1, 1, d_meta, d_cyoff, ntiles, P.cy, E_cy));
+      count_launch(L, (P.ex > 0) + (P.ey > 0) + (P.cx > 0) + (P.cy > 0));
+      // stage 1: persistent query over every tile's windows
+      if (launch_query_persistent(d_j1, ntiles, w1, qnext, 152 * 16, s, L, "k_query_s1_batch")) { rc2 = OWM_ECUDA; break; }
+      // stage 2 on (tile, id) keys
+      const int64_t NW = P.nwin;
+      const uint32_t none = (P.idbits >= 32) ? 0xFFFFFFFFu : ((1u << P.idbits) - 1u);
+      uint32_t* s2k0 = (uint32_t*)at(P.o_s2k0);
+      uint32_t* s2k1 = (uint32_t*)at(P.o_s2k1);
+      uint32_t* s2f = (uint32_t*)at(P.o_s2f);
+      uint32_t* s2p = (uint32_t*)at(P.o_s2p);
+      char* s2t = at(P.o_s2t);
+      if (cudaMemsetAsync(cnt2, 0, T1 * 4, s) != cudaSuccess || cudaMemsetAsync(cnt3, 0, T1 * 4, s) != cudaSuccess) {
+        rc2 = OWM_ECUDA;
+        break;
+      }
+      if (NW > 0) {
+        OWM_LAUNCH("k_b_s2_keys", s, k_b_s2_keys<<<gsz(NW), 256, 0, s>>>(win, NW, d_winoff, ntiles, P.idbits, none, s2k0));
+        count_launch(L);
+        bool a2 = false;
+        size_t sb = radix_sort_temp_bytes(NW);
+        if (radix_sort(s2k0, nullptr, s2k1, nullptr, NW, P.tile_bits + P.idbits, false, s2t, sb, s, &a2, L) !=
+            cudaSuccess) { rc2 = OWM_ECUDA; break; }
+        const uint32_t* sk = a2 ? s2k1 : s2k0;
+        OWM_LAUNCH("k_b_s2_flags", s, k_b_s2_flags<<<gsz(NW), 256, 0, s>>>(sk, NW, P.idbits, none, d_meta, s2f, cnt2));
+        count_launch(L);
+        if (exclusive_scan_u32(s2f, s2p, NW, words + 1, s2t + a256(sb), scan_temp_bytes(std::max<int64_t>(NW, P.ncell)) + 256,
+                               s, L) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+        OWM_LAUNCH("k_b_compact", s, k_b_compact<<<gsz(NW), 256, 0, s>>>(sk, s2f, s2p, NW, llp));
+        count_launch(L);
+      }
+      if (exclusive_scan_u32(cnt2, llp_off, ntiles + 1, nullptr, s2t, scan_temp_bytes(ntiles + 1) + 256, s, L) !=
+          cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      // stage 3
+      const int64_t NC = P.ncell;
+      if (NC > 0) {
+        if (cudaMemsetAsync(mark, 0, (size_t)NC, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+        if (NW > 0) {
+          OWM_LAUNCH("k_b_s3_mark", s, k_b_s3_mark<<<gsz(NW), 256, 0, s>>>(xyz, llp, words + 1, NW, P.idbits, d_meta, E_cx, E_cy, mark));
+          count_launch(L);
+        }
+        if (launch_query_persistent(d_j3, ntiles, w3, qnext, 152 * 16, s, L, "k_query_s3_batch")) { rc2 = OWM_ECUDA; break; }
+        uint32_t* cf = (uint32_t*)at(P.o_cf);
+        uint32_t* cp = (uint32_t*)at(P.o_cp);
+        OWM_LAUNCH("k_b_flag_cells", s, k_b_flag_cells<<<gsz(NC), 256, 0, s>>>(cmin, NC, d_celloff, ntiles, cf, cnt3));
+        count_launch(L);
+        if (exclusive_scan_u32(cf, cp, NC, words + 2, at(P.o_ct), scan_temp_bytes(NC) + 256, s, L) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
+        }
+        OWM_LAUNCH("k_b_compact", s, k_b_compact<<<gsz(NC), 256, 0, s>>>(cmin, cf, cp, NC, s3));
+        count_launch(L);
+      }
+      if (exclusive_scan_u32(cnt3, s3_off, ntiles + 1, nullptr, at(P.o_ct), scan_temp_bytes(ntiles + 1) + 256, s, L) !=
+          cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      OWM_LAUNCH("k_b_assemble", s, k_b_assemble<<<gsz(NW + NC + ntiles + 1), 256, 0, s>>>(s3, s3_off, llp, llp_off, P.idbits, ntiles, d_out, d_outoff));
+      count_launch(L);
+      if (cudaMemcpyAsync(h_off, d_outoff, T1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+    } while (false);
+    if (capture) {
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (rc2 == OWM_OK && e == cudaSuccess) {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        e = cudaGraphInstantiate(&graph, g, 0);
+        if (e == cudaSuccess) {
+          graph_sig = sig;
+          e = cudaGraphLaunch(graph, stream);
+          count_launch(&launches);
+        }
+      }
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        set_last_cuda_error(e, "batch graph", __FILE__, __LINE__);
+        return OWM_ECUDA;
+      }
+    }
+    if (rc2) return rc2;
+  }
+  OWM_CUDA_TRY(cudaEventRecord(done, stream));
+  return OWM_OK;
+}
+
+bool BatchRun::ready() {
+  cudaError_t e = cudaEventQuery(done);
+  if (e == cudaErrorNotReady) return false;
+  cudaGetLastError();
+  return true;
+}
+
+int BatchRun::finish(int64_t* seeds, int64_t cap, int64_t* offsets, owm_run_info* info) {
+  OWM_CUDA_TRY(cudaSetDevice(device));
+  OWM_CUDA_TRY(cudaEventSynchronize(done));
+  uint32_t st = 0;
+  OWM_CUDA_TRY(cudaMemcpy(&st, d_status, 4, cudaMemcpyDeviceToHost));
+  if (st & kStatusNonFinite) return OWM_EINVAL;
+  if (st & kStatusWalkBound) return OWM_ETIMEOUT;
+  const int64_t nt = (int64_t)tiles.size();
+  total_out = h_off[nt];
+  if (offsets) std::memcpy(offsets, h_off, (size_t)(nt + 1) * 8);
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    info->n_seeds = total_out;
+  }
+  if (total_out > cap) return OWM_ERANGE;
+  if (total_out > 0 && seeds) {
+    OWM_CUDA_TRY(cudaMemcpyAsync(seeds, d_out, (size_t)total_out * 8, cudaMemcpyDefault, stream));
+    OWM_CUDA_TRY(cudaStreamSynchronize(stream));
+  }
+  return OWM_OK;
+}
+
+}  // namespace owm
+
+using namespace owm;
+
+struct owm_batch {
+  owm_ctx* ctx;  // used only inside owm_batch_run (profiler, launch count)
+  BatchRun run;
+};
+
+extern "C" {
+
+int owm_batch_create(owm_ctx* ctx, owm_batch** out) {
+  if (!ctx || !out) return OWM_EINVAL;
+  owm_batch* b = new owm_batch();
+  b->ctx = ctx;
+  // own stream: the batch may outlive nothing of its context but the device
+  int rc = b->run.init(ctx->device, nullptr);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return OWM_OK;
+}
+
+int owm_batch_destroy(owm_batch* b) {
+  if (!b) return OWM_OK;
+  b->run.destroy();
+  delete b;
+  return OWM_OK;
+}
+
+int owm_batch_set_graphs(owm_batch* b, int enable) {
+  if (!b) return OWM_EINVAL;
+  b->run.use_graphs = enable != 0;
+  return OWM_OK;
+}
+
+int owm_batch_set_leaf_classes(owm_batch* b, int32_t nclass, const int64_t* bounds, const int32_t* leaf) {
+  if (!b || nclass < 0 || nclass > 8 || (nclass > 0 && (!bounds || !leaf))) return OWM_EINVAL;
+  for (int32_t k = 0; k < nclass; ++k) {
+    int m = leaf[k];
+    if (m < 1 || m > 256 || (m & (m - 1))) return OWM_EINVAL;
+    if (k > 0 && bounds[k] <= bounds[k - 1]) return OWM_EINVAL;
+  }
+  b->run.nclass = nclass;
+  for (int32_t k = 0; k < nclass; ++k) {
+    b->run.class_bound[k] = bounds[k];
+    b->run.class_leaf[k] = leaf[k];
+  }
+  if (b->run.graph) {
+    cudaGraphExecDestroy(b->run.graph);
+    b->run.graph = nullptr;
+    b->run.graph_sig.clear();
+  }
+  return OWM_OK;
+}
+
+int owm_batch_run(owm_batch* b, const owm_tile_desc* tiles, int32_t ntiles, int64_t* seeds, int64_t cap,
+                  int64_t* offsets, owm_run_info* info) {
+  if (!b || !tiles || ntiles <= 0 || !offsets || (!seeds && cap > 0)) return OWM_EINVAL;
+  ProfScope prof_scope(b->ctx->active_prof());
+  int64_t l0 = b->run.launches;
+  int rc = b->run.launch(tiles, ntiles);
+  if (rc) return rc;
+  rc = b->run.finish(seeds, cap, offsets, info);
+  b->ctx->launches += b->run.launches - l0;
+  return rc;
+}
+
+}  // extern "C"

@@ -92,11 +92,10 @@ __device__ __forceinline__ int find_job(const QueryJob* __restrict__ jobs, int32
 
 __device__ __forceinline__ int64_t shfl64(int64_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-__global__ void __launch_bounds__(kQBlock) k_query(const QueryJob* __restrict__ jobs, int32_t njobs,
-                                                   int64_t total_warps) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * kQBlock + threadIdx.x) >> 5;
-  if (warp >= total_warps) return;  // warp-uniform
+// One warp answers the 4 x 8 patch `warp` of the job list (all 32 lanes call
+// this together).
+__device__ __forceinline__ void query_warp(const QueryJob* __restrict__ jobs, int32_t njobs, int64_t warp,
+                                           int lane) {
   const QueryJob& J = jobs[njobs > 1 ? find_job(jobs, njobs, warp) : 0];
   const TreeView T = J.tree;
   const int64_t lw = warp - J.warp_begin;
@@ -251,6 +250,29 @@ __global__ void __launch_bounds__(kQBlock) k_query(const QueryJob* __restrict__ 
   if (active) J.out[oidx] = cnt >= thr ? bid : kNone;
 }
 
+__global__ void __launch_bounds__(kQBlock) k_query(const QueryJob* __restrict__ jobs, int32_t njobs,
+                                                   int64_t total_warps) {
+  const int64_t warp = ((int64_t)blockIdx.x * kQBlock + threadIdx.x) >> 5;
+  if (warp >= total_warps) return;  // warp-uniform
+  query_warp(jobs, njobs, warp, threadIdx.x & 31);
+}
+
+// Persistent form for many uneven jobs: a fixed grid of warps pulls patch
+// indices from one counter until the list is exhausted (each pull advances
+// the counter, so the loop ends after at most total_warps + grid pulls).
+__global__ void __launch_bounds__(kQBlock) k_query_persistent(const QueryJob* __restrict__ jobs, int32_t njobs,
+                                                              int64_t total_warps,
+                                                              unsigned long long* __restrict__ next) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(next, 1ull);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if ((int64_t)w >= total_warps) return;
+    query_warp(jobs, njobs, (int64_t)w, lane);
+  }
+}
+
 // ---- stage 2 -----------------------------------------------------------------
 __global__ void k_s2_keys(const uint32_t* __restrict__ win, int64_t n, uint32_t none_key, uint32_t* __restrict__ keys) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -362,6 +384,18 @@ int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cud
   if (total_warps <= 0) return OWM_OK;
   int64_t blocks = (total_warps * 32 + kQBlock - 1) / kQBlock;
   OWM_LAUNCH(name, s, k_query<<<(unsigned)blocks, kQBlock, 0, s>>>(d_jobs, njobs, total_warps));
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int launch_query_persistent(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, unsigned long long* d_next,
+                            int blocks, cudaStream_t s, int64_t* launches, const char* name) {
+  if (total_warps <= 0) return OWM_OK;
+  OWM_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), s));
+  int64_t need = (total_warps * 32 + kQBlock - 1) / kQBlock;
+  int g = (int)std::min<int64_t>(need, blocks);
+  OWM_LAUNCH(name, s, k_query_persistent<<<g, kQBlock, 0, s>>>(d_jobs, njobs, total_warps, d_next));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;

@@ -37,6 +37,10 @@ int64_t job_warps(int32_t ncols, int32_t nrows);
 // `name` labels the launch for the per-kernel profiler.
 int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches,
                  const char* name);
+// Persistent variant: `blocks` resident blocks pull 4 x 8 patches from the
+// device counter *d_next (reset here) -- load balance for uneven jobs.
+int launch_query_persistent(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, unsigned long long* d_next,
+                            int blocks, cudaStream_t s, int64_t* launches, const char* name);
 // Single job convenience (job staged through a small device buffer).
 int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t* launches, const char* name);
 
