@@ -142,8 +142,9 @@ def tree_cfg(policy: int = OWM_TREE_MAX_NUMBER, max_number: int = 32, min_radius
 
 
 def run_cfg(wsize: int, overlap: float, bsize: int, max_number: int = 32, policy: int = OWM_TREE_MAX_NUMBER,
-            min_radius: float = 0.1) -> RunCfg:
-    return RunCfg(wsize, bsize, overlap, tree_cfg(policy, max_number, min_radius))
+            min_radius: float = 0.1, stage1_walk: bool = False) -> RunCfg:
+    """stage1_walk: False = exact window classes (default), True = per-window tree walk."""
+    return RunCfg(wsize, bsize, overlap, tree_cfg(policy, max_number, min_radius), 1 if stage1_walk else 0, 0)
 
 
 class _Child:

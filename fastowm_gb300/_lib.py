@@ -49,7 +49,8 @@ class TreeInfo(C.Structure):
 
 
 class RunCfg(C.Structure):
-    _fields_ = [("wsize", u32), ("bsize", u32), ("overlap", f64), ("tree", TreeCfg)]
+    _fields_ = [("wsize", u32), ("bsize", u32), ("overlap", f64), ("tree", TreeCfg), ("stage1_walk", i32),
+                ("_pad", i32)]
 
 
 class RunInfo(C.Structure):

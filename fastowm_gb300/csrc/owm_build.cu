@@ -21,8 +21,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "owm_build.cuh"
+#include "owm_classes.cuh"
 #include "owm_devutil.cuh"
 
 namespace owm {
@@ -31,6 +33,23 @@ namespace {
 
 // Quadtree order key: x bit above y bit at each level, like the
 // reference's quadrant index (x >= cx) << 1 | (y >= cy) (optim3_func.cpp:92-100).
+// Integer form: when the domain's ends share sign and exponent, the order key
+// of a double is linear in its value over the domain, so the cell index is
+// (key(v) - key(lo)) >> shift -- no FP64 arithmetic at all.
+__global__ void k_morton_int(const double* __restrict__ xyz, int64_t n, int64_t kx0, int64_t ky0, int shx, int shy,
+                             int bits, uint32_t* __restrict__ keys) {
+  const int64_t qmax = (1ll << bits) - 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t qx = (dkey(__ldg(xyz + 3 * i)) - kx0) >> shx;
+    int64_t qy = (dkey(__ldg(xyz + 3 * i + 1)) - ky0) >> shy;
+    qx = qx < 0 ? 0 : (qx > qmax ? qmax : qx);
+    qy = qy < 0 ? 0 : (qy > qmax ? qmax : qy);
+    keys[i] = (spread_bits16((uint32_t)qx) << 1) | spread_bits16((uint32_t)qy);
+  }
+}
+
+// General form (domain spans exponents): scaled FP64 offsets.
 __global__ void k_morton(const double* __restrict__ xyz, int64_t n, double ox, double oy, double scale,
                          int bits, uint32_t* __restrict__ keys) {
   const float qmax = (float)((1u << bits) - 1u);
@@ -44,16 +63,20 @@ __global__ void k_morton(const double* __restrict__ xyz, int64_t n, double ox, d
   }
 }
 
-// One warp per unit of max(L, 32) sorted positions.  L in {1,2,4,...,1024}.
-template <int L>
+// One warp per unit of max(L, 32) sorted positions.  L in {1,2,4,...,256}.
+// With kCls, every chunk of 32 gathered points is also folded into the
+// stage-1 window classes (the point is already in registers; this kernel is
+// DRAM-bound, so the classification costs next to nothing here).
+template <int L, bool kCls>
 __global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict__ xyz, const uint32_t* __restrict__ perm,
                                                        int64_t n, int32_t nleaves, double ox, double oy,
                                                        int64_t* __restrict__ xk, int64_t* __restrict__ yk,
                                                        int64_t* __restrict__ zk, uint32_t* __restrict__ pid,
-                                                       Node* __restrict__ leaves, uint32_t* __restrict__ status) {
+                                                       Node* __restrict__ leaves, uint32_t* __restrict__ status,
+                                                       ClassArgs A) {
   constexpr int kUnit = L < 32 ? 32 : L;
-  bool finite = true;
   constexpr int kSeg = L < 32 ? L : 32;
+  bool finite = true;
   const int lane = threadIdx.x & 31;
   const int64_t nunits = (n + kUnit - 1) / kUnit;
   for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits;
@@ -63,15 +86,27 @@ __global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict_
 #pragma unroll
     for (int c = 0; c < kUnit; c += 32) {
       int64_t pos = u * kUnit + c + lane;
-      if (pos < n) {
+      const bool valid = pos < n;
+      int64_t x = 0, y = 0, z = 0;
+      if (valid) {
         uint32_t src = __ldg(perm + pos);
-        int64_t x, y, z;
         finite &= load_point(xyz, src, x, y, z);
         xk[pos] = x;
         yk[pos] = y;
         zk[pos] = z;
         pid[pos] = src + 1;
         acc.add(x, y, z, src + 1, (uint32_t)pos);
+      }
+      if (kCls) {
+        if (!__all_sync(0xffffffffu, valid)) {  // ragged tail: idle lanes borrow lane 0's point
+          const int64_t bx = __shfl_sync(0xffffffffu, x, 0), by = __shfl_sync(0xffffffffu, y, 0);
+          if (!valid) {
+            x = bx;
+            y = by;
+            z = 0;
+          }
+        }
+        cls_aggregate_warp(A, pos, valid, x, y, z, lane);
       }
     }
     acc.reduce(kSeg);
@@ -262,17 +297,39 @@ int grid_for(int64_t n, int block) {
 
 template <int L>
 void launch_gather_leaves(const double* xyz, const uint32_t* perm, int64_t n, int32_t nl, double ox, double oy,
-                          TreeStore* t, uint32_t* status, cudaStream_t s) {
+                          TreeStore* t, uint32_t* status, cudaStream_t s, const ClassArgs* cls) {
   constexpr int kUnit = L < 32 ? 32 : L;
   int64_t nunits = (n + kUnit - 1) / kUnit;
   int64_t warps = nunits;
   int64_t blocks = (warps * 32 + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L><<<(unsigned)blocks, 256, 0, s>>>(xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid,
-                                                      t->nodes + (nl - 1), status));
+  if (cls) {
+    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, true><<<(unsigned)blocks, 256, 0, s>>>(
+        xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid, t->nodes + (nl - 1), status, *cls));
+  } else {
+    ClassArgs none;
+    std::memset(&none, 0, sizeof(none));
+    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, false><<<(unsigned)blocks, 256, 0, s>>>(
+        xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid, t->nodes + (nl - 1), status, none));
+  }
 }
 
 }  // namespace
+
+bool morton_int_shifts(double lo, double hi, int bits, int64_t* klo, int* shift) {
+  int64_t a = dkey(lo), b = dkey(hi);
+  int64_t ba, bb;
+  std::memcpy(&ba, &lo, 8);
+  std::memcpy(&bb, &hi, 8);
+  // same sign and same exponent field: keys are linear in the value
+  if ((ba >> 52) != (bb >> 52) || lo <= 0.0) return false;
+  uint64_t span = (uint64_t)(b - a);
+  int len = 0;
+  while (len < 64 && (span >> len) != 0) ++len;
+  *klo = a;
+  *shift = len > bits ? len - bits : 0;
+  return true;
+}
 
 int choose_key_bits(int64_t n, int policy, double side, float min_radius) {
   int b = n <= (1 << 18) ? 8 : 12;
@@ -308,7 +365,9 @@ size_t tree_scratch_bytes(int64_t n) {
 }
 
 int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
-               void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches) {
+               void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
+               const ClassArgs* cls, bool* fused) {
+  if (fused) *fused = false;
   if (n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
   if (scratch_bytes < tree_scratch_bytes(n)) return OWM_ENOMEM;
   char* sp = static_cast<char*>(scratch);
@@ -344,7 +403,14 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   t->key_bits = key_bits;
   t->n = n;
 
-  OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+  int shx = 0, shy = 0;
+  int64_t kx0 = 0, ky0 = 0;
+  if (morton_int_shifts(ox, ox + 2.0 * R, bits_axis, &kx0, &shx) &&
+      morton_int_shifts(oy, oy + 2.0 * R, bits_axis, &ky0, &shy)) {
+    OWM_LAUNCH("k_morton", s, k_morton_int<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
+  } else {
+    OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+  }
   count_launch(launches);
   bool alt = false;
   OWM_CUDA_TRY(radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches));
@@ -389,19 +455,20 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
 
   if (fixed) {
     switch (L) {
-      case 1: launch_gather_leaves<1>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 2: launch_gather_leaves<2>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 4: launch_gather_leaves<4>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 8: launch_gather_leaves<8>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 16: launch_gather_leaves<16>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 32: launch_gather_leaves<32>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 64: launch_gather_leaves<64>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 128: launch_gather_leaves<128>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
-      case 256: launch_gather_leaves<256>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s); break;
+      case 1: launch_gather_leaves<1>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 2: launch_gather_leaves<2>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 4: launch_gather_leaves<4>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 8: launch_gather_leaves<8>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 16: launch_gather_leaves<16>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 32: launch_gather_leaves<32>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 64: launch_gather_leaves<64>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 128: launch_gather_leaves<128>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
+      case 256: launch_gather_leaves<256>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
       default:
         return OWM_EINVAL;  // the API only admits powers of two up to 256
     }
     count_launch(launches);
+    if (fused && cls) *fused = true;
   } else {
     OWM_LAUNCH("k_gather", s, k_gather<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status));
     count_launch(launches);

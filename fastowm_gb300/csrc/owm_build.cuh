@@ -40,13 +40,20 @@ inline int64_t tree_node_cap(int64_t n, const owm_tree_cfg& cfg) {
 }
 
 size_t tree_scratch_bytes(int64_t n);
+// Integer Morton quantisation of [lo, hi]: true (and the key origin and
+// shift) when lo, hi > 0 share their exponent, so order keys are linear.
+bool morton_int_shifts(double lo, double hi, int bits, int64_t* klo, int* shift);
 int choose_key_bits(int64_t n, int policy, double side, float min_radius);
 
 // Builds the tree of n device points (AoS xyz) into t (whose arrays must be
 // allocated with enough capacity).  Scratch is caller-provided.
-// Non-finite input coordinates set bit 0 of *status (device word).
+// Non-finite input coordinates set bit 0 of *status (device word).  With cls,
+// the fixed-leaf gather also folds every point into the stage-1 window
+// classes (*fused says whether it did; the min-radius build does not).
+struct ClassArgs;
 int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bbox, const owm_tree_cfg& cfg, TreeStore* t,
-               void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches);
+               void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
+               const ClassArgs* cls = nullptr, bool* fused = nullptr);
 
 // Structural self-check (checkNumPoints); *h_bad = number of bad nodes.
 int check_tree(const TreeStore* t, int32_t* d_bad, cudaStream_t s, int64_t* launches, int32_t* h_bad);

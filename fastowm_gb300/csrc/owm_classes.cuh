@@ -1,0 +1,123 @@
+// Stage 1 by exact window classes (see owm_classes.cu for the method).
+//
+// Along one axis let L[j] < R[j] be the window edges (order keys, both
+// non-decreasing in j).  For a point key p
+//     s(p) = #{j : L[j] < p} + #{j : R[j] <= p}
+// is non-decreasing in p, and window i contains p (L[i] < p < R[i]) exactly
+// when s(L[i] + 1) <= s(p) <= s(R[i] - 1).  Every point therefore falls in
+// one (s_x, s_y) sub-cell, and each window is a rectangle of sub-cells.
+#pragma once
+
+#include "owm_query.cuh"
+
+namespace owm {
+
+// Everything the per-point classification needs (device pointers).
+struct ClassArgs {
+  const int64_t *Lx, *Rx, *Ly, *Ry;  // edge keys per axis
+  int32_t nx, ny;                     // window columns / rows
+  const int2 *tabx, *taby;            // class tables (q* == 0: none)
+  int64_t kx0, ky0;
+  int32_t shx, shy, qx, qy;
+  int32_t tx, ty;                     // sub-cell grid: 2*nx+1 by 2*ny+1
+  uint32_t* count;                    // [tx*ty] points per sub-cell
+  unsigned long long* zmin;           // [tx*ty] min z (order key, sign-flipped)
+  uint32_t* idmin;                    // [tx*ty] min id among the min-z points
+  uint32_t* cidx;                     // [n] sub-cell of every sorted point
+  int32_t *sxl, *sxh, *syl, *syh;     // s-range of every window column / row
+  uint32_t *rc, *ri;                  // row reduction buffers [nx*ty]
+  unsigned long long* rz;
+};
+
+// Lower-bound style search of v in a[lo, hi) (non-decreasing a): first index
+// whose element is >= v (le == false) or > v (le == true).
+__device__ __forceinline__ int32_t cls_bsearch(const int64_t* a, int32_t lo, int32_t hi, int64_t v, bool le) {
+  while (lo < hi) {
+    int32_t mid = (lo + hi) >> 1;
+    int64_t m = a[mid];
+    if (le ? (m <= v) : (m < v)) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int64_t cls_wmin64(int64_t v) {
+  for (int o = 16; o >= 1; o >>= 1) v = min(v, (int64_t)__shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int64_t cls_wmax64(int64_t v) {
+  for (int o = 16; o >= 1; o >>= 1) v = max(v, (int64_t)__shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// All 32 lanes call this together, each with one point (valid or not).
+// Writes the point's sub-cell to cidx[pos] and folds (count, min z) of the
+// warp's points into the sub-cell counters with one atomic pair per group.
+__device__ __forceinline__ void cls_aggregate_warp(const ClassArgs& A, int64_t pos, bool valid, int64_t px,
+                                                   int64_t py, int64_t pz, int lane) {
+  int32_t sx = -1, sy = -1;
+  if (A.qx > 0) {  // table: one read + one compare per edge array
+    const int64_t q = (px - A.kx0) >> A.shx;
+    if (q >= 0 && q < A.qx) {
+      const int2 a = __ldg(A.tabx + q);
+      sx = a.x + (a.x < A.nx && __ldg(A.Lx + a.x) < px) + a.y + (a.y < A.nx && __ldg(A.Rx + a.y) <= px);
+    }
+  }
+  if (A.qy > 0) {
+    const int64_t q = (py - A.ky0) >> A.shy;
+    if (q >= 0 && q < A.qy) {
+      const int2 a = __ldg(A.taby + q);
+      sy = a.x + (a.x < A.ny && __ldg(A.Ly + a.x) < py) + a.y + (a.y < A.ny && __ldg(A.Ry + a.y) <= py);
+    }
+  }
+  if (__any_sync(0xffffffffu, valid && (sx < 0 || sy < 0))) {
+    // search: the warp's keys lie in [x0, x1] x [y0, y1], so every lane's
+    // answer lies between those for the range ends; lanes 0..7 find the eight
+    // bounds at once, then each lane searches its narrowed interval.
+    const int64_t x0 = cls_wmin64(px), x1 = cls_wmax64(px), y0 = cls_wmin64(py), y1 = cls_wmax64(py);
+    const int qq = lane & 7;
+    const int64_t* arr = (qq < 2) ? A.Lx : (qq < 4) ? A.Rx : (qq < 6) ? A.Ly : A.Ry;
+    const int32_t na = qq < 4 ? A.nx : A.ny;
+    const int64_t v = (qq == 0) ? x0 : (qq == 1) ? x1 : (qq == 2) ? x0 - 1 : (qq == 3) ? x1
+                    : (qq == 4) ? y0 : (qq == 5) ? y1 : (qq == 6) ? y0 - 1 : y1;
+    const int32_t bnd = cls_bsearch(arr, 0, na, v, (qq & 3) != 0);  // '<' for qq = 0, 4
+    const int32_t lx0 = __shfl_sync(0xffffffffu, bnd, 0), lx1 = __shfl_sync(0xffffffffu, bnd, 1);
+    const int32_t rx0 = __shfl_sync(0xffffffffu, bnd, 2), rx1 = __shfl_sync(0xffffffffu, bnd, 3);
+    const int32_t ly0 = __shfl_sync(0xffffffffu, bnd, 4), ly1 = __shfl_sync(0xffffffffu, bnd, 5);
+    const int32_t ry0 = __shfl_sync(0xffffffffu, bnd, 6), ry1 = __shfl_sync(0xffffffffu, bnd, 7);
+    if (sx < 0) sx = cls_bsearch(A.Lx, lx0, lx1, px, false) + cls_bsearch(A.Rx, rx0, rx1, px, true);
+    if (sy < 0) sy = cls_bsearch(A.Ly, ly0, ly1, py, false) + cls_bsearch(A.Ry, ry0, ry1, py, true);
+  }
+  const uint32_t c = (uint32_t)sy * (uint32_t)A.tx + (uint32_t)sx;
+  const unsigned long long zu = valid ? ((unsigned long long)pz ^ 0x8000000000000000ull) : ~0ull;
+  if (valid) A.cidx[pos] = c;
+  const uint32_t peers = __match_any_sync(0xffffffffu, valid ? c : 0xFFFFFFFFu);
+  if (valid) {
+    const uint32_t hi = (uint32_t)(zu >> 32), lo = (uint32_t)zu;
+    const uint32_t mh = __reduce_min_sync(peers, hi);
+    const uint32_t sub = __ballot_sync(peers, hi == mh);
+    uint32_t ml = 0xFFFFFFFFu;
+    if (hi == mh) ml = __reduce_min_sync(sub, lo);
+    ml = __shfl_sync(peers, ml, __ffs(sub) - 1);
+    if (lane == __ffs(peers) - 1) {
+      atomicAdd(A.count + c, (uint32_t)__popc(peers));
+      atomicMin(A.zmin + c, ((unsigned long long)mh << 32) | ml);
+    }
+  }
+}
+
+size_t classes_scratch_bytes(int64_t n, int32_t ncols, int32_t nrows);
+// Carves the buffers from scratch and enqueues the edge split, s-ranges,
+// class tables and counter resets for the windows of p (edge tables ex/ey).
+int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* scratch, size_t scratch_bytes,
+                    int64_t n, ClassArgs* A, cudaStream_t s, int64_t* launches);
+// Aggregation as its own pass over sorted points (when it is not fused into
+// the build's gather).
+int classes_aggregate(const ClassArgs& A, const TreeView& t, int64_t n, cudaStream_t s, int64_t* launches);
+// Tie ids, row and window reductions: stage-1 results into d_win.
+int classes_finish(const ClassArgs& A, const TreeView& t, int64_t n, const owm_params& p, uint32_t* d_win,
+                   cudaStream_t s, int64_t* launches);
+// prepare + aggregate + finish.
+int run_stage1_classes(const TreeView& t, int64_t n, const owm_params& p, const Edge* ex, const Edge* ey,
+                       uint32_t* d_win, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
+
+}  // namespace owm

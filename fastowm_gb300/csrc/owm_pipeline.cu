@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "owm_classes.cuh"
 #include "owm_ctx.cuh"
 
 namespace owm {
@@ -114,7 +115,10 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   const int64_t nc = p.ncells, ng = std::max<int64_t>(p.ngrid, 0);
   rc = tree_alloc(&c->tree, &c->tree_mem, n, cfg.tree, c->stream);
   if (rc) return rc;
-  size_t sbytes = std::max(tree_scratch_bytes(n), std::max(stage2_scratch_bytes(nc), stage3_scratch_bytes(ng)));
+  // scratch = [tree build | window classes]; stages 2 and 3 reuse it after stage 1
+  const size_t tbytes = (tree_scratch_bytes(n) + 255) & ~(size_t)255;
+  const size_t cbytes = cfg.stage1_walk ? 0 : classes_scratch_bytes(n, (int32_t)p.ncols, (int32_t)p.nrows);
+  size_t sbytes = std::max(tbytes + cbytes, std::max(stage2_scratch_bytes(nc), stage3_scratch_bytes(ng)));
   rc = c->scratch.reserve(sbytes, c->stream);
   if (rc) return rc;
   size_t obytes = 2 * al(65536 * sizeof(Edge)) + 2 * al((size_t)nc * 4) + al((size_t)std::max<int64_t>(ng, 1) * 4) +
@@ -139,12 +143,26 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   cudaStream_t s = c->stream;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[0], s));
   rc = clear_status(c);
+  ClassArgs cls;
+  if (!rc && !cfg.stage1_walk) {
+    // window edges and class tables first, so the build's gather can fold
+    // every point into its window class on the fly
+    rc = compute_edges(p, bb.min_x, bb.min_y, false, ex, ey, s, &c->launches);
+    if (!rc)
+      rc = classes_prepare(p, ex, ey, static_cast<char*>(c->scratch.ptr) + tbytes, cbytes, n, &cls, s, &c->launches);
+  }
+  bool fused = false;
   if (!rc)
-    rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, c->scratch.cap, c->d_small + kStatusSlot, s,
-                    &c->launches);
+    rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
+                    &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[1], s));
-  rc = run_stage1(c, c->tree, p, ex, ey, win);
+  if (cfg.stage1_walk) {
+    rc = run_stage1(c, c->tree, p, ex, ey, win);
+  } else {
+    if (!fused) rc = classes_aggregate(cls, c->tree.view(), n, s, &c->launches);
+    if (!rc) rc = classes_finish(cls, c->tree.view(), n, p, win, s, &c->launches);
+  }
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[2], s));
   rc = run_stage2(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches);

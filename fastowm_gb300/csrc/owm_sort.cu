@@ -152,13 +152,11 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restric
 }
 
 template <bool kHasVals, bool kIota>
-__global__ void __launch_bounds__(kBlock) k_rs_downsweep(const uint32_t* __restrict__ kin,
-                                                         const uint32_t* __restrict__ vin,
-                                                         uint32_t* __restrict__ kout,
-                                                         uint32_t* __restrict__ vout, int64_t n,
-                                                         int shift,
-                                                         const uint32_t* __restrict__ hist,
-                                                         int64_t ntiles) {
+__global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __restrict__ kin,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint32_t* __restrict__ kout,
+                                                            uint32_t* __restrict__ vout, int64_t n, int shift,
+                                                            const uint32_t* __restrict__ hist, int64_t ntiles) {
   __shared__ uint32_t s_keys[kTile];
   __shared__ uint32_t s_vals[kHasVals ? kTile : 1];
   __shared__ uint32_t s_wcnt[kWarps][kRadix];
@@ -172,15 +170,21 @@ __global__ void __launch_bounds__(kBlock) k_rs_downsweep(const uint32_t* __restr
   for (int d = threadIdx.x; d < kRadix; d += kBlock) s_glob[d] = hist[(int64_t)d * ntiles + blockIdx.x];
   __syncthreads();
 
-  uint32_t k[kItems], v[kItems];
-  uint16_t rank[kItems];
+  // keys only during ranking; values are fetched at the scatter (shorter
+  // live ranges -> 3 resident blocks per SM)
+  uint32_t k[kItems];
+  uint32_t rank[kItems / 2];  // two 16-bit ranks per word
   const uint32_t lt = lanemask_lt();
+  const bool full = warp_base + 32 * kItems <= n;
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
     int64_t p = warp_base + i * 32 + lane;
-    bool valid = p < n;
-    k[i] = valid ? kin[p] : 0u;
-    if (kHasVals) v[i] = valid ? (kIota ? (uint32_t)p : vin[p]) : 0u;
+    k[i] = (full || p < n) ? __ldg(kin + p) : 0u;
+  }
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    int64_t p = warp_base + i * 32 + lane;
+    bool valid = full || p < n;
     uint32_t d = valid ? ((k[i] >> shift) & 255u) : 256u;
     uint32_t peers = __match_any_sync(0xffffffffu, d);
     uint32_t before = valid ? s_wcnt[w][d] : 0u;
@@ -188,7 +192,11 @@ __global__ void __launch_bounds__(kBlock) k_rs_downsweep(const uint32_t* __restr
     uint32_t r = __popc(peers & lt);
     if (valid && r == 0) s_wcnt[w][d] = before + __popc(peers);
     __syncwarp();
-    rank[i] = (uint16_t)(before + r);
+    uint32_t rk = before + r;
+    if (i & 1)
+      rank[i >> 1] |= rk << 16;
+    else
+      rank[i >> 1] = rk;
   }
   __syncthreads();
   // exclusive prefix over warps per digit, then over digits (one per thread)
@@ -208,11 +216,12 @@ __global__ void __launch_bounds__(kBlock) k_rs_downsweep(const uint32_t* __restr
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
     int64_t p = warp_base + i * 32 + lane;
-    if (p < n) {
+    if (full || p < n) {
       uint32_t d = (k[i] >> shift) & 255u;
-      uint32_t pos = s_start[d] + s_wcnt[w][d] + rank[i];
+      uint32_t rk = (rank[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+      uint32_t pos = s_start[d] + s_wcnt[w][d] + rk;
       s_keys[pos] = k[i];
-      if (kHasVals) s_vals[pos] = v[i];
+      if (kHasVals) s_vals[pos] = kIota ? (uint32_t)p : __ldg(vin + p);
     }
   }
   __syncthreads();

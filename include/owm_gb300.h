@@ -222,6 +222,13 @@ typedef struct {
   uint32_t wsize, bsize;
   double overlap;
   owm_tree_cfg tree;
+  /* Stage-1 algorithm of owm_run (same result either way):
+   *  0  exact window classes over the tree's sorted points: every point is
+   *     assigned once to the sub-cell of windows that contain it, O(N);
+   *  1  warp-cooperative stackless tree walk per window with min-z pruning
+   *     (what owm_stage1 runs). */
+  int32_t stage1_walk;
+  int32_t _pad;
 } owm_run_cfg;
 
 typedef struct {

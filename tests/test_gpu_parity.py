@@ -25,11 +25,14 @@ def _cloud(F, config, n=None, w=None, h=None, tile=0, **over):
 
 
 def _run_both(F, O, ctx, xyz, bb, W, Ov, B, mn=32, policy=None, min_radius=0.1):
+    """GPU path with both stage-1 algorithms (window classes, tree walk) vs the oracle."""
     pol = F.OWM_TREE_MAX_NUMBER if policy is None else policy
     cloud = ctx.cloud(xyz, bb)
     got = ctx.run(cloud, F.run_cfg(W, Ov, B, mn, pol, min_radius))
+    walk = ctx.run(cloud, F.run_cfg(W, Ov, B, mn, pol, min_radius, stage1_walk=True))
     want, nllp = O.run(xyz, bb, W, Ov, B)
     cloud.close()
+    np.testing.assert_array_equal(walk, got)
     return got, want, nllp
 
 
@@ -136,3 +139,12 @@ def test_nonfinite_input_rejected(owm, ctx):
     assert e.value.status == -1
     xyz[77, 2] = 100.0
     ctx.run_host(xyz, bb, owm.run_cfg(W, Ov, B, mn))  # context still usable
+
+
+def test_header_bbox_narrower_than_data(owm, oracle, ctx):
+    """The reference takes the bbox from the file header; points may fall
+    outside it (class tables then fall back to searching)."""
+    xyz, bb, W, Ov, B, mn = _cloud(owm, 1, n=150_000, w=70, h=90)
+    hb = owm.Bbox(bb.min_x + 3.3, bb.min_y + 1.7, bb.max_x - 2.1, bb.max_y - 4.4)
+    got, want, _ = _run_both(owm, oracle, ctx, xyz, hb, W, Ov, B, mn)
+    np.testing.assert_array_equal(got, want)
