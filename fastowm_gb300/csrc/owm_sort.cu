@@ -235,6 +235,169 @@ __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __re
   }
 }
 
+// ---- pipelined downsweep ------------------------------------------------------
+// Persistent form of the downsweep: each block walks tiles blockIdx.x,
+// blockIdx.x + grid, ...  While one tile is ranked and scattered, the next
+// tile's keys, values and digit offsets are already being copied into shared
+// memory with cp.async (double buffer), so global latency is off the critical
+// path.  cp.async.wait_group is a hardware wait on this thread's own copies.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <bool kLoadVals>
+__device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, int64_t n,
+                                         int64_t t, int64_t ntiles, const uint32_t* __restrict__ hist,
+                                         uint32_t* sk, uint32_t* sv, uint32_t* sg) {
+  const int64_t base = t * kTile;
+  const int64_t tn = n - base < kTile ? n - base : kTile;
+  if (tn == kTile) {
+    for (int c = threadIdx.x; c < kTile / 4; c += kBlock) {
+      cp_async16(sk + 4 * c, kin + base + 4 * c);
+      if (kLoadVals) cp_async16(sv + 4 * c, vin + base + 4 * c);
+    }
+  } else {
+    for (int i = threadIdx.x; i < tn; i += kBlock) {
+      cp_async4(sk + i, kin + base + i);
+      if (kLoadVals) cp_async4(sv + i, vin + base + i);
+    }
+  }
+  for (int d = threadIdx.x; d < kRadix; d += kBlock) cp_async4(sg + d, hist + (int64_t)d * ntiles + t);
+}
+
+template <bool kHasVals, bool kIota>
+__global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t* __restrict__ kin,
+                                                                 const uint32_t* __restrict__ vin,
+                                                                 uint32_t* __restrict__ kout,
+                                                                 uint32_t* __restrict__ vout, int64_t n, int shift,
+                                                                 const uint32_t* __restrict__ hist, int64_t ntiles) {
+  constexpr bool kLoadVals = kHasVals && !kIota;
+  extern __shared__ __align__(16) uint32_t dsm[];
+  uint32_t* in_k = dsm;                                   // [2][kTile]
+  uint32_t* in_v = in_k + 2 * kTile;                      // [2][kTile] when kLoadVals
+  uint32_t* out_k = in_v + (kLoadVals ? 2 * kTile : 0);   // [kTile]
+  uint32_t* out_v = out_k + kTile;                        // [kTile] when kHasVals
+  uint32_t* wcnt = out_v + (kHasVals ? kTile : 0);        // [kWarps][kRadix]
+  uint32_t* st_ = wcnt + kWarps * kRadix;                 // [kRadix] tile-local digit starts
+  uint32_t* glob = st_ + kRadix;                          // [2][kRadix] global digit offsets
+
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t lt = lanemask_lt();
+  const int64_t G = gridDim.x;
+  int64_t t = blockIdx.x;
+  if (t < ntiles) rs_issue<kLoadVals>(kin, vin, n, t, ntiles, hist, in_k, in_v, glob);
+  cp_async_commit();
+  if (t + G < ntiles) rs_issue<kLoadVals>(kin, vin, n, t + G, ntiles, hist, in_k + kTile, in_v + kTile, glob + kRadix);
+  cp_async_commit();
+  for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) wcnt[i] = 0;
+
+  for (int it = 0; t < ntiles; ++it, t += G) {
+    const int stg = it & 1;
+    const uint32_t* sk = in_k + stg * kTile;
+    const uint32_t* sv = in_v + stg * kTile;
+    const uint32_t* sg = glob + stg * kRadix;
+    const int64_t tile_base = t * kTile;
+    const int32_t tn = (int32_t)(n - tile_base < kTile ? n - tile_base : kTile);
+    cp_async_wait1();  // this thread's copies of tile t have landed
+    __syncthreads();   // ... and everybody else's
+
+    uint32_t k[kItems];
+    uint32_t rank[kItems / 2];
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) k[i] = sk[w * 32 * kItems + i * 32 + lane];
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int32_t lp = w * 32 * kItems + i * 32 + lane;
+      const bool valid = lp < tn;
+      const uint32_t d = valid ? ((k[i] >> shift) & 255u) : 256u;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t before = valid ? wcnt[w * kRadix + d] : 0u;
+      __syncwarp();
+      const uint32_t r = __popc(peers & lt);
+      if (valid && r == 0) wcnt[w * kRadix + d] = before + __popc(peers);
+      __syncwarp();
+      const uint32_t rk = before + r;
+      if (i & 1)
+        rank[i >> 1] |= rk << 16;
+      else
+        rank[i >> 1] = rk;
+    }
+    __syncthreads();
+    uint32_t tot = 0;
+    {
+      const int d = threadIdx.x;  // kBlock == kRadix
+#pragma unroll
+      for (int q = 0; q < kWarps; ++q) {
+        const uint32_t c = wcnt[q * kRadix + d];
+        wcnt[q * kRadix + d] = tot;
+        tot += c;
+      }
+    }
+    const uint32_t start = block_excl_scan(tot, nullptr);
+    st_[threadIdx.x] = start;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int32_t lp = w * 32 * kItems + i * 32 + lane;
+      if (lp < tn) {
+        const uint32_t d = (k[i] >> shift) & 255u;
+        const uint32_t rk = (rank[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+        const uint32_t pos = st_[d] + wcnt[w * kRadix + d] + rk;
+        out_k[pos] = k[i];
+        if (kHasVals) out_v[pos] = kIota ? (uint32_t)(tile_base + lp) : sv[lp];
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) wcnt[i] = 0;  // for the next tile
+    for (int j = threadIdx.x; j < tn; j += kBlock) {
+      const uint32_t key = out_k[j];
+      const uint32_t d = (key >> shift) & 255u;
+      const uint32_t gp = sg[d] + (uint32_t)j - st_[d];
+      kout[gp] = key;
+      if (kHasVals) vout[gp] = out_v[j];
+    }
+    __syncthreads();  // stage stg and the staging buffers are free again
+    if (t + 2 * G < ntiles)
+      rs_issue<kLoadVals>(kin, vin, n, t + 2 * G, ntiles, hist, in_k + stg * kTile, in_v + stg * kTile,
+                          glob + stg * kRadix);
+    cp_async_commit();
+  }
+}
+
+template <bool kHasVals, bool kIota>
+size_t pipe_smem_bytes() {
+  constexpr bool kLoadVals = kHasVals && !kIota;
+  return sizeof(uint32_t) * (2 * kTile + (kLoadVals ? 2 * kTile : 0) + kTile + (kHasVals ? kTile : 0) +
+                             kWarps * kRadix + kRadix + 2 * kRadix);
+}
+
+template <bool kHasVals, bool kIota>
+cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int64_t n, int shift,
+                        const uint32_t* hist, int64_t ntiles, cudaStream_t s) {
+  static int configured = -1;  // per template instance; device-independent attribute
+  const size_t smem = pipe_smem_bytes<kHasVals, kIota>();
+  if (configured != 1) {
+    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = 1;
+  }
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * 2);
+  OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep_pipe<kHasVals, kIota><<<(unsigned)grid, kBlock, smem, s>>>(
+      kin, vin, kout, vout, n, shift, hist, ntiles));
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 size_t scan_temp_bytes(int64_t n) {
@@ -285,7 +448,15 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
     OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, hist, ntiles));
     cudaError_t e = exclusive_scan_u32(hist, hist, hn, nullptr, stemp, sbytes, s, launches);
     if (e != cudaSuccess) return e;
-    if (has_vals) {
+    if (ntiles >= 64) {  // large sorts: persistent, double-buffered downsweep
+      cudaError_t e2;
+      if (has_vals)
+        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, n, shift, hist, ntiles, s)
+                                  : launch_pipe<true, false>(ka, va, kb, vb, n, shift, hist, ntiles, s);
+      else
+        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles, s);
+      if (e2 != cudaSuccess) return e2;
+    } else if (has_vals) {
       if (first && iota_vals)
         OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
       else
