@@ -220,6 +220,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--tiles", type=int, default=512, help="batched-tiles workload size")
     args = ap.parse_args()
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":
@@ -296,6 +299,9 @@ def main():
                "h2d_bytes_per_step": int(spec.n * 24), "d2h_bytes_per_step": int(nseed * 8 + 32),
                "ms_per_step": round(ems / args.steps, 3)}
 
+    batched = None if args.no_batched else run_batched(F, torch, ctx, args, local, ws)
+    served = None if (args.no_served or ws > 1) else run_served(F, torch, ctx, args, local)
+
     # ---- roofline of the dominant kernel --------------------------------------------------------
     peak, peak_kind = peaks()
     roof = None
@@ -335,11 +341,155 @@ def main():
                                 "launches_per_step": v[1] / args.steps} for k, v in
                             sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "batched": batched, "served": served,
                 "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     cloud.close()
     ctx.close()
     barrier(ws)
+
+
+def _device_tiles(F, torch, config, ntiles, local, first=0):
+    """Generates tiles into one device buffer, back to back (the batch uses it
+    in place).  Returns (device tensor, descs info list)."""
+    specs = [F.synth_config(config, t) for t in range(first, first + ntiles)]
+    total = sum(s[0].n for s in specs)
+    host = np.empty((total, 3), dtype=np.float64)
+    info, off = [], 0
+    for spec, W, Ov, B, mn, seed in specs:
+        xyz, bb = F.synth_cloud(spec, seed, out=host[off:off + spec.n])
+        info.append((off, spec.n, bb, F.run_cfg(W, Ov, B, mn)))
+        off += spec.n
+    dev = torch.from_numpy(host).to(f"cuda:{local}")
+    return dev, info, host
+
+
+def run_batched(F, torch, ctx, args, local, ws):
+    """Config 4: 512 uneven tiles in one batch vs the plain one-tile-per-launch path."""
+    import ctypes as C
+
+    from fastowm_gb300 import autotune
+    from fastowm_gb300._lib import TileDesc
+
+    dev, info, _ = _device_tiles(F, torch, 4, args.tiles, local)
+    total = sum(n for _, n, _, _ in info)
+    base = dev.data_ptr()
+    descs = (TileDesc * len(info))()
+    cap = 0
+    for t, (off, n, bb, cfg) in enumerate(info):
+        descs[t] = TileDesc(C.cast(base + 24 * off, C.POINTER(C.c_double)), n, bb, cfg)
+        p = F.params(bb, n, cfg.wsize, cfg.overlap, cfg.bsize)
+        cap += p.ncells + p.ngrid + 1
+    out = np.empty(cap, dtype=np.int64)
+    offs = np.empty(len(info) + 1, dtype=np.int64)
+    tuned = autotune.tune_leaf_classes(ctx, tiles_per_class=4, reps=2)
+    batch = F.Batch(ctx)
+    autotune.apply(batch, tuned)
+    batch.set_graphs(True)
+
+    def run_once():
+        rc = F.lib().owm_batch_run(batch.handle, descs, len(info), out.ctypes.data_as(C.POINTER(C.c_int64)), cap,
+                                   offs.ctypes.data_as(C.POINTER(C.c_int64)), None)
+        if rc:
+            raise F.OwmError(rc, "batch_run")
+
+    for _ in range(2):
+        run_once()
+    torch.cuda.synchronize()
+    steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        run_once()
+    torch.cuda.synchronize()
+    tb = (time.perf_counter() - t0) / steps
+    batched_seeds = int(offs[-1])
+    # plain path: one owm_run per tile on device-resident clouds
+    clouds = []
+    for off, n, bb, cfg in info:
+        h = C.c_void_p()
+        rc = F.lib().owm_cloud_create(ctx.handle, C.cast(base + 24 * off, C.POINTER(C.c_double)), n, C.byref(bb),
+                                      C.byref(h))
+        if rc:
+            raise F.OwmError(rc, "cloud_create")
+        clouds.append(F.Cloud(ctx, h, n, bb))
+    for c, (_, _, _, cfg) in zip(clouds[:8], info[:8]):
+        ctx.run(c, cfg)
+    lat = []
+    plain_seeds = 0
+    t0 = time.perf_counter()
+    for c, (_, _, _, cfg) in zip(clouds, info):
+        a = time.perf_counter()
+        plain_seeds += len(ctx.run(c, cfg))
+        lat.append(1e3 * (time.perf_counter() - a))
+    tp = time.perf_counter() - t0
+    for c in clouds:
+        c.close()
+    batch.close()
+    del dev
+    return {"workload": f"config 4: {len(info)} tiles, {total} FP64 points, counts log-uniform [50k, 2M], "
+                        f"W 8-16, overlap 0.8, B 20",
+            "batched_mpts": round(total / tb / 1e6, 2), "batched_ms": round(1e3 * tb, 3),
+            "per_tile_mpts": round(total / tp / 1e6, 2), "per_tile_ms_total": round(1e3 * tp, 3),
+            "speedup": round(tp / tb, 2), "per_tile_p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "per_tile_p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "seeds_equal": batched_seeds == plain_seeds, "leaf_classes": tuned["leaves"],
+            "class_bounds": tuned["bounds"], "graphs": True,
+            "timing": "host clock around synchronous calls, device-resident inputs"}
+
+
+def run_served(F, torch, ctx, args, local):
+    """Config 5: Poisson arrivals of uneven tiles into the continuous-batching server."""
+    pool = 48
+    specs = [F.synth_config(5, t) for t in range(pool)]
+    total = sum(s[0].n for s in specs)
+    host = torch.empty((total, 3), dtype=torch.float64, pin_memory=True).numpy()
+    tiles, off = [], 0
+    for spec, W, Ov, B, mn, seed in specs:
+        xyz, bb = F.synth_cloud(spec, seed, out=host[off:off + spec.n])
+        p = F.params(bb, spec.n, W, Ov, B)
+        tiles.append((host[off:off + spec.n], bb, F.run_cfg(W, Ov, B, mn), p.ncells + p.ngrid + 1, spec.n))
+        off += spec.n
+    # plain path from pinned host memory, one tile per call
+    for xyz, bb, cfg, _, _ in tiles[:4]:
+        ctx.run_host(xyz, bb, cfg)
+    t0 = time.perf_counter()
+    for xyz, bb, cfg, _, _ in tiles:
+        ctx.run_host(xyz, bb, cfg)
+    plain = total / (time.perf_counter() - t0) / 1e6
+    srv = F.Server(local, hbm_budget_bytes=120 << 30, max_tiles_per_batch=32, max_inflight_batches=3,
+                   max_points_per_batch=48 << 20, copy_on_submit=False)
+    for xyz, bb, cfg, cap, _ in tiles[:4]:  # warm the slots
+        srv.wait(srv.submit(xyz, bb, cfg), cap)
+    rng = np.random.default_rng(5000)
+    sweep = []
+    for lam in (50, 200, 500, 1000, 2000, float("inf")):
+        # the last point submits everything at once: the served path's saturation throughput
+        nreq = 300 if lam == float("inf") else int(min(max(30, lam * 1.0), 300))
+        arrivals = np.zeros(nreq) if lam == float("inf") else np.cumsum(rng.exponential(1.0 / lam, nreq))
+        tickets = []
+        t0 = time.perf_counter()
+        for k in range(nreq):
+            while time.perf_counter() - t0 < arrivals[k]:
+                pass
+            xyz, bb, cfg, cap, n = tiles[k % pool]
+            tickets.append((srv.submit(xyz, bb, cfg), cap, n))
+        lats, pts = [], 0
+        for tk, cap, n in tickets:
+            _, ms = srv.wait(tk, cap)
+            lats.append(ms)
+            pts += n
+        wall = time.perf_counter() - t0
+        sweep.append({"lambda_tiles_s": "saturation" if lam == float("inf") else lam, "tiles": nreq, "p50_ms": round(float(np.percentile(lats, 50)), 3),
+                      "p99_ms": round(float(np.percentile(lats, 99)), 3), "mpts_s": round(pts / wall / 1e6, 2)})
+    st = srv.stats()
+    srv.close()
+    sat = sweep[-1]["mpts_s"]
+    return {"workload": f"config 5: Poisson arrivals, {pool}-tile pool log-uniform [10k, 5M] points "
+                        f"({total} points), W 8-16, overlap 0.8, B 20, 120 GB budget",
+            "plain_per_tile_mpts": round(plain, 2), "saturation_mpts": sat,
+            "saturation_vs_plain": round(sat / plain, 2), "sweep": sweep, "batches": int(st.batches),
+            "peak_bytes": int(st.peak_bytes),
+            "latency": "submit -> result ready (host clock); inputs borrowed from pinned host memory"}
 
 
 def kernel_times(F, ctx):

@@ -330,9 +330,11 @@ class Server:
     """Continuous-batching request loop over device-resident tiles."""
 
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 120 << 30, max_tiles_per_batch: int = 64,
-                 max_inflight_batches: int = 2, max_points_per_batch: int = 64 << 20, use_graphs: bool = False):
+                 max_inflight_batches: int = 2, max_points_per_batch: int = 64 << 20, use_graphs: bool = False,
+                 copy_on_submit: bool = True):
         cfg = ServerCfg(hbm_budget_bytes, max_tiles_per_batch, max_inflight_batches, max_points_per_batch,
-                        1 if use_graphs else 0, 0)
+                        1 if use_graphs else 0, 1 if copy_on_submit else 0)
+        self._borrowed = {}  # ticket -> array kept alive while the server borrows it
         h = C.c_void_p()
         _check(lib().owm_server_create(device, C.byref(cfg), C.byref(h)), "server_create")
         self.handle = h
@@ -350,6 +352,7 @@ class Server:
         d = TileDesc(_f64p(a), a.shape[0], b, cfg)
         t = C.c_int64()
         _check(lib().owm_server_submit(self.handle, C.byref(d), C.byref(t)), "submit")
+        self._borrowed[t.value] = a
         return t.value
 
     def wait(self, ticket: int, cap: int, timeout_ms: float = 60000.0):
@@ -358,6 +361,7 @@ class Server:
         lat = C.c_double()
         _check(lib().owm_server_wait(self.handle, ticket, _i64p(out), out.size, C.byref(n), C.byref(lat),
                                      timeout_ms), "wait")
+        self._borrowed.pop(ticket, None)
         return out[: n.value].copy(), lat.value
 
     def poll(self, ticket: int, cap: int):
@@ -367,6 +371,7 @@ class Server:
         rc = lib().owm_server_poll(self.handle, ticket, _i64p(out), out.size, C.byref(n), C.byref(lat))
         if rc == OWM_EAGAIN:
             return None
+        self._borrowed.pop(ticket, None)
         _check(rc, "poll")
         return out[: n.value].copy(), lat.value
 

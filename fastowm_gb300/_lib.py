@@ -64,7 +64,7 @@ class TileDesc(C.Structure):
 
 class ServerCfg(C.Structure):
     _fields_ = [("hbm_budget_bytes", i64), ("max_tiles_per_batch", i32), ("max_inflight_batches", i32),
-                ("max_points_per_batch", i64), ("use_graphs", i32), ("_pad", i32)]
+                ("max_points_per_batch", i64), ("use_graphs", i32), ("copy_on_submit", i32)]
 
 
 class ServerStats(C.Structure):

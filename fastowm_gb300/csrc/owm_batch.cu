@@ -562,9 +562,14 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   auto at = [&](size_t off) { return B + off; };
   double* xyz = (double*)at(P.o_xyz);
   const int64_t N = P.npts;
+  // tiles already back to back in one device buffer are used in place
+  bool in_place = is_device_ptr(td[0].xyz);
+  for (int32_t t = 1; t < ntiles && in_place; ++t) in_place = td[t].xyz == td[0].xyz + 3 * P.pt_off[t];
+  if (in_place) xyz = const_cast<double*>(td[0].xyz);
   // points in (host or device sources)
   for (int32_t t = 0; t < ntiles; ++t) {
-    OWM_CUDA_TRY(cudaMemcpyAsync(xyz + 3 * P.pt_off[t], td[t].xyz, (size_t)td[t].n * 24, cudaMemcpyDefault, stream));
+    if (!in_place)
+      OWM_CUDA_TRY(cudaMemcpyAsync(xyz + 3 * P.pt_off[t], td[t].xyz, (size_t)td[t].n * 24, cudaMemcpyDefault, stream));
     TileHost th;
     th.xyz = td[t].xyz;
     owm_bbox bb = td[t].bbox;
@@ -671,6 +676,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   if (use_graphs) {
     sig.assign(reinterpret_cast<const char*>(P.meta.data()), P.meta.size() * sizeof(TileMeta));
     sig.append(reinterpret_cast<const char*>(&mem.ptr), sizeof(void*));
+    sig.append(reinterpret_cast<const char*>(&xyz), sizeof(void*));
     sig.append(reinterpret_cast<const char*>(&P.total), sizeof(P.total));
   }
   if (use_graphs && graph && sig == graph_sig) {

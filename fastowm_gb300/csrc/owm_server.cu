@@ -60,6 +60,7 @@ class PinnedPool {
     return p;
   }
   void put(void* p, size_t cls) {
+    if (!p) return;
     std::lock_guard<std::mutex> lk(mu_);
     free_[cls].push_back(p);
   }
@@ -323,12 +324,12 @@ int owm_server_submit(owm_server* s, const owm_tile_desc* tile, int64_t* ticket)
     return OWM_ENOMEM;  // this tile alone exceeds the budget
   }
   size_t bytes = (size_t)tile->n * 24;
-  r->pts = static_cast<double*>(s->pinned.get(bytes, &r->pts_cls));
-  if (!r->pts) {
+  if (!s->cfg.copy_on_submit) {
+    r->pts = nullptr;  // borrowed: the caller keeps tile->xyz alive until the result is taken
+  } else if (!(r->pts = static_cast<double*>(s->pinned.get(bytes, &r->pts_cls)))) {
     delete r;
     return OWM_ENOMEM;
-  }
-  if (is_device_ptr(tile->xyz)) {
+  } else if (is_device_ptr(tile->xyz)) {
     if (cudaMemcpy(r->pts, tile->xyz, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
       cudaGetLastError();
       s->pinned.put(r->pts, r->pts_cls);
@@ -338,7 +339,7 @@ int owm_server_submit(owm_server* s, const owm_tile_desc* tile, int64_t* ticket)
   } else {
     std::memcpy(r->pts, tile->xyz, bytes);
   }
-  r->desc.xyz = r->pts;
+  if (r->pts) r->desc.xyz = r->pts;
   r->t_submit = now_ms();
   {
     std::lock_guard<std::mutex> lk(s->mu);

@@ -265,7 +265,9 @@ typedef struct {
 int owm_batch_create(owm_ctx* ctx, owm_batch** out);
 int owm_batch_destroy(owm_batch* b);
 /* Runs ntiles tiles; seeds of tile t are seeds[offsets[t] .. offsets[t+1])
- * (offsets has ntiles+1 entries).  cap = total room in seeds. */
+ * (offsets has ntiles+1 entries).  cap = total room in seeds.  Tiles whose
+ * points already lie back to back in one device buffer (tile t+1 starting
+ * right after tile t) are used in place; anything else is copied in. */
 int owm_batch_run(owm_batch* b, const owm_tile_desc* tiles, int32_t ntiles, int64_t* seeds,
                   int64_t cap, int64_t* offsets, owm_run_info* total_info);
 /* Capture the batch's device work into a CUDA graph keyed by the tile
@@ -284,13 +286,16 @@ typedef struct {
   int32_t max_inflight_batches; /* batches overlapping on the device */
   int64_t max_points_per_batch;
   int32_t use_graphs;
-  int32_t _pad;
+  /* 1: copy each tile's points into pinned staging at submit (the caller may
+   * reuse its buffer at once); 0: borrow the caller's buffer until the ticket
+   * is polled/waited (pinned host or device memory is fastest). */
+  int32_t copy_on_submit;
 } owm_server_cfg;
 
 int owm_server_create(int device, const owm_server_cfg* cfg, owm_server** out);
 int owm_server_destroy(owm_server* s);
-/* Enqueue a tile (points copied to pinned staging at submit); *ticket
- * identifies it.  OWM_ENOMEM if the tile alone exceeds the budget. */
+/* Enqueue a tile; *ticket identifies it.  OWM_ENOMEM if the tile alone
+ * exceeds the budget. */
 int owm_server_submit(owm_server* s, const owm_tile_desc* tile, int64_t* ticket);
 /* OWM_EAGAIN until done; then copies up to cap seeds, sets *n_seeds and
  * the tile's latency (submit -> result ready, ms) and releases it. */
