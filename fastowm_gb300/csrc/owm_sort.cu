@@ -252,37 +252,58 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-template <bool kLoadVals>
-__device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, int64_t n,
-                                         int64_t t, int64_t ntiles, const uint32_t* __restrict__ hist,
-                                         uint32_t* sk, uint32_t* sv, uint32_t* sg) {
-  const int64_t base = t * kTile;
-  const int64_t tn = n - base < kTile ? n - base : kTile;
-  if (tn == kTile) {
-    for (int c = threadIdx.x; c < kTile / 4; c += kBlock) {
-      cp_async16(sk + 4 * c, kin + base + 4 * c);
-      if (kLoadVals) cp_async16(sv + 4 * c, vin + base + 4 * c);
-    }
-  } else {
-    for (int i = threadIdx.x; i < tn; i += kBlock) {
-      cp_async4(sk + i, kin + base + i);
-      if (kLoadVals) cp_async4(sv + i, vin + base + i);
-    }
+// Tile map of the persistent downsweep: tile t = keys [t*kTile, ...), its
+// digit offsets at hist[d*ntiles + t].
+struct FlatMap {
+  int64_t n, ntiles;
+  __device__ __forceinline__ int64_t count() const { return ntiles; }
+  __device__ __forceinline__ void tile(int64_t t, int64_t* base, int32_t* size, int64_t* ob, int64_t* os) const {
+    *base = t * kTile;
+    *size = (int32_t)(n - *base < kTile ? n - *base : kTile);
+    *ob = t;
+    *os = ntiles;
   }
-  for (int d = threadIdx.x; d < kRadix; d += kBlock) cp_async4(sg + d, hist + (int64_t)d * ntiles + t);
+};
+// Copies tile t into shared memory.  Element i of the tile goes to slot
+// i + (base & 3), so global and shared addresses agree modulo 16 bytes and
+// the bulk of the tile moves with 16-byte cp.async whatever the tile's start.
+// Slots outside the tile may receive neighbouring keys; they are never read.
+// Stage buffers hold kTile + 4 slots.
+template <bool kLoadVals, class Map>
+__device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, const Map& m,
+                                         int64_t t, int64_t n, const uint32_t* __restrict__ hist, uint32_t* sk,
+                                         uint32_t* sv, uint32_t* sg) {
+  int64_t base, ob, os;
+  int32_t tn;
+  m.tile(t, &base, &tn, &ob, &os);
+  const int r = (int)(base & 3);
+  const int64_t a0 = base - r;                       // 16-byte aligned
+  const int64_t a1 = base + tn;                      // one past the tile
+  const int64_t full_end = a1 & ~(int64_t)3;         // last full 16-byte chunk inside the tile
+  const int nfull = (int)((full_end - a0) >> 2);     // chunks [a0, full_end)
+  for (int c = threadIdx.x; c < nfull; c += kBlock) {
+    cp_async16(sk + 4 * c, kin + a0 + 4 * c);
+    if (kLoadVals) cp_async16(sv + 4 * c, vin + a0 + 4 * c);
+  }
+  for (int64_t g = full_end + threadIdx.x; g < a1 && g < n; g += kBlock) {  // ragged tail
+    cp_async4(sk + (g - a0), kin + g);
+    if (kLoadVals) cp_async4(sv + (g - a0), vin + g);
+  }
+  for (int d = threadIdx.x; d < kRadix; d += kBlock) cp_async4(sg + d, hist + ob + (int64_t)d * os);
 }
 
-template <bool kHasVals, bool kIota>
+template <bool kHasVals, bool kIota, class Map>
 __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t* __restrict__ kin,
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
-                                                                 uint32_t* __restrict__ vout, int64_t n, int shift,
-                                                                 const uint32_t* __restrict__ hist, int64_t ntiles) {
+                                                                 uint32_t* __restrict__ vout, int shift, Map m,
+                                                                 const uint32_t* __restrict__ hist, int64_t n) {
   constexpr bool kLoadVals = kHasVals && !kIota;
   extern __shared__ __align__(16) uint32_t dsm[];
-  uint32_t* in_k = dsm;                                   // [2][kTile]
-  uint32_t* in_v = in_k + 2 * kTile;                      // [2][kTile] when kLoadVals
-  uint32_t* out_k = in_v + (kLoadVals ? 2 * kTile : 0);   // [kTile]
+  constexpr int kStage = kTile + 4;                       // slots per stage (alignment shift)
+  uint32_t* in_k = dsm;                                   // [2][kStage]
+  uint32_t* in_v = in_k + 2 * kStage;                     // [2][kStage] when kLoadVals
+  uint32_t* out_k = in_v + (kLoadVals ? 2 * kStage : 0);  // [kTile]
   uint32_t* out_v = out_k + kTile;                        // [kTile] when kHasVals
   uint32_t* wcnt = out_v + (kHasVals ? kTile : 0);        // [kWarps][kRadix]
   uint32_t* st_ = wcnt + kWarps * kRadix;                 // [kRadix] tile-local digit starts
@@ -291,20 +312,23 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = lanemask_lt();
   const int64_t G = gridDim.x;
+  const int64_t ntiles = m.count();
   int64_t t = blockIdx.x;
-  if (t < ntiles) rs_issue<kLoadVals>(kin, vin, n, t, ntiles, hist, in_k, in_v, glob);
+  if (t < ntiles) rs_issue<kLoadVals>(kin, vin, m, t, n, hist, in_k, in_v, glob);
   cp_async_commit();
-  if (t + G < ntiles) rs_issue<kLoadVals>(kin, vin, n, t + G, ntiles, hist, in_k + kTile, in_v + kTile, glob + kRadix);
+  if (t + G < ntiles) rs_issue<kLoadVals>(kin, vin, m, t + G, n, hist, in_k + kStage, in_v + kStage, glob + kRadix);
   cp_async_commit();
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) wcnt[i] = 0;
 
   for (int it = 0; t < ntiles; ++it, t += G) {
     const int stg = it & 1;
-    const uint32_t* sk = in_k + stg * kTile;
-    const uint32_t* sv = in_v + stg * kTile;
+    int64_t tile_base, ob, os;
+    int32_t tn;
+    m.tile(t, &tile_base, &tn, &ob, &os);
+    const int sh = (int)(tile_base & 3);  // alignment shift of this tile's slots
+    const uint32_t* sk = in_k + stg * kStage + sh;
+    const uint32_t* sv = in_v + stg * kStage + sh;
     const uint32_t* sg = glob + stg * kRadix;
-    const int64_t tile_base = t * kTile;
-    const int32_t tn = (int32_t)(n - tile_base < kTile ? n - tile_base : kTile);
     cp_async_wait1();  // this thread's copies of tile t have landed
     __syncthreads();   // ... and everybody else's
 
@@ -365,7 +389,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     }
     __syncthreads();  // stage stg and the staging buffers are free again
     if (t + 2 * G < ntiles)
-      rs_issue<kLoadVals>(kin, vin, n, t + 2 * G, ntiles, hist, in_k + stg * kTile, in_v + stg * kTile,
+      rs_issue<kLoadVals>(kin, vin, m, t + 2 * G, n, hist, in_k + stg * kStage, in_v + stg * kStage,
                           glob + stg * kRadix);
     cp_async_commit();
   }
@@ -374,27 +398,27 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
 template <bool kHasVals, bool kIota>
 size_t pipe_smem_bytes() {
   constexpr bool kLoadVals = kHasVals && !kIota;
-  return sizeof(uint32_t) * (2 * kTile + (kLoadVals ? 2 * kTile : 0) + kTile + (kHasVals ? kTile : 0) +
+  return sizeof(uint32_t) * (2 * (kTile + 4) + (kLoadVals ? 2 * (kTile + 4) : 0) + kTile + (kHasVals ? kTile : 0) +
                              kWarps * kRadix + kRadix + 2 * kRadix);
 }
 
-template <bool kHasVals, bool kIota>
-cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int64_t n, int shift,
-                        const uint32_t* hist, int64_t ntiles, cudaStream_t s) {
-  static int configured = -1;  // per template instance; device-independent attribute
+template <bool kHasVals, bool kIota, class Map>
+cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int shift,
+                        const Map& m, int64_t max_tiles, const uint32_t* hist, int64_t n, cudaStream_t s) {
+  static bool configured = false;  // per template instance
   const size_t smem = pipe_smem_bytes<kHasVals, kIota>();
-  if (configured != 1) {
-    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota>,
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota, Map>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured = 1;
+    configured = true;
   }
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * 2);
-  OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep_pipe<kHasVals, kIota><<<(unsigned)grid, kBlock, smem, s>>>(
-      kin, vin, kout, vout, n, shift, hist, ntiles));
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(max_tiles, (int64_t)sms * 2));
+  OWM_LAUNCH("k_rs_downsweep", s, (k_rs_downsweep_pipe<kHasVals, kIota, Map><<<(unsigned)grid, kBlock, smem, s>>>(
+      kin, vin, kout, vout, shift, m, hist, n)));
   return cudaGetLastError();
 }
 
@@ -450,11 +474,12 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
     if (e != cudaSuccess) return e;
     if (ntiles >= 64) {  // large sorts: persistent, double-buffered downsweep
       cudaError_t e2;
+      FlatMap fm{n, ntiles};
       if (has_vals)
-        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, n, shift, hist, ntiles, s)
-                                  : launch_pipe<true, false>(ka, va, kb, vb, n, shift, hist, ntiles, s);
+        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, shift, fm, ntiles, hist, n, s)
+                                  : launch_pipe<true, false>(ka, va, kb, vb, shift, fm, ntiles, hist, n, s);
       else
-        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles, s);
+        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, shift, fm, ntiles, hist, n, s);
       if (e2 != cudaSuccess) return e2;
     } else if (has_vals) {
       if (first && iota_vals)

@@ -148,3 +148,11 @@ def test_header_bbox_narrower_than_data(owm, oracle, ctx):
     hb = owm.Bbox(bb.min_x + 3.3, bb.min_y + 1.7, bb.max_x - 2.1, bb.max_y - 4.4)
     got, want, _ = _run_both(owm, oracle, ctx, xyz, hb, W, Ov, B, mn)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("policy,mn,mr", [(1, 32, 0.1), (1, 16, 0.1), (1, 128, 0.1), (0, 32, 0.4)])
+def test_large_cloud_policies(owm, oracle, ctx, policy, mn, mr):
+    """1.5 M points (persistent pipelined sort), both leaf policies, both stage-1 algorithms."""
+    xyz, bb, W, Ov, B, _ = _cloud(owm, 1, n=1_500_000, w=240, h=310)
+    got, want, _ = _run_both(owm, oracle, ctx, xyz, bb, W, Ov, B, mn, policy, mr)
+    np.testing.assert_array_equal(got, want)
