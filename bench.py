@@ -171,10 +171,11 @@ def cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads: int):
                                  want_win=False)
         t = res.t_tree + res.t_owm
         return n / t / 1e6, "reference", t
+    # C port of the same quadtree algorithm (oracle/owm_refport.c), timed the
+    # same way: tree build + stages 1-3, cloud already in memory
     O.build(ref=False)
-    t0 = time.perf_counter()
-    O.run(xyz, bb, W, Ov, B, nthreads=threads)
-    t = time.perf_counter() - t0
+    _, _, tt, to = O.port_run(xyz, bb, W, Ov, B, max_number=mn, level=5, nthreads=threads)
+    t = tt + to
     return n / t / 1e6, "port", t
 
 

@@ -3,6 +3,9 @@
 * ``liboracle.so``      my C restatement of the OWM path (owm_oracle.c)
 * ``_ref/libowmref.so`` the reference's own CPP-TBB-CPU/src/optim3_func.cpp
                         compiled in place (ref_runner.cpp + shim/)
+* ``librefport.so``     C port of that reference algorithm (owm_refport.c):
+                        the timed CPU baseline where the reference sources
+                        are not there to compile
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 this module, as the checker; the product never imports it.
@@ -19,6 +22,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_ORACLE = HERE / "liboracle.so"
 LIB_REF = HERE / "_ref" / "libowmref.so"
+LIB_PORT = HERE / "librefport.so"
 REF_SRC = Path(os.environ.get("OWM_REFERENCE", "/root/reference"))
 
 
@@ -49,6 +53,7 @@ def build(ref: bool | None = None) -> None:
 
 _o = None
 _r = None
+_p = None
 
 
 def _oracle():
@@ -72,6 +77,20 @@ def _oracle():
         _o.oracle_window_box.argtypes = [P(OracleParams), C.c_int64, C.c_int64, P(C.c_double)]
         _o.oracle_cell_box.argtypes = [P(OracleParams), C.c_int64, C.c_int64, P(C.c_double)]
     return _o
+
+
+def _port():
+    global _p
+    if _p is None:
+        if not LIB_PORT.exists():
+            build(ref=False)
+        _p = C.CDLL(str(LIB_PORT))
+        P = C.POINTER
+        _p.refport_run.argtypes = [P(C.c_double), C.c_int64, P(C.c_double), C.c_uint32, C.c_double, C.c_uint32,
+                                   C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, P(C.c_int64), C.c_int64, P(C.c_int64),
+                                   P(C.c_double), P(C.c_double)]
+        _p.refport_run.restype = C.c_int64
+    return _p
 
 
 def ref_available() -> bool:
@@ -179,3 +198,17 @@ def ref_run(xyz, bbox, W: int, O: float, B: int, policy: int = 1, min_radius: fl
         raise RuntimeError(f"reference run failed ({rc})")
     n = res.n_llp + res.n_stage3
     return seeds[:n].astype(np.int64), res.n_llp, (win.astype(np.int64) if want_win else None), res
+
+
+def port_run(xyz, bbox, W: int, O: float, B: int, policy: int = 1, max_number: int = 32, min_radius: float = 0.1,
+             level: int = 5, nthreads: int = 1):
+    """C port of the reference algorithm: (seeds = stage-3 ids ++ LLPs, n_llp, t_tree s, t_owm s)."""
+    a = np.ascontiguousarray(xyz, dtype=np.float64)
+    p = params(bbox, a.shape[0], W, O, B)
+    out = np.empty(p.ncells + max(p.ngrid, 0) + 1, dtype=np.int64)
+    nllp, tt, to = C.c_int64(), C.c_double(), C.c_double()
+    n = _port().refport_run(_d(a), a.shape[0], _d(_bbox_arr(bbox)), W, O, B, policy, max_number, min_radius, level, nthreads,
+                            _q(out), out.size, C.byref(nllp), C.byref(tt), C.byref(to))
+    if n < 0:
+        raise RuntimeError("reference port run failed")
+    return out[:n].copy(), nllp.value, tt.value, to.value

@@ -102,3 +102,19 @@ def test_gpu_matches_golden(owm, ctx, name):
     np.testing.assert_array_equal(seeds, np.concatenate([es, el]))
     t.close()
     c.close()
+
+
+@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if "reference" in c))
+def test_reference_port_matches_golden(owm, oracle, name):
+    """The C port of the reference's quadtree algorithm (the timed CPU
+    baseline on machines without the reference sources) returns the
+    reference's seeds exactly, ties included: same tree, same visiting order."""
+    case = CASES[name]
+    xyz, bb = cloud(owm, case)
+    ref = case["reference"]
+    seeds, n_llp, _, _ = oracle.port_run(xyz, bb, case["wsize"], case["overlap"], case["bsize"],
+                                         policy=case["policy"], max_number=case["max_number"], nthreads=2)
+    assert n_llp == ref["n_llp"]
+    n3 = len(seeds) - n_llp  # seeds = stage-3 ids ++ LLPs
+    np.testing.assert_array_equal(seeds[n3:], unpack(ref["llp"]))
+    np.testing.assert_array_equal(seeds[:n3], unpack(ref["stage3"]))
