@@ -25,7 +25,7 @@ import weakref
 import numpy as np
 
 from . import _lib
-from ._lib import (OWM_EAGAIN, OWM_OK, OWM_TREE_MAX_NUMBER, OWM_TREE_MIN_RADIUS, Bbox, Params, RunCfg, RunInfo,  # noqa: F401
+from ._lib import (OWM_EAGAIN, OWM_ECUDA, OWM_OK, OWM_TREE_MAX_NUMBER, OWM_TREE_MIN_RADIUS, Bbox, Params, RunCfg, RunInfo,  # noqa: F401
                    ServerCfg, ServerStats, SynthSpec, TileDesc, TreeCfg, TreeInfo)
 
 __all__ = ["OwmError", "round2d", "params", "bbox_of", "read_xyz", "write_xyz_ids", "check_results",
@@ -36,6 +36,10 @@ class OwmError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
         msg = lib().owm_status_string(status).decode()
+        if status == OWM_ECUDA:
+            detail = lib().owm_last_error().decode()
+            if detail:
+                msg = f"{msg}: {detail}"
         super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
 
 

@@ -116,6 +116,7 @@ SIGNATURES = {
     "owm_server_wait": (C.c_int, [vp, i64, P(i64), i64, P(i64), P(f64), f64]),
     "owm_server_get_stats": (C.c_int, [vp, P(ServerStats)]),
     "owm_status_string": (C.c_char_p, [C.c_int]),
+    "owm_last_error": (C.c_char_p, []),
     "owm_version": (C.c_int, []),
 }
 

@@ -38,6 +38,10 @@ void count_launch(int64_t* ctx_counter, int64_t k) {
 
 int64_t total_launches() { return g_launches.load(); }
 
+const char* last_cuda_error() { return g_last_error.c_str(); }
+
+void set_last_error_text(const char* what) { g_last_error = what; }
+
 Profiler*& tls_profiler() {
   static thread_local Profiler* p = nullptr;
   return p;
@@ -234,6 +238,8 @@ int owm_ctx_sync(owm_ctx* c) {
 void* owm_ctx_stream(owm_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int64_t owm_ctx_launches(const owm_ctx* c) { return c ? c->launches : owm::total_launches(); }
+
+const char* owm_last_error(void) { return owm::last_cuda_error(); }
 
 int owm_ctx_device_status(owm_ctx* c, int32_t* status) {
   if (!c || !status) return OWM_EINVAL;

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restric
       acc.add(x, y, z, id, (uint32_t)lp);
     }
     acc.reduce(32);
-    if (lane == 0) write_leaf(nodes + m.node_off + (m.nleaves - 1) + j, acc, first, m.ox, m.oy);
+    write_leaf_seg(nodes + m.node_off + (m.nleaves - 1) + j, acc, first, m.ox, m.oy, 32, true);
   }
   if (!finite) atomicOr(status, kStatusNonFinite);
 }

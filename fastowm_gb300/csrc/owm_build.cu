@@ -110,12 +110,9 @@ __global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict_
       }
     }
     acc.reduce(kSeg);
-    if ((lane & (kSeg - 1)) == 0) {
-      int64_t first = u * kUnit + lane;  // L < 32: segment start; else lane 0
-      if (first < n) {
-        int64_t li = first / L;
-        write_leaf(leaves + li, acc, (int32_t)first, ox, oy);
-      }
+    {
+      const int64_t first = u * kUnit + (lane & ~(kSeg - 1));  // L < 32: segment start; else lane 0's
+      write_leaf_seg(leaves + (first < n ? first / L : 0), acc, (int32_t)first, ox, oy, kSeg, first < n);
     }
   }
   if (!finite) atomicOr(status, 1u);
@@ -175,7 +172,7 @@ __global__ void k_leaf_reduce(const int64_t* __restrict__ xk, const int64_t* __r
     acc.init();
     for (int32_t p = b + lane; p < e; p += 32) acc.add(xk[p], yk[p], zk[p], pid[p], (uint32_t)p);
     acc.reduce(32);
-    if (lane == 0) write_leaf(leaves + li, acc, b, ox, oy);
+    write_leaf_seg(leaves + li, acc, b, ox, oy, 32, true);
   }
 }
 

@@ -39,28 +39,39 @@ struct LeafAcc {
     }
     ++count;
   }
-  // reduce with lanes lane^o for o in [1, width)
+  // Reduces over aligned segments of `width` lanes (a power of two <= 32);
+  // every lane of the warp calls this, and every lane of a segment ends with
+  // the segment's result.  Uses the warp reduction unit (redux.sync, 32-bit)
+  // instead of a shuffle tree: a 64-bit min/max is the high words' signed
+  // min/max, then the low words' unsigned min/max over the lanes whose high
+  // word won.  (z, id) stays lexicographic: min z, then min id among the
+  // lanes holding it; the winner's sorted position comes from its lane.
   __device__ __forceinline__ void reduce(int width) {
-    for (int o = width >> 1; o >= 1; o >>= 1) {
-      int64_t a = __shfl_xor_sync(0xffffffffu, xmin, o);
-      int64_t b = __shfl_xor_sync(0xffffffffu, xmax, o);
-      int64_t c = __shfl_xor_sync(0xffffffffu, ymin, o);
-      int64_t d = __shfl_xor_sync(0xffffffffu, ymax, o);
-      int64_t z = __shfl_xor_sync(0xffffffffu, zmin, o);
-      uint32_t id = __shfl_xor_sync(0xffffffffu, idmin, o);
-      uint32_t ps = __shfl_xor_sync(0xffffffffu, posmin, o);
-      uint32_t ct = __shfl_xor_sync(0xffffffffu, count, o);
-      xmin = min(xmin, a);
-      xmax = max(xmax, b);
-      ymin = min(ymin, c);
-      ymax = max(ymax, d);
-      if (zid_less(z, id, zmin, idmin)) {
-        zmin = z;
-        idmin = id;
-        posmin = ps;
-      }
-      count += ct;
-    }
+    const int lane = threadIdx.x & 31;
+    const uint32_t mask = width >= 32 ? 0xFFFFFFFFu : (((1u << width) - 1u) << (lane & ~(width - 1)));
+    xmin = seg_min64(mask, xmin);
+    xmax = seg_max64(mask, xmax);
+    ymin = seg_min64(mask, ymin);
+    ymax = seg_max64(mask, ymax);
+    const int64_t zm = seg_min64(mask, zmin);
+    const uint32_t im = __reduce_min_sync(mask, zmin == zm ? idmin : 0xFFFFFFFFu);
+    const uint32_t win = __ballot_sync(mask, zmin == zm && idmin == im) & mask;
+    posmin = __shfl_sync(mask, posmin, __ffs(win) - 1);
+    zmin = zm;
+    idmin = im;
+    count = __reduce_add_sync(mask, count);
+  }
+  static __device__ __forceinline__ int64_t seg_min64(uint32_t mask, int64_t v) {
+    const int32_t hi = (int32_t)(v >> 32);
+    const int32_t mh = __reduce_min_sync(mask, hi);
+    const uint32_t ml = __reduce_min_sync(mask, hi == mh ? (uint32_t)v : 0xFFFFFFFFu);
+    return (int64_t)(((uint64_t)(uint32_t)mh << 32) | ml);
+  }
+  static __device__ __forceinline__ int64_t seg_max64(uint32_t mask, int64_t v) {
+    const int32_t hi = (int32_t)(v >> 32);
+    const int32_t mh = __reduce_max_sync(mask, hi);
+    const uint32_t ml = __reduce_max_sync(mask, hi == mh ? (uint32_t)v : 0u);
+    return (int64_t)(((uint64_t)(uint32_t)mh << 32) | ml);
   }
 };
 
@@ -78,6 +89,45 @@ __device__ __forceinline__ void write_leaf(Node* nd, const LeafAcc& a, int32_t f
   n.escape = kEnd;
   n.right = -1;
   *nd = n;
+}
+
+// Segment-cooperative form: every lane of an aligned segment of `width` lanes
+// (a power of two) calls this with the segment's reduced accumulator, and the
+// segment's first lane stores the node when `store`.  The four FP64 box
+// roundings run on four lanes at once -- FP64 issue is scarce on GB300 --
+// all as round-down: the upper bounds use ru(v - o) = -rd(o - v), which gives
+// the same bits as write_leaf.
+__device__ __forceinline__ void write_leaf_seg(Node* nd, const LeafAcc& a, int32_t first, double ox, double oy,
+                                               int width, bool store) {
+  const int lane = threadIdx.x & 31;
+  const int base = lane & ~(width - 1);
+  if (width < 4) {
+    if (store && lane == base) write_leaf(nd, a, first, ox, oy);
+    return;
+  }
+  const uint32_t mask = width >= 32 ? 0xFFFFFFFFu : (((1u << width) - 1u) << base);
+  const int c = lane - base;  // lanes c = 0..3 of the segment: x0, y0, x1, y1
+  const double p = c == 0 ? dkey_inv(a.xmin) : c == 1 ? dkey_inv(a.ymin) : c == 2 ? ox : oy;
+  const double q = c == 0 ? ox : c == 1 ? oy : c == 2 ? dkey_inv(a.xmax) : dkey_inv(a.ymax);
+  float v = __double2float_rd(__dsub_rd(p, q));
+  if (c >= 2) v = 0.0f - v;  // exact; 0 - (+0) keeps +0
+  const float x0 = __shfl_sync(mask, v, base), y0 = __shfl_sync(mask, v, base + 1);
+  const float x1 = __shfl_sync(mask, v, base + 2), y1 = __shfl_sync(mask, v, base + 3);
+  if (store && lane == base) {
+    Node n;
+    n.x0 = x0;
+    n.y0 = y0;
+    n.x1 = x1;
+    n.y1 = y1;
+    n.zmin = a.zmin;
+    n.min_id = a.idmin;
+    n.min_pos = a.posmin;
+    n.count = a.count;
+    n.left = first;
+    n.escape = kEnd;
+    n.right = -1;
+    *nd = n;
+  }
 }
 
 // Loads one input point as order keys; returns false if a coordinate is not

@@ -99,6 +99,8 @@ struct TreeView {
   } while (0)
 
 void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+void set_last_error_text(const char* what);
+const char* last_cuda_error();
 
 // Library-wide kernel launch counter (every launch of this library's kernels
 // goes through count_launch) and the per-context one.

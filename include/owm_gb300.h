@@ -313,6 +313,10 @@ int owm_server_get_stats(owm_server* s, owm_server_stats* st);
 
 /* ---- misc -------------------------------------------------------------- */
 const char* owm_status_string(int status);
+/* Detail of the last CUDA failure behind an OWM_ECUDA on the calling thread:
+ * the CUDA error text, the failing call and its source location ("" when
+ * none).  No counterpart in the reference, which exits on errors. */
+const char* owm_last_error(void);
 int owm_version(void);
 
 #ifdef __cplusplus
