@@ -317,7 +317,7 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
   cl->device = c->device;
   cl->n = n;
   cl->bbox = bb;
-  if (cl->mem.reserve((size_t)n * 24, c->stream) != OWM_OK) {
+  if (cl->mem.reserve((size_t)n * 24 + kXyzSlack, c->stream) != OWM_OK) {
     delete cl;
     return OWM_ENOMEM;
   }
@@ -536,7 +536,7 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   } else {
     owm_bbox_of(xyz, n, &bb);
   }
-  int rc = c->input.reserve((size_t)n * 24, c->stream);
+  int rc = c->input.reserve((size_t)n * 24 + kXyzSlack, c->stream);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
   return run_pipeline(c, static_cast<const double*>(c->input.ptr), n, bb, *cfg, seeds, cap, n_seeds, info);

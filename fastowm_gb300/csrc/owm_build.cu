@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict_
       int64_t x = 0, y = 0, z = 0;
       if (valid) {
         uint32_t src = __ldg(perm + pos);
-        finite &= load_point(xyz, src, x, y, z);
+        finite &= load_point16(xyz, src, x, y, z);
         xk[pos] = x;
         yk[pos] = y;
         zk[pos] = z;
@@ -126,7 +126,7 @@ __global__ void k_gather(const double* __restrict__ xyz, const uint32_t* __restr
        pos += (int64_t)gridDim.x * blockDim.x) {
     uint32_t src = __ldg(perm + pos);
     int64_t x, y, z;
-    finite &= load_point(xyz, src, x, y, z);
+    finite &= load_point16(xyz, src, x, y, z);
     xk[pos] = x;
     yk[pos] = y;
     zk[pos] = z;
@@ -366,6 +366,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
                const ClassArgs* cls, bool* fused) {
   if (fused) *fused = false;
   if (n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(d_xyz) & 15u) != 0) return OWM_EINVAL;  // the gather reads 16-byte words
   if (scratch_bytes < tree_scratch_bytes(n)) return OWM_ENOMEM;
   char* sp = static_cast<char*>(scratch);
   auto take = [&](size_t bytes) {

@@ -45,8 +45,9 @@ size_t tree_scratch_bytes(int64_t n);
 bool morton_int_shifts(double lo, double hi, int bits, int64_t* klo, int* shift);
 int choose_key_bits(int64_t n, int policy, double side, float min_radius);
 
-// Builds the tree of n device points (AoS xyz) into t (whose arrays must be
-// allocated with enough capacity).  Scratch is caller-provided.
+// Builds the tree of n device points (AoS xyz, 16-byte aligned, kXyzSlack
+// readable bytes after the last point) into t (whose arrays must be allocated
+// with enough capacity).  Scratch is caller-provided.
 // Non-finite input coordinates set bit 0 of *status (device word).  With cls,
 // the fixed-leaf gather also folds every point into the stage-1 window
 // classes (*fused says whether it did; the min-radius build does not).

@@ -130,6 +130,25 @@ __device__ __forceinline__ void write_leaf_seg(Node* nd, const LeafAcc& a, int32
   }
 }
 
+// load_point with two aligned 16-byte reads instead of three 8-byte ones (a
+// third fewer random requests in the build's gather): the point's 24 bytes lie
+// in the 32 bytes from the 16-byte boundary at or below x.  Needs a 16-byte
+// aligned xyz with kXyzSlack readable bytes after the last point.
+__device__ __forceinline__ bool load_point16(const double* __restrict__ xyz, uint32_t src, int64_t& x, int64_t& y,
+                                             int64_t& z) {
+  const int64_t e = 3 * (int64_t)src;
+  const int odd = (int)(e & 1);
+  const double2* w = reinterpret_cast<const double2*>(xyz + (e - odd));
+  const double2 a = __ldg(w), b = __ldg(w + 1);
+  const double dx = odd ? a.y : a.x, dy = odd ? b.x : a.y, dz = odd ? b.y : b.x;
+  x = dkey(dx);
+  y = dkey(dy);
+  z = dkey(dz);
+  const uint64_t m = 0x7FF0000000000000ull;
+  return ((__double_as_longlong(dx) & m) != m) & ((__double_as_longlong(dy) & m) != m) &
+         ((__double_as_longlong(dz) & m) != m);
+}
+
 // Loads one input point as order keys; returns false if a coordinate is not
 // finite (the reference's comparisons are undefined there: such input is
 // rejected through the context's status word).

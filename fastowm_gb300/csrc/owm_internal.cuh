@@ -98,6 +98,10 @@ struct TreeView {
     }                                                                               \
   } while (0)
 
+// Bytes the single-cloud point buffers keep readable past the last point, so
+// that the build's gather may read whole 16-byte words (load_point16).
+constexpr size_t kXyzSlack = 16;
+
 void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
 void set_last_error_text(const char* what);
 const char* last_cuda_error();
