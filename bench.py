@@ -12,7 +12,8 @@ points and device->host copy of the seeds inside the timed region).
 Multi-GPU (torchrun): every rank runs an independent replica of the
 workload (the path has no exchange step); value = all ranks' points / max
 rank time.  --impl reference times the reference's own CPU path (compiled
-from its sources when present, else the CPU restatement) on rank 0.
+from its sources when present, else the C port of the same quadtree
+algorithm, oracle/owm_refport.c) on rank 0.
 """
 from __future__ import annotations
 
@@ -152,12 +153,23 @@ def kernel_bytes(name: str, n: int, p, nleaves: int) -> float | None:
     """Algorithmic bytes per launch of the main kernels (per-unit figures x units)."""
     if name == "k_query_s1":  # read sorted points once, node summaries, one result per window
         return 24.0 * n + 48.0 * nleaves + 8.0 * p.ncells
-    if name.startswith("k_gather_leaves"):  # perm + xyz in, keyed points + id + leaf out
-        return (4 + 24 + 24 + 4) * n + 48.0 * nleaves
+    if name.startswith("k_gather_leaves"):  # perm + xyz in; keyed points, id, class index and leaf out
+        return (4 + 24 + 24 + 4 + 4) * n + 48.0 * nleaves
     if name == "k_rs_downsweep":
         return 16.0 * n
     if name == "k_morton":
         return 28.0 * n
+    return None
+
+
+def measured_traffic(name: str, n: int) -> float | None:
+    """DRAM bytes per launch of a kernel from its committed ncu summary
+    (profiles/<kernel>_*_dram.md, line 'traffic_bytes_per_point: X'), scaled
+    to n points; None without a summary."""
+    for f in sorted((Path(__file__).resolve().parent / "profiles").glob(f"{name}_*_dram.md")):
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_point:"):
+                return float(line.split(":", 1)[1]) * n
     return None
 
 
@@ -311,9 +323,14 @@ def main():
         per_launch_ms = kms / calls
         bytes_alg = kernel_bytes(name, spec.n, p, tree_leaves)
         achieved = bytes_alg / (per_launch_ms / 1e3) / 1e9 if bytes_alg else None
+        traffic = measured_traffic(name, spec.n)
         roof = {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,
+                "frac": round(achieved / peak, 4) if achieved else None,
+                "traffic": round(traffic) if traffic else None,
+                "traffic_gbs": round(traffic / (per_launch_ms / 1e3) / 1e9, 1) if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, full-size launch "
+                                  "(profiles/), per point x points" if traffic else None,
                 "ms_per_launch": round(per_launch_ms, 4), "bytes_per_launch": bytes_alg}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
