@@ -135,6 +135,12 @@ def max_over_ranks(v: float, ws: int, device: str) -> float:
     return float(t.item())
 
 
+def job_value(ws: int, points_per_rank: int, steps: int, ms_max: float) -> float:
+    """Whole-job Mpts/s: every rank processes its own replica of the workload
+    (weak scaling), so all ranks' points over the slowest rank's time."""
+    return ws * points_per_rank * steps / (ms_max / 1e3) / 1e6
+
+
 def workload(config: int, n_override: int | None):
     import fastowm_gb300 as F
 
@@ -288,7 +294,7 @@ def main():
     ktimes = kernel_times(F, ctx)
     F.lib().owm_ctx_set_profiling(ctx.handle, 0)
     ms_max = max_over_ranks(ms, ws, f"cuda:{local}")
-    value = ws * spec.n * args.steps / (ms_max / 1e3) / 1e6
+    value = job_value(ws, spec.n, args.steps, ms_max)
 
     # ---- e2e: pinned host points in, seeds out, through owm_run_host ---------------------------
     e2e = None
