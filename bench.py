@@ -482,13 +482,10 @@ def run_served(F, torch, ctx, args, local):
     plain = total / (time.perf_counter() - t0) / 1e6
     srv = F.Server(local, hbm_budget_bytes=120 << 30, max_tiles_per_batch=32, max_inflight_batches=3,
                    max_points_per_batch=48 << 20, copy_on_submit=False)
-    for xyz, bb, cfg, cap, _ in tiles[:4]:  # warm the slots
-        srv.wait(srv.submit(xyz, bb, cfg), cap)
     rng = np.random.default_rng(5000)
-    sweep = []
-    for lam in (50, 200, 500, 1000, 2000, float("inf")):
-        # the last point submits everything at once: the served path's saturation throughput
-        nreq = 300 if lam == float("inf") else int(min(max(30, lam * 1.0), 300))
+
+    def burst(lam, nreq):
+        """nreq requests with Poisson arrivals at rate lam (inf: all at once)."""
         arrivals = np.zeros(nreq) if lam == float("inf") else np.cumsum(rng.exponential(1.0 / lam, nreq))
         tickets = []
         t0 = time.perf_counter()
@@ -503,15 +500,25 @@ def run_served(F, torch, ctx, args, local):
             lats.append(ms)
             pts += n
         wall = time.perf_counter() - t0
-        sweep.append({"lambda_tiles_s": "saturation" if lam == float("inf") else lam, "tiles": nreq, "p50_ms": round(float(np.percentile(lats, 50)), 3),
-                      "p99_ms": round(float(np.percentile(lats, 99)), 3), "mpts_s": round(pts / wall / 1e6, 2)})
+        return {"lambda_tiles_s": "saturation" if lam == float("inf") else lam, "tiles": nreq,
+                "p50_ms": round(float(np.percentile(lats, 50)), 3), "p99_ms": round(float(np.percentile(lats, 99)), 3),
+                "mpts_s": round(pts / wall / 1e6, 2)}
+
+    # warm-up (untimed): one saturation burst sizes every slot's buffers for the largest batches
+    burst(float("inf"), 300)
+    sweep = [burst(lam, int(min(max(30, lam * 1.0), 300))) for lam in (50, 200, 500, 1000, 2000)]
+    # saturation throughput: everything submitted at once, three bursts, median reported
+    sat_runs = [burst(float("inf"), 300) for _ in range(3)]
+    sat_runs.sort(key=lambda r: r["mpts_s"])
+    sweep.append(sat_runs[1])
     st = srv.stats()
     srv.close()
     sat = sweep[-1]["mpts_s"]
     return {"workload": f"config 5: Poisson arrivals, {pool}-tile pool log-uniform [10k, 5M] points "
                         f"({total} points), W 8-16, overlap 0.8, B 20, 120 GB budget",
             "plain_per_tile_mpts": round(plain, 2), "saturation_mpts": sat,
-            "saturation_vs_plain": round(sat / plain, 2), "sweep": sweep, "batches": int(st.batches),
+            "saturation_vs_plain": round(sat / plain, 2), "saturation_runs_mpts": [r["mpts_s"] for r in sat_runs],
+            "sweep": sweep, "batches": int(st.batches),
             "peak_bytes": int(st.peak_bytes),
             "latency": "submit -> result ready (host clock); inputs borrowed from pinned host memory"}
 

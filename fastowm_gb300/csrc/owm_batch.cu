@@ -517,6 +517,9 @@ void BatchRun::destroy() {
   if (stream) cudaStreamSynchronize(stream);
   if (h_off) cudaFreeHost(h_off);
   h_off = nullptr;
+  if (h_stage) cudaFreeHost(h_stage);
+  h_stage = nullptr;
+  stage_cap = 0;
   if (done) cudaEventDestroy(done);
   done = nullptr;
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -554,9 +557,27 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   if (cap_tiles < ntiles + 1) {
     if (h_off) cudaFreeHost(h_off);
     h_off = nullptr;
-    OWM_CUDA_TRY(cudaMallocHost(&h_off, (size_t)(ntiles + 1) * 8));
+    OWM_CUDA_TRY(cudaMallocHost(&h_off, (size_t)(ntiles + 2) * 8));  // + the status word
     cap_tiles = ntiles + 1;
   }
+  // Per-batch tables go through pinned staging: a copy from pageable memory
+  // would first wait for this stream's queued point copies, holding the
+  // caller (the server's worker) for the whole transfer.
+  const size_t T1 = (size_t)ntiles + 1;
+  const size_t stage_need = 16 * 16 + (size_t)ntiles * (sizeof(TileMeta) + 2 * sizeof(QueryJob)) + T1 * (8 * 3 + 4 * 7);
+  if (stage_cap < stage_need) {
+    if (h_stage) cudaFreeHost(h_stage);
+    h_stage = nullptr;
+    OWM_CUDA_TRY(cudaMallocHost(&h_stage, stage_need));
+    stage_cap = stage_need;
+  }
+  size_t stage_off = 0;
+  auto stage_copy = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    char* h = h_stage + stage_off;
+    stage_off += (bytes + 15) & ~(size_t)15;
+    std::memcpy(h, src, bytes);
+    return cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, stream);
+  };
   tiles.clear();
   char* B = static_cast<char*>(mem.ptr);
   auto at = [&](size_t off) { return B + off; };
@@ -589,18 +610,17 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   int32_t* d_cyoff = (int32_t*)at(P.o_cyoff);
   int64_t* d_winoff = (int64_t*)at(P.o_winoff);
   int64_t* d_celloff = (int64_t*)at(P.o_celloff);
-  const size_t T1 = (size_t)ntiles + 1;
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_meta, P.meta.data(), (size_t)ntiles * sizeof(TileMeta), cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_ptoff, P.pt_off.data(), T1 * 8, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_leafoff, P.leaf_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_nodeoff, P.node_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_intoff, P.int_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_exoff, P.ex_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_eyoff, P.ey_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_cxoff, P.cx_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_cyoff, P.cy_off.data(), T1 * 4, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_winoff, P.win_off.data(), T1 * 8, cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_celloff, P.cell_off.data(), T1 * 8, cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(stage_copy(d_meta, P.meta.data(), (size_t)ntiles * sizeof(TileMeta)));
+  OWM_CUDA_TRY(stage_copy(d_ptoff, P.pt_off.data(), T1 * 8));
+  OWM_CUDA_TRY(stage_copy(d_leafoff, P.leaf_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_nodeoff, P.node_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_intoff, P.int_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_exoff, P.ex_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_eyoff, P.ey_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_cxoff, P.cx_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_cyoff, P.cy_off.data(), T1 * 4));
+  OWM_CUDA_TRY(stage_copy(d_winoff, P.win_off.data(), T1 * 8));
+  OWM_CUDA_TRY(stage_copy(d_celloff, P.cell_off.data(), T1 * 8));
 
   // query jobs (host-built: pointers are known here)
   TreeView base_view;
@@ -663,8 +683,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   (void)base_view;
   QueryJob* d_j1 = (QueryJob*)at(P.o_jobs1);
   QueryJob* d_j3 = (QueryJob*)at(P.o_jobs3);
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_j1, j1.data(), (size_t)ntiles * sizeof(QueryJob), cudaMemcpyHostToDevice, stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(d_j3, j3.data(), (size_t)ntiles * sizeof(QueryJob), cudaMemcpyHostToDevice, stream));
+  OWM_CUDA_TRY(stage_copy(d_j1, j1.data(), (size_t)ntiles * sizeof(QueryJob)));
+  OWM_CUDA_TRY(stage_copy(d_j3, j3.data(), (size_t)ntiles * sizeof(QueryJob)));
 
   int64_t* d_out = (int64_t*)at(P.o_out);
   int64_t* d_outoff = (int64_t*)at(P.o_outoff);
@@ -796,6 +816,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       OWM_LAUNCH("k_b_assemble", s, k_b_assemble<<<gsz(NW + NC + ntiles + 1), 256, 0, s>>>(s3, s3_off, llp, llp_off, P.idbits, ntiles, d_out, d_outoff));
       count_launch(L);
       if (cudaMemcpyAsync(h_off, d_outoff, T1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      if (cudaMemcpyAsync(h_off + T1, words, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
     } while (false);
     if (capture) {
       cudaGraph_t g = nullptr;
@@ -832,11 +853,11 @@ bool BatchRun::ready() {
 int BatchRun::finish(int64_t* seeds, int64_t cap, int64_t* offsets, owm_run_info* info) {
   OWM_CUDA_TRY(cudaSetDevice(device));
   OWM_CUDA_TRY(cudaEventSynchronize(done));
+  const int64_t nt = (int64_t)tiles.size();
   uint32_t st = 0;
-  OWM_CUDA_TRY(cudaMemcpy(&st, d_status, 4, cudaMemcpyDeviceToHost));
+  std::memcpy(&st, h_off + nt + 1, 4);  // read back with the offsets at the end of the batch
   if (st & kStatusNonFinite) return OWM_EINVAL;
   if (st & kStatusWalkBound) return OWM_ETIMEOUT;
-  const int64_t nt = (int64_t)tiles.size();
   total_out = h_off[nt];
   if (offsets) std::memcpy(offsets, h_off, (size_t)(nt + 1) * 8);
   if (info) {

@@ -44,8 +44,10 @@ struct BatchRun {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   DeviceBuffer mem;
-  int64_t* h_off = nullptr;  // pinned [cap_tiles+1] per-tile output offsets
+  int64_t* h_off = nullptr;  // pinned [cap_tiles+1] per-tile output offsets, then the status word
   int64_t cap_tiles = 0;
+  char* h_stage = nullptr;   // pinned staging of the per-batch tables (copies from it never block)
+  size_t stage_cap = 0;
   int64_t launches = 0;
   bool use_graphs = false;
   cudaGraphExec_t graph = nullptr;
