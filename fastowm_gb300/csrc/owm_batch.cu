@@ -7,9 +7,13 @@
 //   * leaves, Karras hierarchies, escape links and refits of all tiles are
 //     built by single launches that find their tile by binary search over
 //     per-tile offsets;
-//   * stage 1 and stage 3 are one persistent query launch each: warps pull
-//     4 x 8 window patches of any tile from one work counter, which balances
-//     uneven tiles;
+//   * stage 1 by exact window classes: per-tile class tables built by two
+//     launches, every point folded into its tile's sub-cell counters inside
+//     the gather, then batched tie-id, row and window reductions (a tile that
+//     asks for the tree walk switches the whole batch to the persistent walk);
+//   * stage 3 (and the stage-1 walk) is one persistent query launch: warps
+//     pull 4 x 8 window patches of any tile from one work counter, which
+//     balances uneven tiles;
 //   * stage 2 sorts all window results on a (tile, id) key;
 //   * the device part can be captured once into a CUDA graph and replayed
 //     while the tile shapes repeat.
@@ -22,6 +26,7 @@
 #include <cstring>
 
 #include "owm_batch.cuh"
+#include "owm_classes.cuh"
 #include "owm_devutil.cuh"
 
 namespace owm {
@@ -63,7 +68,8 @@ __global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restric
                                                          int64_t total_leaves, int64_t* __restrict__ xk,
                                                          int64_t* __restrict__ yk, int64_t* __restrict__ zk,
                                                          uint32_t* __restrict__ pid, Node* __restrict__ nodes,
-                                                         uint32_t* __restrict__ status) {
+                                                         uint32_t* __restrict__ status,
+                                                         const ClassArgs* __restrict__ cls) {
   const int lane = threadIdx.x & 31;
   bool finite = true;
   for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total_leaves;
@@ -75,23 +81,95 @@ __global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restric
     const int32_t cnt = min(m.leaf, m.n - first);
     LeafAcc acc;
     acc.init();
-    for (int32_t c = lane; c < cnt; c += 32) {
-      const int32_t lp = first + c;
-      const int64_t gp = m.pt_off + lp;
-      const uint32_t src = __ldg(perm + gp);
-      int64_t x, y, z;
-      finite &= load_point(xyz, src, x, y, z);
-      const uint32_t id = (uint32_t)((int64_t)src - m.pt_off + 1);
-      xk[gp] = x;
-      yk[gp] = y;
-      zk[gp] = z;
-      pid[gp] = id;
-      acc.add(x, y, z, id, (uint32_t)lp);
+    for (int32_t c0 = 0; c0 < cnt; c0 += 32) {  // warp-uniform: the class fold needs whole warps
+      const int32_t lp = first + c0 + lane;
+      const bool valid = c0 + lane < cnt;
+      int64_t x = 0, y = 0, z = 0;
+      if (valid) {
+        const int64_t gp = m.pt_off + lp;
+        const uint32_t src = __ldg(perm + gp);
+        finite &= load_point(xyz, src, x, y, z);
+        const uint32_t id = (uint32_t)((int64_t)src - m.pt_off + 1);
+        xk[gp] = x;
+        yk[gp] = y;
+        zk[gp] = z;
+        pid[gp] = id;
+        acc.add(x, y, z, id, (uint32_t)lp);
+      }
+      if (cls) {
+        if (!__all_sync(0xffffffffu, valid)) {  // short leaf: idle lanes borrow lane 0's point
+          const int64_t bx = __shfl_sync(0xffffffffu, x, 0), by = __shfl_sync(0xffffffffu, y, 0);
+          if (!valid) {
+            x = bx;
+            y = by;
+            z = 0;
+          }
+        }
+        cls_aggregate_warp(cls[t], lp, valid, x, y, z, lane);
+      }
     }
     acc.reduce(32);
     write_leaf_seg(nodes + m.node_off + (m.nleaves - 1) + j, acc, first, m.ox, m.oy, 32, true);
   }
   if (!finite) atomicOr(status, kStatusNonFinite);
+}
+
+// ---- stage 1 by window classes, all tiles per launch ----------------------
+// Grid y = tile.  Edge keys of the tile's window columns and rows.
+__global__ void k_bc_split(const ClassArgs* __restrict__ cls, const TileMeta* __restrict__ meta,
+                           const Edge* __restrict__ E_wx, const Edge* __restrict__ E_wy) {
+  const ClassArgs& A = cls[blockIdx.y];
+  const TileMeta& m = meta[blockIdx.y];
+  const int32_t nmax = max(A.nx, A.ny);
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nmax; i += gridDim.x * blockDim.x) {
+    if (i < A.nx) {
+      const Edge e = E_wx[m.ex_off + i];
+      const_cast<int64_t*>(A.Lx)[i] = e.lo_k;
+      const_cast<int64_t*>(A.Rx)[i] = e.hi_k;
+    }
+    if (i < A.ny) {
+      const Edge e = E_wy[m.ey_off + i];
+      const_cast<int64_t*>(A.Ly)[i] = e.lo_k;
+      const_cast<int64_t*>(A.Ry)[i] = e.hi_k;
+    }
+  }
+}
+
+// Grid y = tile.  s-ranges of the windows and the class tables.
+__global__ void k_bc_prep(const ClassArgs* __restrict__ cls) {
+  const ClassArgs& A = cls[blockIdx.y];
+  const int32_t nmax = max(max(A.nx, A.ny), max(A.qx, A.qy));
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nmax; i += gridDim.x * blockDim.x) {
+    if (i < A.nx) cls_range_one(A.Lx, A.Rx, A.nx, i, A.sxl + i, A.sxh + i);
+    if (i < A.ny) cls_range_one(A.Ly, A.Ry, A.ny, i, A.syl + i, A.syh + i);
+    if (i < A.qx) const_cast<int2*>(A.tabx)[i] = cls_table_one(A.Lx, A.Rx, A.nx, A.kx0, A.shx, i);
+    if (i < A.qy) const_cast<int2*>(A.taby)[i] = cls_table_one(A.Ly, A.Ry, A.ny, A.ky0, A.shy, i);
+  }
+}
+
+__global__ void k_bc_ids(const ClassArgs* __restrict__ cls, const int64_t* __restrict__ pt_off, int ntiles,
+                         const int64_t* __restrict__ zk, const uint32_t* __restrict__ pid, int64_t n) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int t = tile_of(pt_off, ntiles, g);
+    cls_ids_one(cls[t], g - __ldg(pt_off + t), __ldg(zk + g), __ldg(pid + g));
+  }
+}
+
+__global__ void k_bc_rows(const ClassArgs* __restrict__ cls, const int64_t* __restrict__ rows_off, int ntiles,
+                          int64_t total) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const int t = tile_of(rows_off, ntiles, k);
+    cls_row_one(cls[t], k - __ldg(rows_off + t));
+  }
+}
+
+__global__ void k_bc_windows(const ClassArgs* __restrict__ cls, const TileMeta* __restrict__ meta,
+                             const int64_t* __restrict__ win_off, int ntiles, int64_t total,
+                             uint32_t* __restrict__ win) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int t = tile_of(win_off, ntiles, w);
+    win[w] = cls_window_one(cls[t], w - __ldg(win_off + t), meta[t].thr);
+  }
 }
 
 __device__ __forceinline__ int bdelta(const uint32_t* __restrict__ mk, const TileMeta& m, int32_t i, int32_t j) {
@@ -330,6 +408,19 @@ struct Plan {
   std::vector<TileMeta> meta;
   std::vector<int64_t> pt_off, win_off, cell_off;
   std::vector<int32_t> leaf_off, node_off, int_off, ex_off, ey_off, cx_off, cy_off;
+  // stage 1 by window classes (when no tile asks for the tree walk)
+  struct ClsLayout {
+    size_t tabx, taby, Lx, Rx, Ly, Ry, sxl, sxh, syl, syh, rc, rz, ri;  // byte offsets in the misc region
+    int64_t sub_off;                                                   // first sub-cell of the tile
+  };
+  bool classes = false;
+  std::vector<ClassArgs> cls;      // per-tile geometry (pointers are set at launch)
+  std::vector<ClsLayout> clay;
+  std::vector<int64_t> rows_off;   // prefix of (window columns x sub-cell rows)
+  int64_t nsub = 0, rows_total = 0;
+  size_t cls_misc = 0;
+  int32_t cls_grid_x = 1;          // blocks per tile of the class prepare launches
+  size_t o_cls = 0, o_rowsoff = 0, o_cidx = 0, o_ccount = 0, o_czmin = 0, o_cidmin = 0, o_cmisc = 0;
   // buffer offsets (bytes) inside the batch buffer
   size_t o_xyz, o_k0, o_k1, o_v0, o_v1, o_sort, o_xk, o_yk, o_zk, o_pid, o_nodes, o_parent, o_flags, o_right,
       o_last, o_edges, o_win, o_s2k0, o_s2k1, o_s2f, o_s2p, o_s2t, o_llp, o_mark, o_cmin, o_cf, o_cp, o_ct, o_s3,
@@ -347,6 +438,14 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
     v->assign(ntiles + 1, 0);
   P->tile_bits = std::max(1, bits_for((uint64_t)ntiles - 1));
   P->mbits = std::min(16, (32 - P->tile_bits) / 2);
+  P->classes = true;
+  for (int32_t t = 0; t < ntiles; ++t) P->classes &= td[t].cfg.stage1_walk == 0;
+  if (P->classes) {
+    P->cls.assign(ntiles, ClassArgs{});
+    P->clay.assign(ntiles, Plan::ClsLayout{});
+    P->rows_off.assign(ntiles + 1, 0);
+  }
+  int32_t cls_span = 1;
   int64_t maxn = 0;
   for (int32_t t = 0; t < ntiles; ++t) {
     const owm_tile_desc& d = td[t];
@@ -417,6 +516,45 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
     P->ey += p.nrows;
     P->cx += p.bsize > 0 ? p.ncols_grid : 0;
     P->cy += p.bsize > 0 ? p.nrows_grid : 0;
+    if (P->classes) {
+      ClassArgs& a = P->cls[t];
+      std::memset(&a, 0, sizeof(a));
+      a.nx = (int32_t)p.ncols;
+      a.ny = (int32_t)p.nrows;
+      a.tx = 2 * a.nx + 1;
+      a.ty = 2 * a.ny + 1;
+      if (!cls_table_geometry(bb.min_x, bb.max_x, p.displace, &a.kx0, &a.shx, &a.qx)) a.qx = 0;
+      if (!cls_table_geometry(bb.min_y, bb.max_y, p.displace, &a.ky0, &a.shy, &a.qy)) a.qy = 0;
+      Plan::ClsLayout& l = P->clay[t];
+      auto piece = [&](size_t bytes) {
+        size_t r = P->cls_misc;
+        P->cls_misc += (bytes + 15) & ~(size_t)15;
+        return r;
+      };
+      const size_t nx = (size_t)a.nx, ny = (size_t)a.ny, rows = nx * (size_t)a.ty;
+      l.tabx = piece((size_t)a.qx * 8);
+      l.taby = piece((size_t)a.qy * 8);
+      l.Lx = piece(nx * 8);
+      l.Rx = piece(nx * 8);
+      l.Ly = piece(ny * 8);
+      l.Ry = piece(ny * 8);
+      l.sxl = piece(nx * 4);
+      l.sxh = piece(nx * 4);
+      l.syl = piece(ny * 4);
+      l.syh = piece(ny * 4);
+      l.rc = piece(rows * 4);
+      l.rz = piece(rows * 8);
+      l.ri = piece(rows * 4);
+      l.sub_off = P->nsub;
+      P->nsub += (int64_t)a.tx * a.ty;
+      P->rows_off[t] = P->rows_total;
+      P->rows_total += (int64_t)rows;
+      cls_span = std::max(cls_span, std::max(std::max(a.nx, a.ny), std::max(a.qx, a.qy)));
+    }
+  }
+  if (P->classes) {
+    P->rows_off[ntiles] = P->rows_total;
+    P->cls_grid_x = std::min(64, (cls_span + 255) / 256);
   }
   P->pt_off[ntiles] = P->npts;
   P->leaf_off[ntiles] = (int32_t)P->nleaves;
@@ -489,6 +627,15 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
   P->o_out = take((size_t)(NW + NC + 1) * 8);
   P->o_outoff = take((size_t)T1 * 8);
   P->o_words = take(256);
+  if (P->classes) {
+    P->o_cls = take((size_t)ntiles * sizeof(ClassArgs));
+    P->o_rowsoff = take((size_t)T1 * 8);
+    P->o_cidx = take((size_t)N * 4);
+    P->o_ccount = take((size_t)std::max<int64_t>(P->nsub, 1) * 4);
+    P->o_czmin = take((size_t)std::max<int64_t>(P->nsub, 1) * 8);
+    P->o_cidmin = take((size_t)std::max<int64_t>(P->nsub, 1) * 4);
+    P->o_cmisc = take(std::max<size_t>(P->cls_misc, 16));
+  }
   P->total = o;
   return OWM_OK;
 }
@@ -564,7 +711,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   // would first wait for this stream's queued point copies, holding the
   // caller (the server's worker) for the whole transfer.
   const size_t T1 = (size_t)ntiles + 1;
-  const size_t stage_need = 16 * 16 + (size_t)ntiles * (sizeof(TileMeta) + 2 * sizeof(QueryJob)) + T1 * (8 * 3 + 4 * 7);
+  const size_t stage_need = 16 * 16 + (size_t)ntiles * (sizeof(TileMeta) + 2 * sizeof(QueryJob) + sizeof(ClassArgs)) +
+                            T1 * (8 * 4 + 4 * 7);
   if (stage_cap < stage_need) {
     if (h_stage) cudaFreeHost(h_stage);
     h_stage = nullptr;
@@ -685,6 +833,37 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   QueryJob* d_j3 = (QueryJob*)at(P.o_jobs3);
   OWM_CUDA_TRY(stage_copy(d_j1, j1.data(), (size_t)ntiles * sizeof(QueryJob)));
   OWM_CUDA_TRY(stage_copy(d_j3, j3.data(), (size_t)ntiles * sizeof(QueryJob)));
+  ClassArgs* d_cls = nullptr;
+  int64_t* d_rowsoff = nullptr;
+  if (P.classes) {
+    std::vector<ClassArgs> A(P.cls);
+    char* misc = at(P.o_cmisc);
+    for (int32_t t = 0; t < ntiles; ++t) {
+      const Plan::ClsLayout& l = P.clay[t];
+      ClassArgs& a = A[t];
+      a.tabx = reinterpret_cast<const int2*>(misc + l.tabx);
+      a.taby = reinterpret_cast<const int2*>(misc + l.taby);
+      a.Lx = reinterpret_cast<const int64_t*>(misc + l.Lx);
+      a.Rx = reinterpret_cast<const int64_t*>(misc + l.Rx);
+      a.Ly = reinterpret_cast<const int64_t*>(misc + l.Ly);
+      a.Ry = reinterpret_cast<const int64_t*>(misc + l.Ry);
+      a.sxl = reinterpret_cast<int32_t*>(misc + l.sxl);
+      a.sxh = reinterpret_cast<int32_t*>(misc + l.sxh);
+      a.syl = reinterpret_cast<int32_t*>(misc + l.syl);
+      a.syh = reinterpret_cast<int32_t*>(misc + l.syh);
+      a.rc = reinterpret_cast<uint32_t*>(misc + l.rc);
+      a.rz = reinterpret_cast<unsigned long long*>(misc + l.rz);
+      a.ri = reinterpret_cast<uint32_t*>(misc + l.ri);
+      a.count = reinterpret_cast<uint32_t*>(at(P.o_ccount)) + l.sub_off;
+      a.zmin = reinterpret_cast<unsigned long long*>(at(P.o_czmin)) + l.sub_off;
+      a.idmin = reinterpret_cast<uint32_t*>(at(P.o_cidmin)) + l.sub_off;
+      a.cidx = reinterpret_cast<uint32_t*>(at(P.o_cidx)) + P.pt_off[t];
+    }
+    d_cls = reinterpret_cast<ClassArgs*>(at(P.o_cls));
+    d_rowsoff = reinterpret_cast<int64_t*>(at(P.o_rowsoff));
+    OWM_CUDA_TRY(stage_copy(d_cls, A.data(), (size_t)ntiles * sizeof(ClassArgs)));
+    OWM_CUDA_TRY(stage_copy(d_rowsoff, P.rows_off.data(), T1 * 8));
+  }
 
   int64_t* d_out = (int64_t*)at(P.o_out);
   int64_t* d_outoff = (int64_t*)at(P.o_outoff);
@@ -698,6 +877,9 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     sig.append(reinterpret_cast<const char*>(&mem.ptr), sizeof(void*));
     sig.append(reinterpret_cast<const char*>(&xyz), sizeof(void*));
     sig.append(reinterpret_cast<const char*>(&P.total), sizeof(P.total));
+    // the class regions' layout (table sizes follow each tile's bbox, not only its meta)
+    if (P.classes) sig.append(reinterpret_cast<const char*>(P.cls.data()), P.cls.size() * sizeof(ClassArgs));
+    sig.push_back(P.classes ? 'c' : 'w');
   }
   if (use_graphs && graph && sig == graph_sig) {
     OWM_CUDA_TRY(cudaGraphLaunch(graph, stream));
@@ -733,10 +915,28 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
           cudaSuccess) { rc2 = OWM_ECUDA; break; }
       const uint32_t* mk = alt ? k1 : k0;
       const uint32_t* perm = alt ? v1 : v0;
+      // edge tables (before the gather: the class fold needs the window edges)
+      if (P.ex) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ex + 127) / 128), 128, 0, s>>>(0, 0, d_meta, d_exoff, ntiles, P.ex, E_wx));
+      if (P.ey) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ey + 127) / 128), 128, 0, s>>>(0, 1, d_meta, d_eyoff, ntiles, P.ey, E_wy));
+      if (P.cx) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cx + 127) / 128), 128, 0, s>>>(1, 0, d_meta, d_cxoff, ntiles, P.cx, E_cx));
+      if (P.cy) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cy + 127) / 128), 128, 0, s>>>(1, 1, d_meta, d_cyoff, ntiles, P.cy, E_cy));
+      count_launch(L, (P.ex > 0) + (P.ey > 0) + (P.cx > 0) + (P.cy > 0));
+      if (P.classes) {
+        const dim3 gp((unsigned)P.cls_grid_x, (unsigned)ntiles);
+        OWM_LAUNCH("k_bc_split", s, k_bc_split<<<gp, 256, 0, s>>>(d_cls, d_meta, E_wx, E_wy));
+        OWM_LAUNCH("k_bc_prep", s, k_bc_prep<<<gp, 256, 0, s>>>(d_cls));
+        count_launch(L, 2);
+        if (cudaMemsetAsync(at(P.o_ccount), 0, (size_t)P.nsub * 4, s) != cudaSuccess ||
+            cudaMemsetAsync(at(P.o_czmin), 0xFF, (size_t)P.nsub * 8, s) != cudaSuccess ||
+            cudaMemsetAsync(at(P.o_cidmin), 0xFF, (size_t)P.nsub * 4, s) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
+        }
+      }
       {
         int64_t blocks = std::min<int64_t>((P.nleaves * 32 + 255) / 256, 152 * 16);
         OWM_LAUNCH("k_b_gather_leaves", s, k_b_gather_leaves<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(
-            xyz, perm, d_meta, d_leafoff, ntiles, P.nleaves, xk, yk, zk, pid, nodes, words));
+            xyz, perm, d_meta, d_leafoff, ntiles, P.nleaves, xk, yk, zk, pid, nodes, words, d_cls));
         count_launch(L);
       }
       if (cudaMemsetAsync(parent, 0xFF, (size_t)P.nnodes * 4, s) != cudaSuccess ||
@@ -754,14 +954,22 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       OWM_LAUNCH("k_b_refit", s, k_b_refit<<<(unsigned)((P.nleaves + 255) / 256), 256, 0, s>>>(
           nodes, parent, flags, d_meta, d_leafoff, ntiles, P.nleaves));
       count_launch(L, 2);
-      // edge tables
-      if (P.ex) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ex + 127) / 128), 128, 0, s>>>(0, 0, d_meta, d_exoff, ntiles, P.ex, E_wx));
-      if (P.ey) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ey + 127) / 128), 128, 0, s>>>(0, 1, d_meta, d_eyoff, ntiles, P.ey, E_wy));
-      if (P.cx) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cx + 127) / 128), 128, 0, s>>>(1, 0, d_meta, d_cxoff, ntiles, P.cx, E_cx));
-      if (P.cy) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cy + 127) / 128), 128, 0, s>>>(1, 1, d_meta, d_cyoff, ntiles, P.cy, E_cy));
-      count_launch(L, (P.ex > 0) + (P.ey > 0) + (P.cx > 0) + (P.cy > 0));
-      // stage 1: persistent query over every tile's windows
-      if (launch_query_persistent(d_j1, ntiles, w1, qnext, 152 * 16, s, L, "k_query_s1_batch")) { rc2 = OWM_ECUDA; break; }
+      // stage 1: window classes (tie ids, rows, windows), or the persistent walk
+      if (P.classes) {
+        OWM_LAUNCH("k_bc_ids", s, k_bc_ids<<<gsz(N), 256, 0, s>>>(d_cls, d_ptoff, ntiles, zk, pid, N));
+        count_launch(L);
+        if (P.rows_total > 0) {
+          OWM_LAUNCH("k_bc_rows", s, k_bc_rows<<<gsz(P.rows_total), 256, 0, s>>>(d_cls, d_rowsoff, ntiles, P.rows_total));
+          count_launch(L);
+        }
+        if (P.nwin > 0) {
+          OWM_LAUNCH("k_bc_windows", s, k_bc_windows<<<gsz(P.nwin), 256, 0, s>>>(d_cls, d_meta, d_winoff, ntiles, P.nwin, win));
+          count_launch(L);
+        }
+      } else if (launch_query_persistent(d_j1, ntiles, w1, qnext, 152 * 16, s, L, "k_query_s1_batch")) {
+        rc2 = OWM_ECUDA;
+        break;
+      }
       // stage 2 on (tile, id) keys
       const int64_t NW = P.nwin;
       const uint32_t none = (P.idbits >= 32) ? 0xFFFFFFFFu : ((1u << P.idbits) - 1u);

@@ -31,14 +31,7 @@ namespace owm {
 namespace {
 
 constexpr int kClsBlock = 256;
-constexpr int32_t kMaxTable = 1 << 16;
-
-__device__ __forceinline__ int32_t count_less(const int64_t* a, int32_t n, int64_t v) {
-  return cls_bsearch(a, 0, n, v, false);
-}
-__device__ __forceinline__ int32_t count_le(const int64_t* a, int32_t n, int64_t v) {
-  return cls_bsearch(a, 0, n, v, true);
-}
+constexpr int32_t kMaxTable = kClsMaxTable;
 
 __global__ void k_cls_split(const Edge* __restrict__ e, int32_t n, int64_t* __restrict__ L, int64_t* __restrict__ R) {
   int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,23 +41,16 @@ __global__ void k_cls_split(const Edge* __restrict__ e, int32_t n, int64_t* __re
   }
 }
 
-// tab[q] = (#{L < cell start}, #{R < cell start}) for cells of 2^sh keys.
 __global__ void k_cls_table(const int64_t* __restrict__ L, const int64_t* __restrict__ R, int32_t n, int64_t k0,
                             int sh, int32_t Q, int2* __restrict__ tab) {
   int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= Q) return;
-  int64_t qs = k0 + ((int64_t)q << sh);
-  tab[q] = make_int2(count_less(L, n, qs), count_less(R, n, qs));
+  if (q < Q) tab[q] = cls_table_one(L, R, n, k0, sh, q);
 }
 
-// s-range [lo, hi] of window i along one axis (empty when lo > hi).
 __global__ void k_cls_ranges(const int64_t* __restrict__ L, const int64_t* __restrict__ R, int32_t n,
                              int32_t* __restrict__ s_lo, int32_t* __restrict__ s_hi) {
   int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int64_t a = L[i] + 1, b = R[i] - 1;
-  s_lo[i] = count_less(L, n, a) + count_le(R, n, a);
-  s_hi[i] = a <= b ? count_less(L, n, b) + count_le(R, n, b) : -1;
+  if (i < n) cls_range_one(L, R, n, i, s_lo + i, s_hi + i);
 }
 
 __global__ void __launch_bounds__(kClsBlock) k_cls_aggregate(ClassArgs A, const int64_t* __restrict__ xk,
@@ -80,64 +66,33 @@ __global__ void __launch_bounds__(kClsBlock) k_cls_aggregate(ClassArgs A, const 
   }
 }
 
-__global__ void k_cls_ids(const int64_t* __restrict__ zk, const uint32_t* __restrict__ pid,
-                          const uint32_t* __restrict__ cidx, int64_t n, const unsigned long long* __restrict__ zmin,
-                          uint32_t* __restrict__ idmin) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = __ldg(cidx + i);
-    const unsigned long long zu = (unsigned long long)__ldg(zk + i) ^ 0x8000000000000000ull;
-    if (zu == __ldg(zmin + c)) atomicMin(idmin + c, __ldg(pid + i));
-  }
-}
-
-__device__ __forceinline__ bool zu_less(unsigned long long za, uint32_t ia, unsigned long long zb, uint32_t ib) {
-  return za < zb || (za == zb && ia < ib);
+__global__ void k_cls_ids(ClassArgs A, const int64_t* __restrict__ zk, const uint32_t* __restrict__ pid, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    cls_ids_one(A, i, __ldg(zk + i), __ldg(pid + i));
 }
 
 __global__ void k_cls_rows(ClassArgs A) {
   const int64_t total = (int64_t)A.nx * A.ty;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t ii = (int32_t)(k / A.ty), t = (int32_t)(k % A.ty);
-    uint32_t c = 0, bi = 0xFFFFFFFFu;
-    unsigned long long bz = ~0ull;
-    const int64_t base = (int64_t)t * A.tx;
-    for (int32_t s = A.sxl[ii]; s <= A.sxh[ii]; ++s) {
-      c += A.count[base + s];
-      const unsigned long long z = A.zmin[base + s];
-      const uint32_t id = A.idmin[base + s];
-      if (zu_less(z, id, bz, bi)) {
-        bz = z;
-        bi = id;
-      }
-    }
-    A.rc[k] = c;
-    A.rz[k] = bz;
-    A.ri[k] = bi;
-  }
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x)
+    cls_row_one(A, k);
 }
 
 __global__ void k_cls_windows(ClassArgs A, uint32_t thr, uint32_t* __restrict__ out) {
   const int64_t total = (int64_t)A.nx * A.ny;
-  const unsigned long long sentinel = (unsigned long long)kZSentinel ^ 0x8000000000000000ull;
-  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t ii = (int32_t)(w / A.ny), jj = (int32_t)(w % A.ny);  // step = ii*nrows + jj
-    uint32_t c = 0, bi = 0;
-    unsigned long long bz = sentinel;  // the reference starts from point 0 {0, 0, DBL_MAX}
-    const int64_t base = (int64_t)ii * A.ty;
-    for (int32_t t = A.syl[jj]; t <= A.syh[jj]; ++t) {
-      c += A.rc[base + t];
-      if (zu_less(A.rz[base + t], A.ri[base + t], bz, bi)) {
-        bz = A.rz[base + t];
-        bi = A.ri[base + t];
-      }
-    }
-    out[w] = c >= thr ? bi : kNone;
-  }
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x)
+    out[w] = cls_window_one(A, w, thr);
 }
 
-// Cells of 2^sh key units no wider than half the window step over [lo, hi]
-// (keys are linear there when lo and hi share sign and exponent).
-bool table_geometry(double lo, double hi, double step, int64_t* k0, int* sh, int32_t* Q) {
+int grid(int64_t n, int block = 256) {
+  int64_t g = (n + block - 1) / block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
+}
+
+size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+bool cls_table_geometry(double lo, double hi, double step, int64_t* k0, int* sh, int32_t* Q) {
   if (!(lo > 0.0) || !(hi >= lo) || !(step > 0.0)) return false;
   int64_t blo, bhi;
   std::memcpy(&blo, &lo, 8);
@@ -155,15 +110,6 @@ bool table_geometry(double lo, double hi, double step, int64_t* k0, int* sh, int
   *Q = (int32_t)q;
   return true;
 }
-
-int grid(int64_t n, int block = 256) {
-  int64_t g = (n + block - 1) / block;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
-}
-
-size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
-
-}  // namespace
 
 size_t classes_scratch_bytes(int64_t n, int32_t ncols, int32_t nrows) {
   const int64_t tx = 2 * (int64_t)ncols + 1, ty = 2 * (int64_t)nrows + 1;
@@ -214,8 +160,8 @@ int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* s
   A->ty = (int32_t)ty;
   A->tabx = tabx;
   A->taby = taby;
-  if (!table_geometry(p.bbox.min_x, p.bbox.max_x, p.displace, &A->kx0, &A->shx, &A->qx)) A->qx = 0;
-  if (!table_geometry(p.bbox.min_y, p.bbox.max_y, p.displace, &A->ky0, &A->shy, &A->qy)) A->qy = 0;
+  if (!cls_table_geometry(p.bbox.min_x, p.bbox.max_x, p.displace, &A->kx0, &A->shx, &A->qx)) A->qx = 0;
+  if (!cls_table_geometry(p.bbox.min_y, p.bbox.max_y, p.displace, &A->ky0, &A->shy, &A->qy)) A->qy = 0;
   OWM_LAUNCH("k_cls_split", s, k_cls_split<<<(nc + 255) / 256, 256, 0, s>>>(ex, nc, Lx, Rx));
   OWM_LAUNCH("k_cls_split", s, k_cls_split<<<(nr + 255) / 256, 256, 0, s>>>(ey, nr, Ly, Ry));
   OWM_LAUNCH("k_cls_ranges", s, k_cls_ranges<<<(nc + 255) / 256, 256, 0, s>>>(Lx, Rx, nc, A->sxl, A->sxh));
@@ -242,7 +188,7 @@ int classes_aggregate(const ClassArgs& A, const TreeView& t, int64_t n, cudaStre
 
 int classes_finish(const ClassArgs& A, const TreeView& t, int64_t n, const owm_params& p, uint32_t* d_win,
                    cudaStream_t s, int64_t* launches) {
-  OWM_LAUNCH("k_cls_ids", s, k_cls_ids<<<grid(n), 256, 0, s>>>(t.zk, t.pid, A.cidx, n, A.zmin, A.idmin));
+  OWM_LAUNCH("k_cls_ids", s, k_cls_ids<<<grid(n), 256, 0, s>>>(A, t.zk, t.pid, n));
   OWM_LAUNCH("k_cls_rows", s, k_cls_rows<<<grid((int64_t)A.nx * A.ty), 256, 0, s>>>(A));
   OWM_LAUNCH("k_cls_windows", s, k_cls_windows<<<grid((int64_t)A.nx * A.ny), 256, 0, s>>>(A, p.min_num_points, d_win));
   count_launch(launches, 3);

@@ -105,6 +105,87 @@ __device__ __forceinline__ void cls_aggregate_warp(const ClassArgs& A, int64_t p
   }
 }
 
+// ---- per-element bodies, shared by the single-cloud and the batched kernels ----
+constexpr int32_t kClsMaxTable = 1 << 16;  // class-table cells per axis, at most
+
+__device__ __forceinline__ int32_t cls_count_less(const int64_t* a, int32_t n, int64_t v) {
+  return cls_bsearch(a, 0, n, v, false);
+}
+__device__ __forceinline__ int32_t cls_count_le(const int64_t* a, int32_t n, int64_t v) {
+  return cls_bsearch(a, 0, n, v, true);
+}
+
+// s-range [lo, hi] of window i along one axis (empty when lo > hi).
+__device__ __forceinline__ void cls_range_one(const int64_t* L, const int64_t* R, int32_t n, int32_t i, int32_t* lo,
+                                              int32_t* hi) {
+  const int64_t a = L[i] + 1, b = R[i] - 1;
+  *lo = cls_count_less(L, n, a) + cls_count_le(R, n, a);
+  *hi = a <= b ? cls_count_less(L, n, b) + cls_count_le(R, n, b) : -1;
+}
+
+// Class-table cell q: (#{L < cell start}, #{R < cell start}) for cells of
+// 2^sh keys from k0.
+__device__ __forceinline__ int2 cls_table_one(const int64_t* L, const int64_t* R, int32_t n, int64_t k0, int sh,
+                                              int32_t q) {
+  const int64_t qs = k0 + ((int64_t)q << sh);
+  return make_int2(cls_count_less(L, n, qs), cls_count_less(R, n, qs));
+}
+
+// Tie id of sorted point i (index into A.cidx): among the points holding
+// their sub-cell's min z, the smallest id.
+__device__ __forceinline__ void cls_ids_one(const ClassArgs& A, int64_t i, int64_t zk, uint32_t pid) {
+  const uint32_t c = A.cidx[i];
+  const unsigned long long zu = (unsigned long long)zk ^ 0x8000000000000000ull;
+  if (zu == A.zmin[c]) atomicMin(A.idmin + c, pid);
+}
+
+__device__ __forceinline__ bool cls_zu_less(unsigned long long za, uint32_t ia, unsigned long long zb, uint32_t ib) {
+  return za < zb || (za == zb && ia < ib);
+}
+
+// Row reduction k = ii * ty + t: sub-cells s of window column ii in sub-cell row t.
+__device__ __forceinline__ void cls_row_one(const ClassArgs& A, int64_t k) {
+  const int32_t ii = (int32_t)(k / A.ty), t = (int32_t)(k % A.ty);
+  uint32_t c = 0, bi = 0xFFFFFFFFu;
+  unsigned long long bz = ~0ull;
+  const int64_t base = (int64_t)t * A.tx;
+  for (int32_t s = A.sxl[ii]; s <= A.sxh[ii]; ++s) {
+    c += A.count[base + s];
+    const unsigned long long z = A.zmin[base + s];
+    const uint32_t id = A.idmin[base + s];
+    if (cls_zu_less(z, id, bz, bi)) {
+      bz = z;
+      bi = id;
+    }
+  }
+  A.rc[k] = c;
+  A.rz[k] = bz;
+  A.ri[k] = bi;
+}
+
+// Window w (step = ii * nrows + jj): reduce its rows, apply minNumPoints.  The
+// search starts from the reference's sentinel point 0 {0, 0, DBL_MAX}.
+__device__ __forceinline__ uint32_t cls_window_one(const ClassArgs& A, int64_t w, uint32_t thr) {
+  const unsigned long long sentinel = (unsigned long long)kZSentinel ^ 0x8000000000000000ull;
+  const int32_t ii = (int32_t)(w / A.ny), jj = (int32_t)(w % A.ny);
+  uint32_t c = 0, bi = 0;
+  unsigned long long bz = sentinel;
+  const int64_t base = (int64_t)ii * A.ty;
+  for (int32_t t = A.syl[jj]; t <= A.syh[jj]; ++t) {
+    c += A.rc[base + t];
+    if (cls_zu_less(A.rz[base + t], A.ri[base + t], bz, bi)) {
+      bz = A.rz[base + t];
+      bi = A.ri[base + t];
+    }
+  }
+  return c >= thr ? bi : kNone;
+}
+
+// Class-table geometry over [lo, hi]: cells of 2^sh key units no wider than
+// half the window step (keys are linear there when lo and hi share sign and
+// exponent); false when no table applies (the per-point search then runs).
+bool cls_table_geometry(double lo, double hi, double step, int64_t* k0, int* sh, int32_t* Q);
+
 size_t classes_scratch_bytes(int64_t n, int32_t ncols, int32_t nrows);
 // Carves the buffers from scratch and enqueues the edge split, s-ranges,
 // class tables and counter resets for the windows of p (edge tables ex/ey).

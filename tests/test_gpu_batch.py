@@ -93,3 +93,28 @@ def test_server_rejects_tile_over_budget(owm):
         srv.submit(xyz, bb, cfg)
     assert e.value.status == -2
     srv.close()
+
+
+def test_batch_stage1_classes_equals_walk(owm, ctx):
+    """Stage 1 of a batch by window classes (default) and by the persistent
+    tree walk (any tile with stage1_walk set switches the batch) agree, tile
+    by tile; ties included (config-3 style z quantisation)."""
+    tiles = _tiles(owm, 20, start=90)
+    walk = [(xyz, bb, owm.run_cfg(cfg.wsize, cfg.overlap, cfg.bsize, cfg.tree.max_number, stage1_walk=True))
+            for xyz, bb, cfg in tiles]
+    # ties: quantise z of two tiles to 1 cm
+    for k in (2, 7):
+        xyz, bb, cfg = tiles[k]
+        q = xyz.copy()
+        q[:, 2] = np.round(q[:, 2] * 100.0) / 100.0
+        tiles[k] = (q, bb, cfg)
+        walk[k] = (q, bb, walk[k][2])
+    b = owm.Batch(ctx)
+    got_cls = b.run(tiles)
+    got_walk = b.run(walk)
+    mixed = tiles[:-1] + walk[-1:]  # one tile asks for the walk
+    got_mixed = b.run(mixed)
+    for k in range(len(tiles)):
+        np.testing.assert_array_equal(got_cls[k], got_walk[k], err_msg=f"tile {k}")
+        np.testing.assert_array_equal(got_cls[k], got_mixed[k], err_msg=f"tile {k} (mixed)")
+    b.close()
