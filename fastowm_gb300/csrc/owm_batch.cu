@@ -51,11 +51,19 @@ __global__ void k_b_morton(const double* __restrict__ xyz, int64_t n, const int6
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     int t = tile_of(pt_off, ntiles, i);
     const TileMeta& m = meta[t];
-    double x = __ldg(xyz + 3 * i), y = __ldg(xyz + 3 * i + 1);
-    float fx = (float)((x - m.mox) * m.mscale), fy = (float)((y - m.moy) * m.mscale);
-    fx = fminf(fmaxf(fx, 0.0f), qmax);
-    fy = fminf(fmaxf(fy, 0.0f), qmax);
-    keys[i] = ((uint32_t)t << (2 * mbits)) | (spread_bits16((uint32_t)fx) << 1) | spread_bits16((uint32_t)fy);
+    const double x = __ldg(xyz + 3 * i), y = __ldg(xyz + 3 * i + 1);
+    uint32_t qx, qy;
+    if (m.mint) {  // order keys are linear over the tile's domain: no FP64 arithmetic
+      const int64_t qm = (1ll << mbits) - 1;
+      int64_t a = (dkey(x) - m.mkx0) >> m.mshx, b = (dkey(y) - m.mky0) >> m.mshy;
+      qx = (uint32_t)(a < 0 ? 0 : (a > qm ? qm : a));
+      qy = (uint32_t)(b < 0 ? 0 : (b > qm ? qm : b));
+    } else {
+      float fx = (float)((x - m.mox) * m.mscale), fy = (float)((y - m.moy) * m.mscale);
+      qx = (uint32_t)fminf(fmaxf(fx, 0.0f), qmax);
+      qy = (uint32_t)fminf(fmaxf(fy, 0.0f), qmax);
+    }
+    keys[i] = ((uint32_t)t << (2 * mbits)) | (spread_bits16(qx) << 1) | spread_bits16(qy);
   }
 }
 
@@ -476,6 +484,10 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
     m.mox = bb.min_x + rx - R;
     m.moy = bb.min_y + ry - R;
     m.mscale = (double)(1u << P->mbits) / (2.0 * R);
+    m.mint = (morton_int_shifts(m.mox, m.mox + 2.0 * R, P->mbits, &m.mkx0, &m.mshx) &&
+              morton_int_shifts(m.moy, m.moy + 2.0 * R, P->mbits, &m.mky0, &m.mshy))
+                 ? 1
+                 : 0;
     m.ox = bb.min_x;
     m.oy = bb.min_y;
     m.min_x = bb.min_x;

@@ -18,6 +18,8 @@ struct TileMeta {
   int32_t node_off; // first global node: internal [0, nl-1), leaves [nl-1, 2nl-1)
   int32_t int_off;  // first global internal-node slot
   double mox, moy, mscale;  // Morton domain (square) of the tile
+  int64_t mkx0, mky0;       // integer Morton form (mint): cell = (key(v) - k0) >> sh
+  int32_t mshx, mshy, mint, mpad;
   double ox, oy;            // float-box origin (bbox corner)
   double min_x, min_y, displace;
   int32_t ncols, nrows, ncg, nrg;
