@@ -242,6 +242,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--tiles", type=int, default=512, help="batched-tiles workload size")
+    ap.add_argument("--only", choices=["batched", "served"], default=None,
+                    help="run that leg alone and print its JSON (profiling and tuning runs)")
     args = ap.parse_args()
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":
@@ -255,6 +257,16 @@ def main():
     from fastowm_gb300 import RunInfo
 
     torch.cuda.set_device(local)
+    if args.only:
+        ctx = F.Context(local)
+        leg = run_batched(F, torch, ctx, args, local, ws) if args.only == "batched" else \
+            run_served(F, torch, ctx, args, local)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "impl": "ours", "only": args.only, args.only: leg}),
+                  flush=True)
+        ctx.close()
+        barrier(ws)
+        return
     spec, W, Ov, B, mn, seed = workload(args.config, args.n)
     # pinned host buffer for the e2e leg; generated in place
     host = torch.empty((spec.n, 3), dtype=torch.float64, pin_memory=True)
@@ -426,7 +438,19 @@ def run_batched(F, torch, ctx, args, local, ws):
         run_once()
     torch.cuda.synchronize()
     tb = (time.perf_counter() - t0) / steps
-    batched_seeds = int(offs[-1])
+    batched = [out[offs[t]:offs[t + 1]].copy() for t in range(len(info))]
+    # per-kernel breakdown: one more run, untimed, outside graphs (a replayed
+    # graph is one launch to the per-kernel event profiler)
+    batch.set_graphs(False)
+    F.lib().owm_ctx_set_profiling(ctx.handle, 1)
+    k0 = kernel_times(F, ctx)
+    run_once()
+    torch.cuda.synchronize()
+    k1 = kernel_times(F, ctx)
+    F.lib().owm_ctx_set_profiling(ctx.handle, 0)
+    kb = {k: (v[0] - k0.get(k, (0.0, 0))[0], v[1] - k0.get(k, (0.0, 0))[1]) for k, v in k1.items()}
+    kb = {k: v for k, v in kb.items() if v[1] > 0}
+    ktot = sum(v[0] for v in kb.values()) or 1.0
     # plain path: one owm_run per tile on device-resident clouds
     clouds = []
     for off, n, bb, cfg in info:
@@ -439,13 +463,14 @@ def run_batched(F, torch, ctx, args, local, ws):
     for c, (_, _, _, cfg) in zip(clouds[:8], info[:8]):
         ctx.run(c, cfg)
     lat = []
-    plain_seeds = 0
+    plain = []
     t0 = time.perf_counter()
     for c, (_, _, _, cfg) in zip(clouds, info):
         a = time.perf_counter()
-        plain_seeds += len(ctx.run(c, cfg))
+        plain.append(ctx.run(c, cfg))
         lat.append(1e3 * (time.perf_counter() - a))
     tp = time.perf_counter() - t0
+    equal = all(np.array_equal(a, b) for a, b in zip(batched, plain))
     for c in clouds:
         c.close()
     batch.close()
@@ -456,9 +481,12 @@ def run_batched(F, torch, ctx, args, local, ws):
             "per_tile_mpts": round(total / tp / 1e6, 2), "per_tile_ms_total": round(1e3 * tp, 3),
             "speedup": round(tp / tb, 2), "per_tile_p50_ms": round(float(np.percentile(lat, 50)), 3),
             "per_tile_p99_ms": round(float(np.percentile(lat, 99)), 3),
-            "seeds_equal": batched_seeds == plain_seeds, "leaf_classes": tuned["leaves"],
-            "class_bounds": tuned["bounds"], "graphs": True,
-            "timing": "host clock around synchronous calls, device-resident inputs"}
+            "seeds_equal": bool(equal), "seeds_compared": "every tile's seed array, batched vs its own plain run",
+            "leaf_classes": tuned["leaves"], "class_bounds": tuned["bounds"], "graphs": True,
+            "kernels": {k: {"ms": round(v[0], 4), "share": round(v[0] / ktot, 4), "launches": int(v[1])}
+                        for k, v in sorted(kb.items(), key=lambda kv: -kv[1][0])},
+            "timing": "host clock around synchronous calls, device-resident inputs; kernels: one extra "
+                      "untimed run without graphs, CUDA events per launch"}
 
 
 def run_served(F, torch, ctx, args, local):
