@@ -284,6 +284,31 @@ class Context:
                                   C.byref(n), C.byref(inf)), "run_host")
         return out[: n.value].copy()
 
+    def run_host_submit(self, xyz, bbox, cfg: RunCfg, out: np.ndarray | None = None) -> int:
+        """Queues owm_run_host asynchronously; returns a ticket for run_host_wait.
+        xyz and the output array are kept alive until the wait."""
+        a = _as_xyz(xyz)
+        b = _bbox(bbox) or bbox_of(a)
+        p = params(b, a.shape[0], cfg.wsize, cfg.overlap, cfg.bsize)
+        cap = p.ncells + max(p.ngrid, 0) + 1
+        if out is None or out.size < cap:
+            out = np.empty(cap, dtype=np.int64)
+        t = C.c_int64()
+        _check(lib().owm_run_host_submit(self.handle, _f64p(a), a.shape[0], C.byref(b), C.byref(cfg), _i64p(out),
+                                         out.size, C.byref(t)), "run_host_submit")
+        if not hasattr(self, "_pending"):
+            self._pending = {}
+        self._pending[t.value] = (a, out)
+        return t.value
+
+    def run_host_wait(self, ticket: int, info: RunInfo | None = None) -> np.ndarray:
+        n = C.c_int64()
+        inf = info if info is not None else RunInfo()
+        rc = lib().owm_run_host_wait(self.handle, ticket, C.byref(n), C.byref(inf))
+        _, out = self._pending.pop(ticket, (None, None)) if hasattr(self, "_pending") else (None, None)
+        _check(rc, "run_host_wait")
+        return out[: n.value].copy()
+
 
 class Batch(_Child):
     """Many tiles built and queried together (one launch per stage)."""

@@ -210,11 +210,23 @@ int owm_ctx_destroy(owm_ctx* c) {
   if (!c) return OWM_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   c->scratch.release(c->stream);
   c->tree_mem.release(c->stream);
   c->input.release(c->stream);
   c->outbuf.release(c->stream);
+  for (auto& a : c->aslot) {
+    a.input.release(c->copy_stream ? c->copy_stream : c->stream);
+    if (a.ready) cudaEventDestroy(a.ready);
+    if (a.done) cudaEventDestroy(a.done);
+    if (a.h_seeds) cudaFreeHost(a.h_seeds);
+    if (a.h_words) cudaFreeHost(a.h_words);
+  }
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
   c->prof.clear();
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   c->prof.pool.clear();
@@ -540,6 +552,86 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
   return run_pipeline(c, static_cast<const double*>(c->input.ptr), n, bb, *cfg, seeds, cap, n_seeds, info);
+}
+
+int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, const owm_run_cfg* cfg,
+                        int64_t* seeds, int64_t cap, int64_t* ticket) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
+  if (!c || !xyz || !cfg || !ticket || n <= 0 || n >= 0x7FFFFFFFLL || (!seeds && cap > 0)) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  owm_ctx::AsyncSlot& a = c->aslot[c->next_ticket & 1];
+  if (a.ticket != 0) return OWM_EAGAIN;  // both runs in flight: wait for the older one first
+  owm_bbox bb;
+  if (bbox) {
+    bb = *bbox;
+  } else if (is_device_ptr(xyz)) {
+    int rc = device_bbox(c, xyz, n, &bb);
+    if (rc) return rc;
+  } else {
+    owm_bbox_of(xyz, n, &bb);
+  }
+  if (!c->copy_stream) OWM_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  if (!a.ready) OWM_CUDA_TRY(cudaEventCreateWithFlags(&a.ready, cudaEventDisableTiming));
+  if (!a.done) OWM_CUDA_TRY(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+  if (!a.h_words) OWM_CUDA_TRY(cudaMallocHost(&a.h_words, 32));
+  // This slot's previous run has been waited for, so nothing reads its input
+  // buffer any more.  Reserving on the copy stream orders a (re)allocation
+  // before the copy without making the copy wait for the other run's compute.
+  int rc = a.input.reserve((size_t)n * 24 + kXyzSlack, c->copy_stream);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaMemcpyAsync(a.input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->copy_stream));
+  OWM_CUDA_TRY(cudaEventRecord(a.ready, c->copy_stream));
+  OWM_CUDA_TRY(cudaStreamWaitEvent(c->stream, a.ready, 0));
+  int64_t* d_seeds = nullptr;
+  int64_t room = 0;
+  rc = run_pipeline_enqueue(c, static_cast<const double*>(a.input.ptr), n, bb, *cfg, &a.p, &d_seeds, &room);
+  if (rc) return rc;
+  if (a.h_cap < room) {
+    OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));  // growth only: the old staging may still be a copy target
+    if (a.h_seeds) cudaFreeHost(a.h_seeds);
+    a.h_seeds = nullptr;
+    a.h_cap = 0;
+    OWM_CUDA_TRY(cudaMallocHost(&a.h_seeds, (size_t)room * 8));
+    a.h_cap = room;
+  }
+  OWM_CUDA_TRY(cudaMemcpyAsync(a.h_words, c->d_small, 32, cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaMemcpyAsync(a.h_seeds, d_seeds, (size_t)room * 8, cudaMemcpyDeviceToHost, c->stream));
+  OWM_CUDA_TRY(cudaEventRecord(a.done, c->stream));
+  a.seeds = seeds;
+  a.cap = cap;
+  a.room = room;
+  a.ticket = c->next_ticket++;
+  *ticket = a.ticket;
+  return OWM_OK;
+}
+
+int owm_run_host_wait(owm_ctx* c, int64_t ticket, int64_t* n_seeds, owm_run_info* info) {
+  if (!c || !n_seeds || ticket <= 0) return OWM_EINVAL;
+  owm_ctx::AsyncSlot& a = c->aslot[ticket & 1];
+  if (a.ticket != ticket) return OWM_EINVAL;  // unknown or already collected
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  cudaError_t e = cudaEventSynchronize(a.done);
+  a.ticket = 0;
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "owm_run_host_wait", __FILE__, __LINE__);
+    return OWM_ECUDA;
+  }
+  const uint32_t st = a.h_words[kStatusSlot];
+  if (st & kStatusNonFinite) return OWM_EINVAL;
+  if (st & kStatusWalkBound) return OWM_ETIMEOUT;
+  const int64_t nllp = a.h_words[kLlpSlot], ns3 = a.h_words[kS3Slot];
+  const int64_t total = nllp + ns3;
+  *n_seeds = total;
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    info->n_llp = nllp;
+    info->n_stage3 = ns3;
+    info->n_seeds = total;
+    info->params = a.p;
+  }
+  if (total > a.cap || total > a.room) return OWM_ERANGE;
+  if (total > 0) std::memcpy(a.seeds, a.h_seeds, (size_t)total * 8);
+  return OWM_OK;
 }
 
 }  // extern "C"

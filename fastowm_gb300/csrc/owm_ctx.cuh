@@ -65,6 +65,24 @@ struct owm_ctx {
   owm::DeviceBuffer scratch, tree_mem, input, outbuf;
   owm::TreeStore tree;  // tree of the last owm_run
   cudaEvent_t ev[8] = {};
+  // owm_run_host_submit / _wait: two runs in flight, each with its own input
+  // buffer and pinned result staging; the host->device copy of one runs on
+  // copy_stream while the other computes on `stream`.
+  struct AsyncSlot {
+    int64_t ticket = 0;  // 0 = free
+    owm::DeviceBuffer input;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    int64_t* h_seeds = nullptr;  // pinned [h_cap]
+    int64_t h_cap = 0;
+    uint32_t* h_words = nullptr;  // pinned [8]: status, counts
+    int64_t* seeds = nullptr;     // caller's output
+    int64_t cap = 0, room = 0;
+    owm_params p{};
+    int rc = 0;
+  };
+  cudaStream_t copy_stream = nullptr;
+  AsyncSlot aslot[2];
+  int64_t next_ticket = 1;
 };
 
 namespace owm {
@@ -76,5 +94,10 @@ int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out);
 int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Edge* ey, uint32_t* d_win);
 int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
                  int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info);
+// The device part of run_pipeline: enqueues the whole run on c->stream and
+// leaves the status words in c->d_small and the assembled seeds (room slots)
+// at *d_seeds; no host sync (except inside the min-radius build).
+int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+                         owm_params* p, int64_t** d_seeds, int64_t* room);
 
 }  // namespace owm

@@ -106,10 +106,10 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   return run_query(j, c->d_job, c->stream, &c->launches, "k_query_s1");
 }
 
-int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
-                 int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
+int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+                         owm_params* p_out, int64_t** d_seeds, int64_t* room_out) {
   if (validate_tree_cfg(&cfg.tree) != OWM_OK) return OWM_EINVAL;
-  owm_params p;
+  owm_params& p = *p_out;
   int rc = owm_params_compute(&bb, n, cfg.wsize, cfg.overlap, cfg.bsize, &p);
   if (rc) return rc;
   const int64_t nc = p.ncells, ng = std::max<int64_t>(p.ngrid, 0);
@@ -177,6 +177,19 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   OWM_LAUNCH("k_assemble", s, k_assemble<<<ga, 256, 0, s>>>(s3, d_ns3, llp, d_nllp, room, s64));
   count_launch(&c->launches);
   OWM_CUDA_TRY(cudaGetLastError());
+  *d_seeds = s64;
+  *room_out = room;
+  return OWM_OK;
+}
+
+int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+                 int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
+  owm_params p;
+  int64_t* s64 = nullptr;
+  int64_t room = 0;
+  int rc = run_pipeline_enqueue(c, d_xyz, n, bb, cfg, &p, &s64, &room);
+  if (rc) return rc;
+  cudaStream_t s = c->stream;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small, 32, cudaMemcpyDeviceToHost, s));
   OWM_CUDA_TRY(cudaStreamSynchronize(s));
   if (c->h_small[kStatusSlot] & kStatusNonFinite) return OWM_EINVAL;

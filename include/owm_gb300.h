@@ -249,6 +249,20 @@ int owm_run_host(owm_ctx* ctx, const double* xyz, int64_t n, const owm_bbox* bbo
                  const owm_run_cfg* cfg, int64_t* seeds, int64_t cap, int64_t* n_seeds,
                  owm_run_info* info);
 
+/* Asynchronous form of owm_run_host, for streams of clouds: submit queues
+ * the host->device copy of xyz (on a copy stream of the context), the run
+ * and the device->host copy of the seeds, and returns a ticket at once; wait
+ * blocks until that run is done and writes its seeds and counts.  Two runs
+ * may be in flight per context, so the copy of one cloud overlaps the
+ * compute of the other.  Tickets alternate between two slots: submit returns
+ * OWM_EAGAIN while the run two tickets back has not been waited for.  xyz
+ * (pinned for the copy to overlap) and seeds must stay valid until wait
+ * returns.  Results are exactly those of owm_run_host.  No counterpart in
+ * the reference, whose driver runs one cloud at a time synchronously. */
+int owm_run_host_submit(owm_ctx* ctx, const double* xyz, int64_t n, const owm_bbox* bbox,
+                        const owm_run_cfg* cfg, int64_t* seeds, int64_t cap, int64_t* ticket);
+int owm_run_host_wait(owm_ctx* ctx, int64_t ticket, int64_t* n_seeds, owm_run_info* info);
+
 /* ---- batched tiles ----------------------------------------------------- */
 /* Many independent tiles (own bbox, Wsize, overlap, Bsize, leaf size) built
  * and queried together: one sort over all tiles, one launch per stage, with
