@@ -242,6 +242,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--tiles", type=int, default=512, help="batched-tiles workload size")
+    ap.add_argument("--leaf", type=int, default=0,
+                    help="leaf size (maxNumber) of the main workload; 0 = tuned by fastowm_gb300.autotune, "
+                         "-1 = the workload's configured value")
     ap.add_argument("--only", choices=["batched", "served"], default=None,
                     help="run that leg alone and print its JSON (profiling and tuning runs)")
     args = ap.parse_args()
@@ -279,13 +282,23 @@ def main():
     stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
     info = RunInfo()
 
+    # leaf size (the reference's maxNumber knob): every choice gives the same
+    # seeds, so the library's tuner picks the fastest unless --leaf fixes it
+    leaf_tuning = None
+    if args.leaf > 0:
+        mn = args.leaf
+    elif args.leaf == 0:
+        from fastowm_gb300 import autotune
+
+        leaf_tuning = autotune.tune_leaf_single(ctx, cloud, lambda L: F.run_cfg(W, Ov, B, L))
+        mn = leaf_tuning["leaf"]
+    cfg = F.run_cfg(W, Ov, B, mn)
     for _ in range(args.warmup):
         seeds = ctx.run(cloud, cfg, info)
     tree_leaves = (spec.n + mn - 1) // mn
 
-    # ---- value: device-resident inputs, per-kernel events on ---------------------------------
+    # ---- value: device-resident inputs, K plain steps ------------------------------------------
     clocks = Clocks(local)
-    F.lib().owm_ctx_set_profiling(ctx.handle, 1)
     barrier(ws)
     torch.cuda.synchronize()
     clocks.start()
@@ -303,10 +316,15 @@ def main():
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     barrier(ws)
-    ktimes = kernel_times(F, ctx)
-    F.lib().owm_ctx_set_profiling(ctx.handle, 0)
     ms_max = max_over_ranks(ms, ws, f"cuda:{local}")
     value = job_value(ws, spec.n, args.steps, ms_max)
+    # ---- per-kernel times: the same K steps again with CUDA events around every launch ----------
+    F.lib().owm_ctx_set_profiling(ctx.handle, 1)
+    for _ in range(args.steps):
+        ctx.run(cloud, cfg, info)
+    torch.cuda.synchronize()
+    ktimes = kernel_times(F, ctx)
+    F.lib().owm_ctx_set_profiling(ctx.handle, 0)
 
     # ---- e2e: pinned host points in, seeds out, through the host entry points -----------------
     # Headline: owm_run_host_submit/_wait with two runs in flight, so the
@@ -365,8 +383,9 @@ def main():
                 "frac": round(achieved / peak, 4) if achieved else None,
                 "traffic": round(traffic) if traffic else None,
                 "traffic_gbs": round(traffic / (per_launch_ms / 1e3) / 1e9, 1) if traffic else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, full-size launch "
-                                  "(profiles/), per point x points" if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a full-size launch at "
+                                  "leaf 32 (profiles/), per point x points; the leaf records are under 1% "
+                                  "of it" if traffic else None,
                 "ms_per_launch": round(per_launch_ms, 4), "bytes_per_launch": bytes_alg}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -386,11 +405,14 @@ def main():
                                        f"{spec.x1 - spec.x0:.0f} x {spec.y1 - spec.y0:.0f} m, plain GPU path "
                                        f"(one cloud per launch sequence)",
                            "wsize": W, "overlap": Ov, "bsize": B, "leaf_max_number": mn,
+                           "leaf_tuning_ms": leaf_tuning["ms"] if leaf_tuning else None,
                            "windows": int(p.ncells), "cells": int(p.ngrid), "seeds": int(len(seeds)),
                            "l2": "inputs (2.4 GB at 100M points) larger than L2; no flush",
                            "parallelism": f"replicas x{ws}"},
                 "phases_ms": {"tree": round(phase[0] / args.steps, 4), "stage1": round(phase[1] / args.steps, 4),
                               "stage2": round(phase[2] / args.steps, 4), "stage3": round(phase[3] / args.steps, 4)},
+                "kernel_timing": "second pass over the same K steps with CUDA events around every launch "
+                                 "(the value pass runs without them)",
                 "kernels": {k: {"ms": round(v[0] / args.steps, 4), "share": round(v[0] / tot_k, 4),
                                 "launches_per_step": v[1] / args.steps} for k, v in
                             sorted(ktimes.items(), key=lambda kv: -kv[1][0])},

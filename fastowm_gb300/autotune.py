@@ -66,3 +66,34 @@ def tune_leaf_classes(ctx, bounds=DEFAULT_BOUNDS, leaves=DEFAULT_LEAVES, tiles_p
 
 def apply(batch, tuned: dict) -> None:
     batch.set_leaf_classes(tuned["bounds"], tuned["leaves"])
+
+
+def tune_leaf_single(ctx, cloud, make_cfg, leaves=(32, 64, 128), reps: int = 3) -> dict:
+    """Leaf size for one cloud: times owm_run on the device-resident cloud
+    with each candidate (make_cfg(leaf) -> RunCfg) and returns
+    {"leaf": best, "ms": {leaf: median ms}}.  Every choice gives the same
+    seeds; the tuner checks that too."""
+    import torch
+
+    import fastowm_gb300 as F
+
+    stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
+    timings, ref = {}, None
+    for leaf in leaves:
+        cfg = make_cfg(leaf)
+        seeds = ctx.run(cloud, cfg)  # warm-up (buffers)
+        if ref is None:
+            ref = seeds
+        elif not np.array_equal(seeds, ref):
+            raise RuntimeError(f"leaf {leaf}: seeds differ from leaf {leaves[0]}")
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.run(cloud, cfg)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        timings[leaf] = round(float(np.median(ts)), 3)
+    best = min(timings, key=timings.get)
+    return {"leaf": best, "ms": timings}
