@@ -159,8 +159,8 @@ def kernel_bytes(name: str, n: int, p, nleaves: int) -> float | None:
     """Algorithmic bytes per launch of the main kernels (per-unit figures x units)."""
     if name == "k_query_s1":  # read sorted points once, node summaries, one result per window
         return 24.0 * n + 48.0 * nleaves + 8.0 * p.ncells
-    if name.startswith("k_gather_leaves"):  # perm + xyz in; keyed points, id, class index and leaf out
-        return (4 + 24 + 24 + 4 + 4) * n + 48.0 * nleaves
+    if name.startswith("k_gather_leaves"):  # perm + xyz in; keyed points, id and leaf out
+        return (4 + 24 + 24 + 4) * n + 48.0 * nleaves
     if name == "k_rs_downsweep":
         return 16.0 * n
     if name == "k_morton":

@@ -9,7 +9,7 @@
 //     per-tile offsets;
 //   * stage 1 by exact window classes: per-tile class tables built by two
 //     launches, every point folded into its tile's sub-cell counters inside
-//     the gather, then batched tie-id, row and window reductions (a tile that
+//     the gather, then batched row and window reductions (a tile that
 //     asks for the tree walk switches the whole batch to the persistent walk);
 //   * stage 3 (and the stage-1 walk) is one persistent query launch: warps
 //     pull 4 x 8 window patches of any tile from one work counter, which
@@ -93,11 +93,12 @@ __global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restric
       const int32_t lp = first + c0 + lane;
       const bool valid = c0 + lane < cnt;
       int64_t x = 0, y = 0, z = 0;
+      uint32_t id = 0;
       if (valid) {
         const int64_t gp = m.pt_off + lp;
         const uint32_t src = __ldg(perm + gp);
         finite &= load_point(xyz, src, x, y, z);
-        const uint32_t id = (uint32_t)((int64_t)src - m.pt_off + 1);
+        id = (uint32_t)((int64_t)src - m.pt_off + 1);
         xk[gp] = x;
         yk[gp] = y;
         zk[gp] = z;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restric
             z = 0;
           }
         }
-        cls_aggregate_warp(cls[t], lp, valid, x, y, z, lane);
+        cls_aggregate_warp(cls[t], valid, x, y, z, id, lane);
       }
     }
     acc.reduce(32);
@@ -152,14 +153,6 @@ __global__ void k_bc_prep(const ClassArgs* __restrict__ cls) {
     if (i < A.ny) cls_range_one(A.Ly, A.Ry, A.ny, i, A.syl + i, A.syh + i);
     if (i < A.qx) const_cast<int2*>(A.tabx)[i] = cls_table_one(A.Lx, A.Rx, A.nx, A.kx0, A.shx, i);
     if (i < A.qy) const_cast<int2*>(A.taby)[i] = cls_table_one(A.Ly, A.Ry, A.ny, A.ky0, A.shy, i);
-  }
-}
-
-__global__ void k_bc_ids(const ClassArgs* __restrict__ cls, const int64_t* __restrict__ pt_off, int ntiles,
-                         const int64_t* __restrict__ zk, const uint32_t* __restrict__ pid, int64_t n) {
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
-    const int t = tile_of(pt_off, ntiles, g);
-    cls_ids_one(cls[t], g - __ldg(pt_off + t), __ldg(zk + g), __ldg(pid + g));
   }
 }
 
@@ -428,7 +421,7 @@ struct Plan {
   int64_t nsub = 0, rows_total = 0;
   size_t cls_misc = 0;
   int32_t cls_grid_x = 1;          // blocks per tile of the class prepare launches
-  size_t o_cls = 0, o_rowsoff = 0, o_cidx = 0, o_ccount = 0, o_czmin = 0, o_cidmin = 0, o_cmisc = 0;
+  size_t o_cls = 0, o_rowsoff = 0, o_ccount = 0, o_czid = 0, o_cmisc = 0;
   // buffer offsets (bytes) inside the batch buffer
   size_t o_xyz, o_k0, o_k1, o_v0, o_v1, o_sort, o_xk, o_yk, o_zk, o_pid, o_nodes, o_parent, o_flags, o_right,
       o_last, o_edges, o_win, o_s2k0, o_s2k1, o_s2f, o_s2p, o_s2t, o_llp, o_mark, o_cmin, o_cf, o_cp, o_ct, o_s3,
@@ -642,10 +635,8 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
   if (P->classes) {
     P->o_cls = take((size_t)ntiles * sizeof(ClassArgs));
     P->o_rowsoff = take((size_t)T1 * 8);
-    P->o_cidx = take((size_t)N * 4);
     P->o_ccount = take((size_t)std::max<int64_t>(P->nsub, 1) * 4);
-    P->o_czmin = take((size_t)std::max<int64_t>(P->nsub, 1) * 8);
-    P->o_cidmin = take((size_t)std::max<int64_t>(P->nsub, 1) * 4);
+    P->o_czid = take((size_t)std::max<int64_t>(P->nsub, 1) * 16);
     P->o_cmisc = take(std::max<size_t>(P->cls_misc, 16));
   }
   P->total = o;
@@ -867,9 +858,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       a.rz = reinterpret_cast<unsigned long long*>(misc + l.rz);
       a.ri = reinterpret_cast<uint32_t*>(misc + l.ri);
       a.count = reinterpret_cast<uint32_t*>(at(P.o_ccount)) + l.sub_off;
-      a.zmin = reinterpret_cast<unsigned long long*>(at(P.o_czmin)) + l.sub_off;
-      a.idmin = reinterpret_cast<uint32_t*>(at(P.o_cidmin)) + l.sub_off;
-      a.cidx = reinterpret_cast<uint32_t*>(at(P.o_cidx)) + P.pt_off[t];
+      a.zid = reinterpret_cast<ulonglong2*>(at(P.o_czid)) + l.sub_off;
     }
     d_cls = reinterpret_cast<ClassArgs*>(at(P.o_cls));
     d_rowsoff = reinterpret_cast<int64_t*>(at(P.o_rowsoff));
@@ -939,8 +928,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
         OWM_LAUNCH("k_bc_prep", s, k_bc_prep<<<gp, 256, 0, s>>>(d_cls));
         count_launch(L, 2);
         if (cudaMemsetAsync(at(P.o_ccount), 0, (size_t)P.nsub * 4, s) != cudaSuccess ||
-            cudaMemsetAsync(at(P.o_czmin), 0xFF, (size_t)P.nsub * 8, s) != cudaSuccess ||
-            cudaMemsetAsync(at(P.o_cidmin), 0xFF, (size_t)P.nsub * 4, s) != cudaSuccess) {
+            cudaMemsetAsync(at(P.o_czid), 0xFF, (size_t)P.nsub * 16, s) != cudaSuccess) {
           rc2 = OWM_ECUDA;
           break;
         }
@@ -968,8 +956,6 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       count_launch(L, 2);
       // stage 1: window classes (tie ids, rows, windows), or the persistent walk
       if (P.classes) {
-        OWM_LAUNCH("k_bc_ids", s, k_bc_ids<<<gsz(N), 256, 0, s>>>(d_cls, d_ptoff, ntiles, zk, pid, N));
-        count_launch(L);
         if (P.rows_total > 0) {
           OWM_LAUNCH("k_bc_rows", s, k_bc_rows<<<gsz(P.rows_total), 256, 0, s>>>(d_cls, d_rowsoff, ntiles, P.rows_total));
           count_launch(L);

@@ -88,8 +88,9 @@ __global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict_
       int64_t pos = u * kUnit + c + lane;
       const bool valid = pos < n;
       int64_t x = 0, y = 0, z = 0;
+      uint32_t src = 0;
       if (valid) {
-        uint32_t src = __ldg(perm + pos);
+        src = __ldg(perm + pos);
         finite &= load_point16(xyz, src, x, y, z);
         xk[pos] = x;
         yk[pos] = y;
@@ -106,7 +107,7 @@ __global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict_
             z = 0;
           }
         }
-        cls_aggregate_warp(A, pos, valid, x, y, z, lane);
+        cls_aggregate_warp(A, valid, x, y, z, src + 1, lane);
       }
     }
     acc.reduce(kSeg);

@@ -9,10 +9,10 @@
 //                     point's class is one table read and two compares),
 //                     counter resets
 //   aggregation       per sorted point: its sub-cell; warp match + reduce of
-//                     (count, min z), one atomic pair per group -- fused into
-//                     the build's gather for owm_run, or k_cls_aggregate
-//   k_cls_ids         the min id among the points holding their sub-cell's
-//                     min z (ties break on (z, id))
+//                     (count, (z, id)-min), then per group one atomic add and
+//                     one 128-bit atomic min of the (z, id) pair (ties break
+//                     on (z, id)) -- fused into the build's gather for
+//                     owm_run, or k_cls_aggregate
 //   k_cls_rows        per (window column, sub-cell row): reduce along x
 //   k_cls_windows     per window: reduce along y, apply minNumPoints
 // All integer: containment is exact by construction, and the search starts
@@ -55,20 +55,16 @@ __global__ void k_cls_ranges(const int64_t* __restrict__ L, const int64_t* __res
 
 __global__ void __launch_bounds__(kClsBlock) k_cls_aggregate(ClassArgs A, const int64_t* __restrict__ xk,
                                                              const int64_t* __restrict__ yk,
-                                                             const int64_t* __restrict__ zk, int64_t n) {
+                                                             const int64_t* __restrict__ zk,
+                                                             const uint32_t* __restrict__ pid, int64_t n) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * kClsBlock) >> 5;
   for (int64_t wb = (((int64_t)blockIdx.x * kClsBlock + threadIdx.x) >> 5) * 32; wb < n; wb += nwarps * 32) {
     const int64_t pos = wb + lane;
     const bool valid = pos < n;
     const int64_t q = valid ? pos : wb;
-    cls_aggregate_warp(A, pos, valid, __ldg(xk + q), __ldg(yk + q), __ldg(zk + q), lane);
+    cls_aggregate_warp(A, valid, __ldg(xk + q), __ldg(yk + q), __ldg(zk + q), __ldg(pid + q), lane);
   }
-}
-
-__global__ void k_cls_ids(ClassArgs A, const int64_t* __restrict__ zk, const uint32_t* __restrict__ pid, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    cls_ids_one(A, i, __ldg(zk + i), __ldg(pid + i));
 }
 
 __global__ void k_cls_rows(ClassArgs A) {
@@ -113,9 +109,10 @@ bool cls_table_geometry(double lo, double hi, double step, int64_t* k0, int* sh,
 
 size_t classes_scratch_bytes(int64_t n, int32_t ncols, int32_t nrows) {
   const int64_t tx = 2 * (int64_t)ncols + 1, ty = 2 * (int64_t)nrows + 1;
-  return 2 * a256((size_t)kMaxTable * 8) + a256((size_t)n * 4) + 2 * a256((size_t)ncols * 8) +
+  (void)n;  // nothing per point: the sub-cell counters are the whole state
+  return 2 * a256((size_t)kMaxTable * 8) + 2 * a256((size_t)ncols * 8) +
          2 * a256((size_t)nrows * 8) + 2 * a256((size_t)ncols * 4) + 2 * a256((size_t)nrows * 4) +
-         a256((size_t)(tx * ty) * 4) + a256((size_t)(tx * ty) * 8) + a256((size_t)(tx * ty) * 4) +
+         a256((size_t)(tx * ty) * 4) + a256((size_t)(tx * ty) * 16) +
          2 * a256((size_t)(ncols * ty) * 4) + a256((size_t)(ncols * ty) * 8) + 1024;
 }
 
@@ -135,7 +132,6 @@ int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* s
   std::memset(A, 0, sizeof(*A));
   int2* tabx = (int2*)take((size_t)kMaxTable * 8);
   int2* taby = (int2*)take((size_t)kMaxTable * 8);
-  A->cidx = (uint32_t*)take((size_t)n * 4);
   int64_t* Lx = (int64_t*)take((size_t)nc * 8);
   int64_t* Rx = (int64_t*)take((size_t)nc * 8);
   int64_t* Ly = (int64_t*)take((size_t)nr * 8);
@@ -145,8 +141,7 @@ int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* s
   A->syl = (int32_t*)take((size_t)nr * 4);
   A->syh = (int32_t*)take((size_t)nr * 4);
   A->count = (uint32_t*)take((size_t)(tx * ty) * 4);
-  A->zmin = (unsigned long long*)take((size_t)(tx * ty) * 8);
-  A->idmin = (uint32_t*)take((size_t)(tx * ty) * 4);
+  A->zid = (ulonglong2*)take((size_t)(tx * ty) * 16);
   A->rc = (uint32_t*)take((size_t)(nc * ty) * 4);
   A->rz = (unsigned long long*)take((size_t)(nc * ty) * 8);
   A->ri = (uint32_t*)take((size_t)(nc * ty) * 4);
@@ -171,8 +166,7 @@ int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* s
   if (A->qy) OWM_LAUNCH("k_cls_table", s, k_cls_table<<<(A->qy + 255) / 256, 256, 0, s>>>(Ly, Ry, nr, A->ky0, A->shy, A->qy, taby));
   count_launch(launches, (A->qx > 0) + (A->qy > 0));
   OWM_CUDA_TRY(cudaMemsetAsync(A->count, 0, (size_t)(tx * ty) * 4, s));
-  OWM_CUDA_TRY(cudaMemsetAsync(A->zmin, 0xFF, (size_t)(tx * ty) * 8, s));
-  OWM_CUDA_TRY(cudaMemsetAsync(A->idmin, 0xFF, (size_t)(tx * ty) * 4, s));
+  OWM_CUDA_TRY(cudaMemsetAsync(A->zid, 0xFF, (size_t)(tx * ty) * 16, s));
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
 }
@@ -180,7 +174,7 @@ int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* s
 int classes_aggregate(const ClassArgs& A, const TreeView& t, int64_t n, cudaStream_t s, int64_t* launches) {
   int64_t blocks = std::min<int64_t>(((n + 31) / 32 * 32 + kClsBlock - 1) / kClsBlock, 152 * 8);
   OWM_LAUNCH("k_cls_aggregate", s, k_cls_aggregate<<<(unsigned)std::max<int64_t>(blocks, 1), kClsBlock, 0, s>>>(
-      A, t.xk, t.yk, t.zk, n));
+      A, t.xk, t.yk, t.zk, t.pid, n));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
@@ -188,10 +182,11 @@ int classes_aggregate(const ClassArgs& A, const TreeView& t, int64_t n, cudaStre
 
 int classes_finish(const ClassArgs& A, const TreeView& t, int64_t n, const owm_params& p, uint32_t* d_win,
                    cudaStream_t s, int64_t* launches) {
-  OWM_LAUNCH("k_cls_ids", s, k_cls_ids<<<grid(n), 256, 0, s>>>(A, t.zk, t.pid, n));
+  (void)t;
+  (void)n;
   OWM_LAUNCH("k_cls_rows", s, k_cls_rows<<<grid((int64_t)A.nx * A.ty), 256, 0, s>>>(A));
   OWM_LAUNCH("k_cls_windows", s, k_cls_windows<<<grid((int64_t)A.nx * A.ny), 256, 0, s>>>(A, p.min_num_points, d_win));
-  count_launch(launches, 3);
+  count_launch(launches, 2);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
 }

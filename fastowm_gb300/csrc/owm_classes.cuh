@@ -21,9 +21,7 @@ struct ClassArgs {
   int32_t shx, shy, qx, qy;
   int32_t tx, ty;                     // sub-cell grid: 2*nx+1 by 2*ny+1
   uint32_t* count;                    // [tx*ty] points per sub-cell
-  unsigned long long* zmin;           // [tx*ty] min z (order key, sign-flipped)
-  uint32_t* idmin;                    // [tx*ty] min id among the min-z points
-  uint32_t* cidx;                     // [n] sub-cell of every sorted point
+  ulonglong2* zid;                    // [tx*ty] (z order key sign-flipped, id): the (z, id)-min
   int32_t *sxl, *sxh, *syl, *syh;     // s-range of every window column / row
   uint32_t *rc, *ri;                  // row reduction buffers [nx*ty]
   unsigned long long* rz;
@@ -49,11 +47,42 @@ __device__ __forceinline__ int64_t cls_wmax64(int64_t v) {
   return v;
 }
 
+// 128-bit compare-and-swap on global memory (sm_90+): *addr = {new_lo,
+// new_hi} if it equals {cmp_lo, cmp_hi}; returns the value found.
+__device__ __forceinline__ void cls_cas128(ulonglong2* addr, unsigned long long cmp_lo, unsigned long long cmp_hi,
+                                           unsigned long long new_lo, unsigned long long new_hi,
+                                           unsigned long long* old_lo, unsigned long long* old_hi) {
+  asm volatile(
+      "{\n\t.reg .b128 d, b, c;\n\t"
+      "mov.b128 b, {%2, %3};\n\t"
+      "mov.b128 c, {%4, %5};\n\t"
+      "atom.global.cas.b128 d, [%6], b, c;\n\t"
+      "mov.b128 {%0, %1}, d;\n\t}"
+      : "=l"(*old_lo), "=l"(*old_hi)
+      : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "l"(addr)
+      : "memory");
+}
+
+// Lexicographic atomic min of (z, id) in one 16-byte word.  Lock-free: a
+// failed swap means another thread stored a smaller pair, and the stored pair
+// only decreases, so the loop ends.  A stale first read is never below the
+// stored pair, so returning early on it is safe.
+__device__ __forceinline__ void cls_zid_min(ulonglong2* p, unsigned long long z, unsigned long long id) {
+  ulonglong2 cur = __ldcg(p);
+  while (z < cur.x || (z == cur.x && id < cur.y)) {
+    unsigned long long lo, hi;
+    cls_cas128(p, cur.x, cur.y, z, id, &lo, &hi);
+    if (lo == cur.x && hi == cur.y) break;
+    cur.x = lo;
+    cur.y = hi;
+  }
+}
+
 // All 32 lanes call this together, each with one point (valid or not).
-// Writes the point's sub-cell to cidx[pos] and folds (count, min z) of the
-// warp's points into the sub-cell counters with one atomic pair per group.
-__device__ __forceinline__ void cls_aggregate_warp(const ClassArgs& A, int64_t pos, bool valid, int64_t px,
-                                                   int64_t py, int64_t pz, int lane) {
+// Folds the warp's points into their sub-cells: per group of lanes in one
+// sub-cell, one atomic add of the count and one (z, id) atomic min.
+__device__ __forceinline__ void cls_aggregate_warp(const ClassArgs& A, bool valid, int64_t px, int64_t py,
+                                                   int64_t pz, uint32_t id, int lane) {
   int32_t sx = -1, sy = -1;
   if (A.qx > 0) {  // table: one read + one compare per edge array
     const int64_t q = (px - A.kx0) >> A.shx;
@@ -89,18 +118,15 @@ __device__ __forceinline__ void cls_aggregate_warp(const ClassArgs& A, int64_t p
   }
   const uint32_t c = (uint32_t)sy * (uint32_t)A.tx + (uint32_t)sx;
   const unsigned long long zu = valid ? ((unsigned long long)pz ^ 0x8000000000000000ull) : ~0ull;
-  if (valid) A.cidx[pos] = c;
   const uint32_t peers = __match_any_sync(0xffffffffu, valid ? c : 0xFFFFFFFFu);
   if (valid) {
     const uint32_t hi = (uint32_t)(zu >> 32), lo = (uint32_t)zu;
     const uint32_t mh = __reduce_min_sync(peers, hi);
-    const uint32_t sub = __ballot_sync(peers, hi == mh);
-    uint32_t ml = 0xFFFFFFFFu;
-    if (hi == mh) ml = __reduce_min_sync(sub, lo);
-    ml = __shfl_sync(peers, ml, __ffs(sub) - 1);
+    const uint32_t ml = __reduce_min_sync(peers, hi == mh ? lo : 0xFFFFFFFFu);
+    const uint32_t mid = __reduce_min_sync(peers, (hi == mh && lo == ml) ? id : 0xFFFFFFFFu);
     if (lane == __ffs(peers) - 1) {
       atomicAdd(A.count + c, (uint32_t)__popc(peers));
-      atomicMin(A.zmin + c, ((unsigned long long)mh << 32) | ml);
+      cls_zid_min(A.zid + c, ((unsigned long long)mh << 32) | ml, mid);
     }
   }
 }
@@ -131,14 +157,6 @@ __device__ __forceinline__ int2 cls_table_one(const int64_t* L, const int64_t* R
   return make_int2(cls_count_less(L, n, qs), cls_count_less(R, n, qs));
 }
 
-// Tie id of sorted point i (index into A.cidx): among the points holding
-// their sub-cell's min z, the smallest id.
-__device__ __forceinline__ void cls_ids_one(const ClassArgs& A, int64_t i, int64_t zk, uint32_t pid) {
-  const uint32_t c = A.cidx[i];
-  const unsigned long long zu = (unsigned long long)zk ^ 0x8000000000000000ull;
-  if (zu == A.zmin[c]) atomicMin(A.idmin + c, pid);
-}
-
 __device__ __forceinline__ bool cls_zu_less(unsigned long long za, uint32_t ia, unsigned long long zb, uint32_t ib) {
   return za < zb || (za == zb && ia < ib);
 }
@@ -151,8 +169,9 @@ __device__ __forceinline__ void cls_row_one(const ClassArgs& A, int64_t k) {
   const int64_t base = (int64_t)t * A.tx;
   for (int32_t s = A.sxl[ii]; s <= A.sxh[ii]; ++s) {
     c += A.count[base + s];
-    const unsigned long long z = A.zmin[base + s];
-    const uint32_t id = A.idmin[base + s];
+    const ulonglong2 e = A.zid[base + s];
+    const unsigned long long z = e.x;
+    const uint32_t id = (uint32_t)e.y;
     if (cls_zu_less(z, id, bz, bi)) {
       bz = z;
       bi = id;
