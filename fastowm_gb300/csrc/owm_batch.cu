@@ -438,7 +438,10 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
   for (auto* v : {&P->leaf_off, &P->node_off, &P->int_off, &P->ex_off, &P->ey_off, &P->cx_off, &P->cy_off})
     v->assign(ntiles + 1, 0);
   P->tile_bits = std::max(1, bits_for((uint64_t)ntiles - 1));
-  P->mbits = std::min(16, (32 - P->tile_bits) / 2);
+  // Morton bits per axis: fit (tile, Morton) keys in 24 bits (three 8-bit
+  // sort passes) while that leaves at least 7 bits per axis (128 x 128 cells
+  // per tile); else use up to 32 bits.  Seeds do not depend on it.
+  P->mbits = (24 - P->tile_bits) / 2 >= 7 ? (24 - P->tile_bits) / 2 : std::min(16, (32 - P->tile_bits) / 2);
   P->classes = true;
   for (int32_t t = 0; t < ntiles; ++t) P->classes &= td[t].cfg.stage1_walk == 0;
   if (P->classes) {
