@@ -580,23 +580,42 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
   int rc = a.input.reserve((size_t)n * 24 + kXyzSlack, c->copy_stream);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(a.input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->copy_stream));
-  OWM_CUDA_TRY(cudaEventRecord(a.ready, c->copy_stream));
-  OWM_CUDA_TRY(cudaStreamWaitEvent(c->stream, a.ready, 0));
+  // From here on the copy may still be reading xyz: a failed submit waits for
+  // it before returning, so the caller may free xyz after any return.
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamSynchronize(c->stream);
+    return code;
+  };
+  cudaError_t e = cudaEventRecord(a.ready, c->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, a.ready, 0);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
+    return fail(OWM_ECUDA);
+  }
   int64_t* d_seeds = nullptr;
   int64_t room = 0;
   rc = run_pipeline_enqueue(c, static_cast<const double*>(a.input.ptr), n, bb, *cfg, &a.p, &d_seeds, &room);
-  if (rc) return rc;
+  if (rc) return fail(rc);
   if (a.h_cap < room) {
-    OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));  // growth only: the old staging may still be a copy target
+    // growth only: the old staging may still be a copy target
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(OWM_ECUDA);
     if (a.h_seeds) cudaFreeHost(a.h_seeds);
     a.h_seeds = nullptr;
     a.h_cap = 0;
-    OWM_CUDA_TRY(cudaMallocHost(&a.h_seeds, (size_t)room * 8));
+    if (cudaMallocHost(&a.h_seeds, (size_t)room * 8) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(OWM_ENOMEM);
+    }
     a.h_cap = room;
   }
-  OWM_CUDA_TRY(cudaMemcpyAsync(a.h_words, c->d_small, 32, cudaMemcpyDeviceToHost, c->stream));
-  OWM_CUDA_TRY(cudaMemcpyAsync(a.h_seeds, d_seeds, (size_t)room * 8, cudaMemcpyDeviceToHost, c->stream));
-  OWM_CUDA_TRY(cudaEventRecord(a.done, c->stream));
+  e = cudaMemcpyAsync(a.h_words, c->d_small, 32, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a.h_seeds, d_seeds, (size_t)room * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(a.done, c->stream);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
+    return fail(OWM_ECUDA);
+  }
   a.seeds = seeds;
   a.cap = cap;
   a.room = room;
