@@ -16,7 +16,7 @@ from pathlib import Path
 import numpy as np
 
 DEFAULT_BOUNDS = (150_000, 500_000, 1_000_000, 1 << 40)
-DEFAULT_LEAVES = (16, 32, 64, 128)
+DEFAULT_LEAVES = (16, 32, 64, 128, 256)
 
 
 def _class_tiles(F, lo: int, hi: int, want: int, config: int = 4, start: int = 0, limit: int = 4096):
@@ -68,7 +68,7 @@ def apply(batch, tuned: dict) -> None:
     batch.set_leaf_classes(tuned["bounds"], tuned["leaves"])
 
 
-def tune_leaf_single(ctx, cloud, make_cfg, leaves=(32, 64, 128), reps: int = 3) -> dict:
+def tune_leaf_single(ctx, cloud, make_cfg, leaves=(32, 64, 128, 256), reps: int = 3) -> dict:
     """Leaf size for one cloud: times owm_run on the device-resident cloud
     with each candidate (make_cfg(leaf) -> RunCfg) and returns
     {"leaf": best, "ms": {leaf: median ms}}.  Every choice gives the same
