@@ -937,7 +937,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
         }
       }
       {
-        int64_t blocks = std::min<int64_t>((P.nleaves * 32 + 255) / 256, 152 * 16);
+        // one warp per leaf: resident warps then work on neighbouring leaves
+        int64_t blocks = std::min<int64_t>((P.nleaves * 32 + 255) / 256, (int64_t)152 * 1024);
         OWM_LAUNCH("k_b_gather_leaves", s, k_b_gather_leaves<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(
             xyz, perm, d_meta, d_leafoff, ntiles, P.nleaves, xk, yk, zk, pid, nodes, words, d_cls));
         count_launch(L);
