@@ -388,7 +388,7 @@ def main():
                 "traffic": round(traffic) if traffic else None,
                 "traffic_gbs": round(traffic / (per_launch_ms / 1e3) / 1e9, 1) if traffic else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a full-size launch at "
-                                  "leaf 64 (profiles/), per point x points; the leaf records are under 1% "
+                                  "leaf 256 (profiles/), per point x points; the leaf records are under 1% "
                                   "of it" if traffic else None,
                 "ms_per_launch": round(per_launch_ms, 4), "bytes_per_launch": bytes_alg}
     cpu = None
