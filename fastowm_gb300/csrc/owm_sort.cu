@@ -4,7 +4,7 @@
 // Radix pass over a tile of 4096 keys per 256-thread block:
 //   upsweep    digit histogram of the tile (vectorised 16-byte key loads)
 //   scan       exclusive scan of the digit-major [256 x tiles] count table
-//   downsweep  stable ranking inside the tile with __match_any_sync warp
+//   downsweep  stable ranking inside the tile with a ballot-based warp
 //              multisplit, keys/values staged in shared memory in digit order,
 //              then written out so that each digit's run is a contiguous,
 //              coalesced stretch of the output.
@@ -31,6 +31,21 @@ constexpr int kScanChunk = kScanBlock * kScanItems;  // 8192 values per block
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Lanes of the warp whose 8-bit digit equals this lane's, among the lanes
+// with valid set: one ballot per digit bit, the mask narrowed by each
+// (warp-level multisplit by ballots, Ashkiani et al., 2016).  Cheaper than
+// the general 32-bit match instruction when the label has few bits.
+__device__ __forceinline__ uint32_t match_digit8(uint32_t d, bool valid) {
+  uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const uint32_t bit = (d >> b) & 1u;
+    const uint32_t v = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? v : ~v;
+  }
   return m;
 }
 
@@ -185,8 +200,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __re
   for (int i = 0; i < kItems; ++i) {
     int64_t p = warp_base + i * 32 + lane;
     bool valid = full || p < n;
-    uint32_t d = valid ? ((k[i] >> shift) & 255u) : 256u;
-    uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t d = (k[i] >> shift) & 255u;
+    uint32_t peers = match_digit8(d, valid);
     uint32_t before = valid ? s_wcnt[w][d] : 0u;
     __syncwarp();
     uint32_t r = __popc(peers & lt);
@@ -340,8 +355,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     for (int i = 0; i < kItems; ++i) {
       const int32_t lp = w * 32 * kItems + i * 32 + lane;
       const bool valid = lp < tn;
-      const uint32_t d = valid ? ((k[i] >> shift) & 255u) : 256u;
-      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t d = (k[i] >> shift) & 255u;
+      const uint32_t peers = match_digit8(d, valid);
       const uint32_t before = valid ? wcnt[w * kRadix + d] : 0u;
       __syncwarp();
       const uint32_t r = __popc(peers & lt);
