@@ -313,8 +313,8 @@ __global__ void k_b_s2_flags(const uint32_t* __restrict__ keys, int64_t n, int i
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     uint32_t k = keys[i];
     uint32_t t = k >> idbits;
-    bool f = (k & none) != none && (i == 0 || keys[i - 1] != k);
-    if (meta[t].need_dup) f = f && (i + 1 < n && keys[i + 1] == k);
+    bool f = (k & none) != none;  // overlap 0: every valid minimum
+    if (meta[t].need_dup) f = f && (i == 0 || keys[i - 1] != k) && (i + 1 < n && keys[i + 1] == k);
     flags[i] = f ? 1u : 0u;
     if (f) atomicAdd(tile_count + t, 1u);
   }

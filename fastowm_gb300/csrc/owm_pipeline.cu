@@ -118,7 +118,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   // scratch = [tree build | window classes]; stages 2 and 3 reuse it after stage 1
   const size_t tbytes = (tree_scratch_bytes(n) + 255) & ~(size_t)255;
   const size_t cbytes = cfg.stage1_walk ? 0 : classes_scratch_bytes(n, (int32_t)p.ncols, (int32_t)p.nrows);
-  size_t sbytes = std::max(tbytes + cbytes, std::max(stage2_scratch_bytes(nc), stage3_scratch_bytes(ng)));
+  size_t sbytes = std::max(tbytes + cbytes, std::max(std::max(stage2_bitmap_scratch_bytes(n), stage2_scratch_bytes(nc)), stage3_scratch_bytes(ng)));
   rc = c->scratch.reserve(sbytes, c->stream);
   if (rc) return rc;
   size_t obytes = 2 * al(65536 * sizeof(Edge)) + 2 * al((size_t)nc * 4) + al((size_t)std::max<int64_t>(ng, 1) * 4) +
@@ -165,7 +165,9 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   }
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[2], s));
-  rc = run_stage2(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches);
+  rc = p.overlap > 0.0
+           ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches)
+           : run_stage2(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
   rc = run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, c->scratch.ptr, c->scratch.cap, c->d_job,

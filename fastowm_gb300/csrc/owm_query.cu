@@ -21,7 +21,8 @@
 // "inside"/"outside" when that is certain.
 //
 // Stage 2 (owm_optim3.cpp:160,173; optim3_func.cpp:610-625): radix sort of
-// the window results, then ids with run length >= 2, ascending.
+// the window results, then ids with run length >= 2, ascending; for one cloud
+// with overlap > 0 occupancy bitmaps give the same list without the sort.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -282,14 +283,51 @@ __global__ void k_s2_keys(const uint32_t* __restrict__ win, int64_t n, uint32_t 
 }
 
 // Sorted keys -> flag of the first element of every run of length >= 2
-// (overlap > 0), or of every valid run (overlap == 0).
+// (overlap > 0), or of every valid element (overlap == 0: the reference
+// counts all valid minima there, owm_optim3.cpp:185-188, and this build
+// compacts them; only the sentinel id 0 of empty windows can repeat).
 __global__ void k_s2_flags(const uint32_t* __restrict__ keys, int64_t n, uint32_t none_key, int need_dup,
                            uint32_t* __restrict__ flags) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     uint32_t k = keys[i];
-    bool f = k != none_key && (i == 0 || keys[i - 1] != k);
-    if (need_dup) f = f && (i + 1 < n && keys[i + 1] == k);
+    bool f = k != none_key;
+    if (need_dup) f = f && (i == 0 || keys[i - 1] != k) && (i + 1 < n && keys[i + 1] == k);
     flags[i] = f ? 1u : 0u;
+  }
+}
+
+// Stage 2 with overlap > 0 by occupancy bitmaps.  Ids of one cloud lie in
+// [0, npoints]: the first atomic OR of an id's bit into `once` returns the old
+// word, so a second occurrence also sets the bit in `twice`.  The LLPs are
+// the set bits of `twice` -- ids that are the minimum of two or more windows
+// -- in ascending id order: the list that sorting the minima and keeping the
+// first id of every run of length >= 2 gives (owm_optim3.cpp:160-173,
+// stage2 in optim3_func.cpp:609-625).
+__global__ void k_s2_mark(const uint32_t* __restrict__ win, int64_t n, uint32_t max_id,
+                          uint32_t* __restrict__ once, uint32_t* __restrict__ twice) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = win[i];
+    if (v > max_id) continue;  // kNone (and nothing else: ids are <= max_id)
+    const uint32_t bit = 1u << (v & 31u);
+    const uint32_t old = atomicOr(once + (v >> 5), bit);
+    if (old & bit) atomicOr(twice + (v >> 5), bit);
+  }
+}
+
+__global__ void k_s2_popc(const uint32_t* __restrict__ bm, int64_t nw, uint32_t* __restrict__ cnt) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x)
+    cnt[w] = (uint32_t)__popc(bm[w]);
+}
+
+__global__ void k_s2_emit(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ pos, int64_t nw,
+                          uint32_t* __restrict__ out) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t b = bm[w];
+    uint32_t p = pos[w];
+    while (b) {
+      out[p++] = (uint32_t)(w * 32) + (uint32_t)(__ffs(b) - 1);
+      b &= b - 1;
+    }
   }
 }
 
@@ -446,6 +484,44 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
   count_launch(launches);
   OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, n, d_count, ct, cb, s, launches));
   OWM_LAUNCH("k_compact", s, k_compact<<<grid1d(n), 256, 0, s>>>(sk, flags, pos, n, d_llp));
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+size_t stage2_bitmap_scratch_bytes(int64_t npoints) {
+  const int64_t nw = (npoints + 1 + 31) / 32;
+  return 4 * align256((size_t)nw * 4) + align256(scan_temp_bytes(nw)) + 1024;
+}
+
+int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
+                      uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches) {
+  if (n <= 0) {
+    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+    return OWM_OK;
+  }
+  if (npoints < 0 || npoints >= (int64_t)kNone || !(overlap > 0.0)) return OWM_EINVAL;
+  if (scratch_bytes < stage2_bitmap_scratch_bytes(npoints)) return OWM_ENOMEM;
+  const int64_t nw = (npoints + 1 + 31) / 32;  // bits for ids 0..npoints
+  char* sp = static_cast<char*>(scratch);
+  auto take = [&](size_t b) {
+    void* p = sp;
+    sp += align256(b);
+    return p;
+  };
+  uint32_t* once = (uint32_t*)take((size_t)nw * 4);
+  uint32_t* twice = (uint32_t*)take((size_t)nw * 4);
+  uint32_t* cnt = (uint32_t*)take((size_t)nw * 4);
+  uint32_t* pos = (uint32_t*)take((size_t)nw * 4);
+  size_t cb = scan_temp_bytes(nw);
+  void* ct = take(cb);
+  OWM_CUDA_TRY(cudaMemsetAsync(once, 0, 2 * align256((size_t)nw * 4), s));  // once, then twice
+  OWM_LAUNCH("k_s2_mark", s, k_s2_mark<<<grid1d(n), 256, 0, s>>>(d_win, n, (uint32_t)npoints, once, twice));
+  const uint32_t* sel = twice;
+  OWM_LAUNCH("k_s2_popc", s, k_s2_popc<<<grid1d(nw), 256, 0, s>>>(sel, nw, cnt));
+  count_launch(launches, 2);
+  OWM_CUDA_TRY(exclusive_scan_u32(cnt, pos, nw, d_count, ct, cb, s, launches));
+  OWM_LAUNCH("k_s2_emit", s, k_s2_emit<<<grid1d(nw), 256, 0, s>>>(sel, pos, nw, d_llp));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;

@@ -323,6 +323,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
   uint32_t* wcnt = out_v + (kHasVals ? kTile : 0);        // [kWarps][kRadix]
   uint32_t* st_ = wcnt + kWarps * kRadix;                 // [kRadix] tile-local digit starts
   uint32_t* glob = st_ + kRadix;                          // [2][kRadix] global digit offsets
+  uint32_t* adj = glob + 2 * kRadix;                      // [kRadix] global minus tile-local start
 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = lanemask_lt();
@@ -349,18 +350,26 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
 
     uint32_t k[kItems];
     uint32_t rank[kItems / 2];
+    uint32_t peers[kItems];
+    const bool full = tn == kTile;
 #pragma unroll
     for (int i = 0; i < kItems; ++i) k[i] = sk[w * 32 * kItems + i * 32 + lane];
+    // all items' peer masks first: their ballots are independent and pipeline
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int32_t lp = w * 32 * kItems + i * 32 + lane;
-      const bool valid = lp < tn;
+      peers[i] = match_digit8((k[i] >> shift) & 255u, full || lp < tn);
+    }
+    // then the per-warp digit counters, item by item (stable order)
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int32_t lp = w * 32 * kItems + i * 32 + lane;
+      const bool valid = full || lp < tn;
       const uint32_t d = (k[i] >> shift) & 255u;
-      const uint32_t peers = match_digit8(d, valid);
       const uint32_t before = valid ? wcnt[w * kRadix + d] : 0u;
       __syncwarp();
-      const uint32_t r = __popc(peers & lt);
-      if (valid && r == 0) wcnt[w * kRadix + d] = before + __popc(peers);
+      const uint32_t r = __popc(peers[i] & lt);
+      if (valid && r == 0) wcnt[w * kRadix + d] = before + __popc(peers[i]);
       __syncwarp();
       const uint32_t rk = before + r;
       if (i & 1)
@@ -381,11 +390,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     }
     const uint32_t start = block_excl_scan(tot, nullptr);
     st_[threadIdx.x] = start;
+    adj[threadIdx.x] = sg[threadIdx.x] - start;  // output slot j of digit d -> adj[d] + j
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int32_t lp = w * 32 * kItems + i * 32 + lane;
-      if (lp < tn) {
+      if (full || lp < tn) {
         const uint32_t d = (k[i] >> shift) & 255u;
         const uint32_t rk = (rank[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
         const uint32_t pos = st_[d] + wcnt[w * kRadix + d] + rk;
@@ -397,8 +407,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) wcnt[i] = 0;  // for the next tile
     for (int j = threadIdx.x; j < tn; j += kBlock) {
       const uint32_t key = out_k[j];
-      const uint32_t d = (key >> shift) & 255u;
-      const uint32_t gp = sg[d] + (uint32_t)j - st_[d];
+      const uint32_t gp = adj[(key >> shift) & 255u] + (uint32_t)j;
       kout[gp] = key;
       if (kHasVals) vout[gp] = out_v[j];
     }
@@ -414,7 +423,7 @@ template <bool kHasVals, bool kIota>
 size_t pipe_smem_bytes() {
   constexpr bool kLoadVals = kHasVals && !kIota;
   return sizeof(uint32_t) * (2 * (kTile + 4) + (kLoadVals ? 2 * (kTile + 4) : 0) + kTile + (kHasVals ? kTile : 0) +
-                             kWarps * kRadix + kRadix + 2 * kRadix);
+                             kWarps * kRadix + kRadix + 2 * kRadix + kRadix);
 }
 
 template <bool kHasVals, bool kIota, class Map>
