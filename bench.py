@@ -168,6 +168,16 @@ def kernel_bytes(name: str, n: int, p, nleaves: int) -> float | None:
     return None
 
 
+def path_bytes(n: int, p) -> float:
+    """Compulsory HBM bytes of one whole step (the lower-bound model of the
+    path): build 128 B/pt (read xyz 24, write key 8 and id 8, one sort pass
+    reading and writing 16 each, permute: read id 8, gather xyz 24, write
+    permuted xyz 24), stage 1 reading the permuted points once (24 B/pt) plus
+    leaf summaries (~2 B/pt) and writing 8 B/window, stage 2 about 32 B/window,
+    stage 3 8 B per grid cell: 154 B/pt + 40 B/window + 8 B/cell."""
+    return 154.0 * n + 40.0 * p.ncells + 8.0 * p.ngrid
+
+
 def measured_traffic(name: str, n: int) -> float | None:
     """DRAM bytes per launch of a kernel from its committed ncu summary
     (profiles/<kernel>_*_dram.md, line 'traffic_bytes_per_point: X'), scaled
@@ -400,6 +410,11 @@ def main():
         cpu = {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{sspec.n} pts, same generator and density ({sspec.x1 - sspec.x0:.0f} m square), "
                          f"W={sW} O={sO} B={sB}, build+OWM once ({t:.2f} s)"}
+    pb = path_bytes(spec.n, p)
+    path_gbs = pb / (ms_max / args.steps / 1e3) / 1e9
+    path_roof = {"model": "compulsory bytes of the whole step: 154 B/pt + 40 B/window + 8 B/cell",
+                 "bytes_per_step": pb, "achieved": round(path_gbs, 1), "peak": peak, "peak_kind": peak_kind,
+                 "unit": "GB/s", "frac": round(path_gbs / peak, 4)}
     if rank == 0:
         tot_k = sum(v[0] for v in ktimes.values()) or 1.0
         line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -420,7 +435,7 @@ def main():
                 "kernels": {k: {"ms": round(v[0] / args.steps, 4), "share": round(v[0] / tot_k, 4),
                                 "launches_per_step": v[1] / args.steps} for k, v in
                             sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
-                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "roofline": roof, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "batched": batched, "served": served,
                 "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)

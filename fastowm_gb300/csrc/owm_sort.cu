@@ -1,9 +1,11 @@
 // Device-wide primitives: exclusive scan and an on-chip-staged LSD radix sort
 // (8-bit digits, reduce-then-scan).
 //
-// Radix pass over a tile of 4096 keys per 256-thread block:
-//   upsweep    digit histogram of the tile (vectorised 16-byte key loads)
-//   scan       exclusive scan of the digit-major [256 x tiles] count table
+// Radix pass over tiles of 4096 keys.  Large sorts split the tiles into one
+// contiguous chunk per persistent block:
+//   upsweep    digit histogram of each chunk (vectorised 16-byte key loads)
+//   scan       exclusive scan of the digit-major [256 x chunks] count table
+//              (small sorts: per tile, [256 x tiles])
 //   downsweep  stable ranking inside the tile with a ballot-based warp
 //              multisplit, keys/values staged in shared memory in digit order,
 //              then written out so that each digit's run is a contiguous,
@@ -23,6 +25,14 @@ constexpr int kItems = 16;
 constexpr int kTile = kBlock * kItems;  // 4096 keys
 constexpr int kWarps = kBlock / 32;
 constexpr int kRadix = 256;
+constexpr int kSubChunks = 4;     // upsweep blocks per downsweep chunk
+constexpr int64_t kMaxChunks = 1024;  // persistent downsweep blocks, at most
+
+// Count-table entries a sort of ntiles tiles may use: per tile (small
+// sorts) or per upsweep part (large sorts).
+int64_t hist_entries(int64_t ntiles) {
+  return std::max<int64_t>(ntiles, kSubChunks * std::min<int64_t>(ntiles, kMaxChunks)) * kRadix;
+}
 
 constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 8;
@@ -166,6 +176,50 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restric
   }
 }
 
+// Tiles [*t0, *t1) of chunk b when ntiles tiles are split into g chunks.
+__device__ __forceinline__ void chunk_tiles(int64_t ntiles, int64_t g, int64_t b, int64_t* t0, int64_t* t1) {
+  const int64_t q = ntiles / g, r = ntiles % g;
+  *t0 = b * q + (b < r ? b : r);
+  *t1 = *t0 + q + (b < r ? 1 : 0);
+}
+
+// Digit histogram of sub-chunk blockIdx.x: part blockIdx.x % kSubChunks of
+// chunk blockIdx.x / kSubChunks (gridDim.x / kSubChunks chunks), into
+// hist[d * gridDim.x + blockIdx.x].  The scanned entry of a chunk's first
+// part is then that chunk's output base.  Keys are 16-byte aligned.
+__global__ void __launch_bounds__(kBlock) k_rs_upsweep_chunk(const uint32_t* __restrict__ keys, int64_t n,
+                                                             int shift, uint32_t* __restrict__ hist,
+                                                             int64_t ntiles) {
+  __shared__ uint32_t h[kWarps][kRadix];
+  for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  int64_t c0, c1, t0, t1;
+  chunk_tiles(ntiles, gridDim.x / kSubChunks, blockIdx.x / kSubChunks, &c0, &c1);
+  chunk_tiles(c1 - c0, kSubChunks, blockIdx.x % kSubChunks, &t0, &t1);
+  t0 += c0;
+  t1 += c0;
+  // an empty part (t0 == t1, possibly past the last key) reads nothing
+  const int64_t b = t0 * kTile < n ? t0 * kTile : n, e = t1 * kTile < n ? t1 * kTile : n;
+  const int64_t e4 = b + ((e - b) & ~(int64_t)3);  // 16-byte loads up to here
+  const uint4* k4 = reinterpret_cast<const uint4*>(keys + b);
+  for (int64_t i = threadIdx.x; i < (e4 - b) / 4; i += kBlock) {
+    const uint4 q = __ldg(k4 + i);
+    atomicAdd(&h[w][(q.x >> shift) & 255u], 1u);
+    atomicAdd(&h[w][(q.y >> shift) & 255u], 1u);
+    atomicAdd(&h[w][(q.z >> shift) & 255u], 1u);
+    atomicAdd(&h[w][(q.w >> shift) & 255u], 1u);
+  }
+  for (int64_t p = e4 + threadIdx.x; p < e; p += kBlock) atomicAdd(&h[w][(__ldg(keys + p) >> shift) & 255u], 1u);
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += kBlock) {
+    uint32_t s = 0;
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) s += h[q][d];
+    hist[(int64_t)d * gridDim.x + blockIdx.x] = s;
+  }
+}
+
 template <bool kHasVals, bool kIota>
 __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __restrict__ kin,
                                                             const uint32_t* __restrict__ vin,
@@ -267,30 +321,16 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-// Tile map of the persistent downsweep: tile t = keys [t*kTile, ...), its
-// digit offsets at hist[d*ntiles + t].
-struct FlatMap {
-  int64_t n, ntiles;
-  __device__ __forceinline__ int64_t count() const { return ntiles; }
-  __device__ __forceinline__ void tile(int64_t t, int64_t* base, int32_t* size, int64_t* ob, int64_t* os) const {
-    *base = t * kTile;
-    *size = (int32_t)(n - *base < kTile ? n - *base : kTile);
-    *ob = t;
-    *os = ntiles;
-  }
-};
-// Copies tile t into shared memory.  Element i of the tile goes to slot
-// i + (base & 3), so global and shared addresses agree modulo 16 bytes and
-// the bulk of the tile moves with 16-byte cp.async whatever the tile's start.
-// Slots outside the tile may receive neighbouring keys; they are never read.
-// Stage buffers hold kTile + 4 slots.
-template <bool kLoadVals, class Map>
-__device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, const Map& m,
-                                         int64_t t, int64_t n, const uint32_t* __restrict__ hist, uint32_t* sk,
-                                         uint32_t* sv, uint32_t* sg) {
-  int64_t base, ob, os;
-  int32_t tn;
-  m.tile(t, &base, &tn, &ob, &os);
+// Copies tile t (keys [t*kTile, ...)) into shared memory.  Element i of the
+// tile goes to slot i + (base & 3), so global and shared addresses agree
+// modulo 16 bytes and the bulk of the tile moves with 16-byte cp.async
+// whatever the tile's start.  Slots outside the tile may receive neighbouring
+// keys; they are never read.  Stage buffers hold kTile + 4 slots.
+template <bool kLoadVals>
+__device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                         int64_t t, int64_t n, uint32_t* sk, uint32_t* sv) {
+  const int64_t base = t * kTile;
+  const int32_t tn = (int32_t)(n - base < kTile ? n - base : kTile);
   const int r = (int)(base & 3);
   const int64_t a0 = base - r;                       // 16-byte aligned
   const int64_t a1 = base + tn;                      // one past the tile
@@ -304,15 +344,23 @@ __device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const
     cp_async4(sk + (g - a0), kin + g);
     if (kLoadVals) cp_async4(sv + (g - a0), vin + g);
   }
-  for (int d = threadIdx.x; d < kRadix; d += kBlock) cp_async4(sg + d, hist + ob + (int64_t)d * os);
 }
 
-template <bool kHasVals, bool kIota, class Map>
+// Persistent downsweep over chunk blockIdx.x of the tiles (the same chunks as
+// k_rs_upsweep_chunk).  The block walks its tiles in order and carries each
+// digit's running output offset in a register (thread d owns digit d): it
+// starts at the scanned chunk count hist[d * gridDim.x + blockIdx.x] and grows
+// by the digit's count in every tile.  While one tile is ranked and
+// scattered, the next two are already being copied into shared memory with
+// cp.async (double buffer); cp.async.wait_group is a hardware wait on this
+// thread's own copies.
+template <bool kHasVals, bool kIota>
 __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t* __restrict__ kin,
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
-                                                                 uint32_t* __restrict__ vout, int shift, Map m,
-                                                                 const uint32_t* __restrict__ hist, int64_t n) {
+                                                                 uint32_t* __restrict__ vout, int shift,
+                                                                 int64_t ntiles, const uint32_t* __restrict__ hist,
+                                                                 int64_t n) {
   constexpr bool kLoadVals = kHasVals && !kIota;
   extern __shared__ __align__(16) uint32_t dsm[];
   constexpr int kStage = kTile + 4;                       // slots per stage (alignment shift)
@@ -322,29 +370,27 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
   uint32_t* out_v = out_k + kTile;                        // [kTile] when kHasVals
   uint32_t* wcnt = out_v + (kHasVals ? kTile : 0);        // [kWarps][kRadix]
   uint32_t* st_ = wcnt + kWarps * kRadix;                 // [kRadix] tile-local digit starts
-  uint32_t* glob = st_ + kRadix;                          // [2][kRadix] global digit offsets
-  uint32_t* adj = glob + 2 * kRadix;                      // [kRadix] global minus tile-local start
+  uint32_t* adj = st_ + kRadix;                           // [kRadix] output offset minus tile-local start
 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = lanemask_lt();
-  const int64_t G = gridDim.x;
-  const int64_t ntiles = m.count();
-  int64_t t = blockIdx.x;
-  if (t < ntiles) rs_issue<kLoadVals>(kin, vin, m, t, n, hist, in_k, in_v, glob);
+  int64_t t0, t1;
+  chunk_tiles(ntiles, gridDim.x, blockIdx.x, &t0, &t1);
+  // kBlock == kRadix; the upsweep ran kSubChunks parts per chunk
+  uint32_t run = hist[(int64_t)threadIdx.x * gridDim.x * kSubChunks + (int64_t)blockIdx.x * kSubChunks];
+  if (t0 < t1) rs_issue<kLoadVals>(kin, vin, t0, n, in_k, in_v);
   cp_async_commit();
-  if (t + G < ntiles) rs_issue<kLoadVals>(kin, vin, m, t + G, n, hist, in_k + kStage, in_v + kStage, glob + kRadix);
+  if (t0 + 1 < t1) rs_issue<kLoadVals>(kin, vin, t0 + 1, n, in_k + kStage, in_v + kStage);
   cp_async_commit();
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) wcnt[i] = 0;
 
-  for (int it = 0; t < ntiles; ++it, t += G) {
-    const int stg = it & 1;
-    int64_t tile_base, ob, os;
-    int32_t tn;
-    m.tile(t, &tile_base, &tn, &ob, &os);
+  for (int64_t t = t0; t < t1; ++t) {
+    const int stg = (int)((t - t0) & 1);
+    const int64_t tile_base = t * kTile;
+    const int32_t tn = (int32_t)(n - tile_base < kTile ? n - tile_base : kTile);
     const int sh = (int)(tile_base & 3);  // alignment shift of this tile's slots
     const uint32_t* sk = in_k + stg * kStage + sh;
     const uint32_t* sv = in_v + stg * kStage + sh;
-    const uint32_t* sg = glob + stg * kRadix;
     cp_async_wait1();  // this thread's copies of tile t have landed
     __syncthreads();   // ... and everybody else's
 
@@ -390,7 +436,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     }
     const uint32_t start = block_excl_scan(tot, nullptr);
     st_[threadIdx.x] = start;
-    adj[threadIdx.x] = sg[threadIdx.x] - start;  // output slot j of digit d -> adj[d] + j
+    adj[threadIdx.x] = run - start;  // output slot j of digit d -> adj[d] + j
+    run += tot;
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
@@ -412,9 +459,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
       if (kHasVals) vout[gp] = out_v[j];
     }
     __syncthreads();  // stage stg and the staging buffers are free again
-    if (t + 2 * G < ntiles)
-      rs_issue<kLoadVals>(kin, vin, m, t + 2 * G, n, hist, in_k + stg * kStage, in_v + stg * kStage,
-                          glob + stg * kRadix);
+    if (t + 2 < t1) rs_issue<kLoadVals>(kin, vin, t + 2, n, in_k + stg * kStage, in_v + stg * kStage);
     cp_async_commit();
   }
 }
@@ -423,26 +468,22 @@ template <bool kHasVals, bool kIota>
 size_t pipe_smem_bytes() {
   constexpr bool kLoadVals = kHasVals && !kIota;
   return sizeof(uint32_t) * (2 * (kTile + 4) + (kLoadVals ? 2 * (kTile + 4) : 0) + kTile + (kHasVals ? kTile : 0) +
-                             kWarps * kRadix + kRadix + 2 * kRadix + kRadix);
+                             kWarps * kRadix + 2 * kRadix);
 }
 
-template <bool kHasVals, bool kIota, class Map>
+template <bool kHasVals, bool kIota>
 cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int shift,
-                        const Map& m, int64_t max_tiles, const uint32_t* hist, int64_t n, cudaStream_t s) {
+                        int64_t ntiles, int64_t chunks, const uint32_t* hist, int64_t n, cudaStream_t s) {
   static bool configured = false;  // per template instance
   const size_t smem = pipe_smem_bytes<kHasVals, kIota>();
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota, Map>,
+    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(max_tiles, (int64_t)sms * 2));
-  OWM_LAUNCH("k_rs_downsweep", s, (k_rs_downsweep_pipe<kHasVals, kIota, Map><<<(unsigned)grid, kBlock, smem, s>>>(
-      kin, vin, kout, vout, shift, m, hist, n)));
+  OWM_LAUNCH("k_rs_downsweep", s, (k_rs_downsweep_pipe<kHasVals, kIota><<<(unsigned)chunks, kBlock, smem, s>>>(
+      kin, vin, kout, vout, shift, ntiles, hist, n)));
   return cudaGetLastError();
 }
 
@@ -455,7 +496,7 @@ size_t scan_temp_bytes(int64_t n) {
 
 size_t radix_sort_temp_bytes(int64_t n) {
   int64_t ntiles = (n + kTile - 1) / kTile;
-  int64_t hn = ntiles * kRadix;
+  int64_t hn = hist_entries(ntiles);
   size_t hbytes = ((size_t)hn * sizeof(uint32_t) + 255) & ~(size_t)255;
   return hbytes + scan_temp_bytes(hn) + 256;
 }
@@ -484,34 +525,45 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   if (temp_bytes < radix_sort_temp_bytes(n) || end_bit <= 0 || end_bit > 32) return cudaErrorInvalidValue;
   const bool has_vals = v0 != nullptr;
   int64_t ntiles = (n + kTile - 1) / kTile;
-  int64_t hn = ntiles * kRadix;
+  int64_t hn = ntiles * kRadix;  // per-tile table of small sorts
   uint32_t* hist = static_cast<uint32_t*>(temp);
-  size_t hbytes = ((size_t)hn * sizeof(uint32_t) + 255) & ~(size_t)255;
+  size_t hbytes = ((size_t)hist_entries(ntiles) * sizeof(uint32_t) + 255) & ~(size_t)255;
   void* stemp = static_cast<char*>(temp) + hbytes;
   size_t sbytes = temp_bytes - hbytes;
   uint32_t *ka = k0, *va = v0, *kb = k1, *vb = v1;
   bool alt = false;
   bool first = true;
+  // large sorts: one contiguous chunk of tiles per persistent block (two per SM)
+  int64_t chunks = 0;
+  if (ntiles >= 64) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    chunks = std::min<int64_t>(std::min<int64_t>(ntiles, (int64_t)sms * 2), kMaxChunks);
+  }
   for (int shift = 0; shift < end_bit; shift += 8) {
-    OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, hist, ntiles));
-    cudaError_t e = exclusive_scan_u32(hist, hist, hn, nullptr, stemp, sbytes, s, launches);
-    if (e != cudaSuccess) return e;
-    if (ntiles >= 64) {  // large sorts: persistent, double-buffered downsweep
+    if (chunks) {
+      OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep_chunk<<<(unsigned)(chunks * kSubChunks), kBlock, 0, s>>>(
+          ka, n, shift, hist, ntiles));
+      cudaError_t e = exclusive_scan_u32(hist, hist, chunks * kSubChunks * kRadix, nullptr, stemp, sbytes, s, launches);
+      if (e != cudaSuccess) return e;
       cudaError_t e2;
-      FlatMap fm{n, ntiles};
       if (has_vals)
-        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, shift, fm, ntiles, hist, n, s)
-                                  : launch_pipe<true, false>(ka, va, kb, vb, shift, fm, ntiles, hist, n, s);
+        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, shift, ntiles, chunks, hist, n, s)
+                                  : launch_pipe<true, false>(ka, va, kb, vb, shift, ntiles, chunks, hist, n, s);
       else
-        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, shift, fm, ntiles, hist, n, s);
+        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, shift, ntiles, chunks, hist, n, s);
       if (e2 != cudaSuccess) return e2;
-    } else if (has_vals) {
-      if (first && iota_vals)
+    } else {  // small sorts: one block per tile, per-tile counts
+      OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, hist, ntiles));
+      cudaError_t e = exclusive_scan_u32(hist, hist, hn, nullptr, stemp, sbytes, s, launches);
+      if (e != cudaSuccess) return e;
+      if (has_vals && first && iota_vals)
         OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
-      else
+      else if (has_vals)
         OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
-    } else {
-      OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles));
+      else
+        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles));
     }
     count_launch(launches, 2);
     first = false;
