@@ -63,6 +63,70 @@ __global__ void k_morton(const double* __restrict__ xyz, int64_t n, double ox, d
   }
 }
 
+// Morton key of one point, integer form (k_morton_int) and FP64 form
+// (k_morton), for the counting variant below.
+struct MortonIntKey {
+  int64_t kx0, ky0, qmax;
+  int shx, shy;
+  __device__ __forceinline__ uint32_t operator()(const double* __restrict__ p) const {
+    int64_t qx = (dkey(__ldg(p)) - kx0) >> shx;
+    int64_t qy = (dkey(__ldg(p + 1)) - ky0) >> shy;
+    qx = qx < 0 ? 0 : (qx > qmax ? qmax : qx);
+    qy = qy < 0 ? 0 : (qy > qmax ? qmax : qy);
+    return (spread_bits16((uint32_t)qx) << 1) | spread_bits16((uint32_t)qy);
+  }
+};
+struct MortonFpKey {
+  double ox, oy, scale;
+  float qmax;
+  __device__ __forceinline__ uint32_t operator()(const double* __restrict__ p) const {
+    float fx = (float)((__ldg(p) - ox) * scale), fy = (float)((__ldg(p + 1) - oy) * scale);
+    fx = fminf(fmaxf(fx, 0.0f), qmax);
+    fy = fminf(fmaxf(fy, 0.0f), qmax);
+    return (spread_bits16((uint32_t)fx) << 1) | spread_bits16((uint32_t)fy);
+  }
+};
+
+// Morton keys of part blockIdx.x of a large sort (sort_part_range), with the
+// part's counts of the sort's first digit (bits 0..7) into
+// counts[d * gridDim.x + blockIdx.x]: the first radix pass then needs no
+// separate read of the keys.
+template <class KeyOf>
+__global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict__ xyz, int64_t n, KeyOf key_of,
+                                                       int64_t ntiles, uint32_t* __restrict__ keys,
+                                                       uint32_t* __restrict__ counts) {
+  __shared__ uint32_t h[8][256];
+  for (int i = threadIdx.x; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
+  __syncthreads();
+  int64_t b, e;
+  sort_part_range(n, ntiles, gridDim.x, blockIdx.x, &b, &e);
+  uint32_t* hw = h[threadIdx.x >> 5];
+  int64_t i = b + threadIdx.x;
+  for (; i + 3 * 256 < e; i += 4 * 256) {  // four points in flight per thread
+    uint32_t k[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) k[u] = key_of(xyz + 3 * (i + u * 256));
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      keys[i + u * 256] = k[u];
+      atomicAdd(hw + (k[u] & 255u), 1u);
+    }
+  }
+  for (; i < e; i += 256) {
+    const uint32_t k = key_of(xyz + 3 * i);
+    keys[i] = k;
+    atomicAdd(hw + (k & 255u), 1u);
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;
+    uint32_t s = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) s += h[w][d];
+    counts[(int64_t)d * gridDim.x + blockIdx.x] = s;
+  }
+}
+
 // One warp per unit of max(L, 32) sorted positions.  L in {1,2,4,...,256}.
 // With kCls, every chunk of 32 gathered points is also folded into the
 // stage-1 window classes (the point is already in registers; this kernel is
@@ -406,15 +470,31 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
 
   int shx = 0, shy = 0;
   int64_t kx0 = 0, ky0 = 0;
+  // large sorts: the Morton pass also counts the first radix digit, in the
+  // sort's count-table layout at the start of its temp
+  const RadixSortPlan plan = radix_sort_plan(n);
+  uint32_t* first_counts = static_cast<uint32_t*>(sort_tmp);
   if (morton_int_shifts(ox, ox + 2.0 * R, bits_axis, &kx0, &shx) &&
       morton_int_shifts(oy, oy + 2.0 * R, bits_axis, &ky0, &shy)) {
-    OWM_LAUNCH("k_morton", s, k_morton_int<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
+    if (plan.parts) {
+      const MortonIntKey kf{kx0, ky0, (1ll << bits_axis) - 1, shx, shy};
+      OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey><<<(unsigned)plan.parts, 256, 0, s>>>(
+          d_xyz, n, kf, plan.ntiles, k0, first_counts));
+    } else {
+      OWM_LAUNCH("k_morton", s, k_morton_int<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
+    }
   } else {
-    OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+    if (plan.parts) {
+      const MortonFpKey kf{ox, oy, scale, (float)((1u << bits_axis) - 1u)};
+      OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey><<<(unsigned)plan.parts, 256, 0, s>>>(
+          d_xyz, n, kf, plan.ntiles, k0, first_counts));
+    } else {
+      OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+    }
   }
   count_launch(launches);
   bool alt = false;
-  OWM_CUDA_TRY(radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches));
+  OWM_CUDA_TRY(radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches, plan.parts > 0));
   const uint32_t* mk = alt ? k1 : k0;
   const uint32_t* perm = alt ? v1 : v0;
 

@@ -140,10 +140,43 @@ size_t scan_temp_bytes(int64_t n);
 // LSD radix sort of uint32 keys (and optional uint32 values) on bits
 // [0, end_bit).  Data ping-pongs between (k0,v0) and (k1,v1); *in_alt tells
 // where the result is.  If iota_vals, the values of the first pass are the
-// positions 0..n-1 (v0 is not read).  Stable.
+// positions 0..n-1 (v0 is not read).  Stable.  With first_counts_given the
+// caller has already written the first pass's digit counts (see
+// RadixSortPlan) at the start of temp.
 cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int64_t n, int end_bit,
                        bool iota_vals, void* temp, size_t temp_bytes, cudaStream_t s, bool* in_alt,
-                       int64_t* launches);
+                       int64_t* launches, bool first_counts_given = false);
+
+// Layout of a large sort's count table, for producers of keys that also count
+// the first pass's digits (bits 0..7) on the fly.  The keys are split into
+// `parts` contiguous ranges (sort_part_range); count[d * parts + p] is the
+// number of keys of part p whose low byte is d, at the start of the sort's
+// temp.  parts == 0: the sort takes its small-sort path (counts not given).
+constexpr int64_t kSortTile = 4096;
+struct RadixSortPlan {
+  int64_t ntiles = 0, parts = 0;
+};
+RadixSortPlan radix_sort_plan(int64_t n);
+
+// Tiles [*t0, *t1) of chunk b when ntiles tiles are split into g chunks.
+__host__ __device__ __forceinline__ void chunk_tiles(int64_t ntiles, int64_t g, int64_t b, int64_t* t0, int64_t* t1) {
+  const int64_t q = ntiles / g, r = ntiles % g;
+  *t0 = b * q + (b < r ? b : r);
+  *t1 = *t0 + q + (b < r ? 1 : 0);
+}
+
+// Keys [*b, *e) of part p of a plan for n keys (4 parts per downsweep chunk;
+// a part may be empty).
+__host__ __device__ __forceinline__ void sort_part_range(int64_t n, int64_t ntiles, int64_t parts, int64_t p,
+                                                         int64_t* b, int64_t* e) {
+  int64_t c0, c1, t0, t1;
+  chunk_tiles(ntiles, parts / 4, p / 4, &c0, &c1);
+  chunk_tiles(c1 - c0, 4, p % 4, &t0, &t1);
+  t0 = (t0 + c0) * kSortTile;
+  t1 = (t1 + c0) * kSortTile;
+  *b = t0 < n ? t0 : n;
+  *e = t1 < n ? t1 : n;
+}
 
 // Exclusive scan of n uint32 (in place allowed); *total (device) gets the sum
 // when non-null.

@@ -23,9 +23,10 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kItems = 16;
 constexpr int kTile = kBlock * kItems;  // 4096 keys
+static_assert(kTile == kSortTile, "the count-table layout is shared with key producers");
 constexpr int kWarps = kBlock / 32;
 constexpr int kRadix = 256;
-constexpr int kSubChunks = 4;     // upsweep blocks per downsweep chunk
+constexpr int kSubChunks = 4;     // upsweep blocks per downsweep chunk (sort_part_range)
 constexpr int64_t kMaxChunks = 1024;  // persistent downsweep blocks, at most
 
 // Count-table entries a sort of ntiles tiles may use: per tile (small
@@ -176,13 +177,6 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restric
   }
 }
 
-// Tiles [*t0, *t1) of chunk b when ntiles tiles are split into g chunks.
-__device__ __forceinline__ void chunk_tiles(int64_t ntiles, int64_t g, int64_t b, int64_t* t0, int64_t* t1) {
-  const int64_t q = ntiles / g, r = ntiles % g;
-  *t0 = b * q + (b < r ? b : r);
-  *t1 = *t0 + q + (b < r ? 1 : 0);
-}
-
 // Digit histogram of sub-chunk blockIdx.x: part blockIdx.x % kSubChunks of
 // chunk blockIdx.x / kSubChunks (gridDim.x / kSubChunks chunks), into
 // hist[d * gridDim.x + blockIdx.x].  The scanned entry of a chunk's first
@@ -194,13 +188,8 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep_chunk(const uint32_t* __r
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) (&h[0][0])[i] = 0;
   __syncthreads();
   const int w = threadIdx.x >> 5;
-  int64_t c0, c1, t0, t1;
-  chunk_tiles(ntiles, gridDim.x / kSubChunks, blockIdx.x / kSubChunks, &c0, &c1);
-  chunk_tiles(c1 - c0, kSubChunks, blockIdx.x % kSubChunks, &t0, &t1);
-  t0 += c0;
-  t1 += c0;
-  // an empty part (t0 == t1, possibly past the last key) reads nothing
-  const int64_t b = t0 * kTile < n ? t0 * kTile : n, e = t1 * kTile < n ? t1 * kTile : n;
+  int64_t b, e;  // an empty part reads nothing
+  sort_part_range(n, ntiles, gridDim.x, blockIdx.x, &b, &e);
   const int64_t e4 = b + ((e - b) & ~(int64_t)3);  // 16-byte loads up to here
   const uint4* k4 = reinterpret_cast<const uint4*>(keys + b);
   for (int64_t i = threadIdx.x; i < (e4 - b) / 4; i += kBlock) {
@@ -494,6 +483,23 @@ size_t scan_temp_bytes(int64_t n) {
   return (size_t)(parts + 64) * sizeof(uint32_t);
 }
 
+namespace {
+int64_t sort_chunks(int64_t ntiles) {
+  if (ntiles < 64) return 0;  // small sorts: one block per tile
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return std::min<int64_t>(std::min<int64_t>(ntiles, (int64_t)sms * 2), kMaxChunks);
+}
+}  // namespace
+
+RadixSortPlan radix_sort_plan(int64_t n) {
+  RadixSortPlan p;
+  p.ntiles = (n + kTile - 1) / kTile;
+  p.parts = sort_chunks(p.ntiles) * kSubChunks;
+  return p;
+}
+
 size_t radix_sort_temp_bytes(int64_t n) {
   int64_t ntiles = (n + kTile - 1) / kTile;
   int64_t hn = hist_entries(ntiles);
@@ -519,7 +525,7 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
 
 cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int64_t n, int end_bit,
                        bool iota_vals, void* temp, size_t temp_bytes, cudaStream_t s, bool* in_alt,
-                       int64_t* launches) {
+                       int64_t* launches, bool first_counts_given) {
   *in_alt = false;
   if (n <= 0) return cudaSuccess;
   if (temp_bytes < radix_sort_temp_bytes(n) || end_bit <= 0 || end_bit > 32) return cudaErrorInvalidValue;
@@ -534,17 +540,13 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   bool alt = false;
   bool first = true;
   // large sorts: one contiguous chunk of tiles per persistent block (two per SM)
-  int64_t chunks = 0;
-  if (ntiles >= 64) {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    chunks = std::min<int64_t>(std::min<int64_t>(ntiles, (int64_t)sms * 2), kMaxChunks);
-  }
+  const int64_t chunks = sort_chunks(ntiles);
+  if (first_counts_given && !chunks) return cudaErrorInvalidValue;
   for (int shift = 0; shift < end_bit; shift += 8) {
     if (chunks) {
-      OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep_chunk<<<(unsigned)(chunks * kSubChunks), kBlock, 0, s>>>(
-          ka, n, shift, hist, ntiles));
+      if (!(first && first_counts_given))
+        OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep_chunk<<<(unsigned)(chunks * kSubChunks), kBlock, 0, s>>>(
+            ka, n, shift, hist, ntiles));
       cudaError_t e = exclusive_scan_u32(hist, hist, chunks * kSubChunks * kRadix, nullptr, stemp, sbytes, s, launches);
       if (e != cudaSuccess) return e;
       cudaError_t e2;
@@ -565,7 +567,7 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
       else
         OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles));
     }
-    count_launch(launches, 2);
+    count_launch(launches, (chunks && first && first_counts_given) ? 1 : 2);
     first = false;
     std::swap(ka, kb);
     std::swap(va, vb);
