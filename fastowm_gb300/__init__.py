@@ -176,6 +176,12 @@ class Cloud(_Child):
     def _destroy(self, h):
         lib().owm_cloud_destroy(h)
 
+    def points(self) -> np.ndarray:
+        """The cloud's points copied to the host, [n, 3] float64."""
+        out = np.empty((self.n, 3), dtype=np.float64)
+        _check(lib().owm_cloud_copy_out(self.handle, _f64p(out), self.n), "cloud_copy_out")
+        return out
+
 
 class Tree(_Child):
     def __init__(self, ctx: "Context", handle: C.c_void_p, cloud: Cloud):
@@ -230,6 +236,30 @@ class Context:
         b = _bbox(bbox) or bbox_of(a)
         _check(lib().owm_cloud_create(self.handle, _f64p(a), a.shape[0], C.byref(b), C.byref(h)), "cloud_create")
         return Cloud(self, h, a.shape[0], b)
+
+    def _parsed_cloud(self, h: C.c_void_p) -> Cloud:
+        b = Bbox()
+        _check(lib().owm_cloud_bbox(h, C.byref(b)), "cloud_bbox")
+        return Cloud(self, h, int(lib().owm_cloud_size(h)), b)
+
+    def cloud_parse_xyz(self, text) -> Cloud:
+        """Parses .xyz text (bytes, or a uint8 array such as a pinned host
+        buffer) on the device into a cloud (owm_cloud_parse_xyz)."""
+        h = C.c_void_p()
+        if isinstance(text, (bytes, bytearray)):
+            buf = bytes(text)
+            _check(lib().owm_cloud_parse_xyz(self.handle, buf, len(buf), C.byref(h)), "cloud_parse_xyz")
+        else:
+            a = np.ascontiguousarray(text, dtype=np.uint8).reshape(-1)
+            _check(lib().owm_cloud_parse_xyz(self.handle, C.cast(a.ctypes.data, C.c_char_p), a.size, C.byref(h)),
+                   "cloud_parse_xyz")
+        return self._parsed_cloud(h)
+
+    def cloud_load_xyz(self, path: str) -> Cloud:
+        """Reads and parses an .xyz file on the device (owm_cloud_load_xyz)."""
+        h = C.c_void_p()
+        _check(lib().owm_cloud_load_xyz(self.handle, str(path).encode(), C.byref(h)), "cloud_load_xyz")
+        return self._parsed_cloud(h)
 
     def tree(self, cloud: Cloud, policy: int = OWM_TREE_MAX_NUMBER, max_number: int = 32, min_radius: float = 0.1,
              level: int = 5) -> Tree:

@@ -94,6 +94,10 @@ SIGNATURES = {
     "owm_cloud_create": (C.c_int, [vp, P(f64), i64, P(Bbox), P(vp)]),
     "owm_cloud_destroy": (C.c_int, [vp]),
     "owm_cloud_size": (i64, [vp]),
+    "owm_cloud_bbox": (C.c_int, [vp, P(Bbox)]),
+    "owm_cloud_copy_out": (C.c_int, [vp, P(f64), i64]),
+    "owm_cloud_parse_xyz": (C.c_int, [vp, C.c_char_p, i64, P(vp)]),
+    "owm_cloud_load_xyz": (C.c_int, [vp, C.c_char_p, P(vp)]),
     "owm_tree_build": (C.c_int, [vp, vp, P(TreeCfg), P(vp)]),
     "owm_tree_get_info": (C.c_int, [vp, vp, P(TreeInfo)]),
     "owm_tree_check": (C.c_int, [vp, vp]),

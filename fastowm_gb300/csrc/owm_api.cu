@@ -15,6 +15,10 @@
 #include <mutex>
 #include <string>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include "owm_ctx.cuh"
 
 namespace owm {
@@ -355,6 +359,133 @@ int owm_cloud_destroy(owm_cloud* cl) {
 }
 
 int64_t owm_cloud_size(const owm_cloud* cl) { return cl ? cl->n : 0; }
+
+int owm_cloud_bbox(const owm_cloud* cl, owm_bbox* out) {
+  if (!cl || !out) return OWM_EINVAL;
+  *out = cl->bbox;
+  return OWM_OK;
+}
+
+int owm_cloud_copy_out(const owm_cloud* cl, double* xyz, int64_t n) {
+  if (!cl || !xyz || n < 0 || n > cl->n) return OWM_EINVAL;
+  if (n == 0) return OWM_OK;
+  OWM_CUDA_TRY(cudaSetDevice(cl->device));
+  OWM_CUDA_TRY(cudaMemcpy(xyz, cl->mem.ptr, (size_t)n * 24, cudaMemcpyDefault));
+  return OWM_OK;
+}
+
+namespace {
+// Wraps parsed device points as a cloud (bbox: the header's, else the data's).
+int finish_parsed_cloud(owm_ctx* c, DeviceBuffer& mem, int64_t n, int64_t declared, const owm_bbox& hb,
+                        owm_cloud** out) {
+  owm_bbox bb = hb;
+  if (declared < 0) {
+    int rc = device_bbox(c, static_cast<const double*>(mem.ptr), n, &bb);
+    if (rc) return rc;
+  }
+  if (!std::isfinite(bb.min_x) || !std::isfinite(bb.max_x) || !std::isfinite(bb.min_y) ||
+      !std::isfinite(bb.max_y) || bb.max_x < bb.min_x || bb.max_y < bb.min_y)
+    return OWM_EIO;
+  owm_cloud* cl = new owm_cloud();
+  cl->ctx = c;
+  cl->device = c->device;
+  cl->n = n;
+  cl->bbox = bb;
+  cl->mem = mem;
+  mem.ptr = nullptr;
+  mem.cap = 0;
+  *out = cl;
+  return OWM_OK;
+}
+}  // namespace
+
+int owm_cloud_parse_xyz(owm_ctx* c, const char* text, int64_t nbytes, owm_cloud** out) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
+  if (!c || !text || !out || nbytes < 0) return OWM_EINVAL;
+  *out = nullptr;
+  if (nbytes == 0) return OWM_EIO;  // like an empty file
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  int64_t data_off = 0, declared = -1;
+  owm_bbox hb{};
+  int rc = xyz_header(text, nbytes, &data_off, &declared, &hb);
+  if (rc) return rc;
+  DeviceBuffer dt, pts;
+  rc = dt.reserve((size_t)((nbytes + 15) & ~(int64_t)15) + 32, c->stream);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(dt.ptr, text, (size_t)nbytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "text copy", __FILE__, __LINE__);
+    dt.release(c->stream);
+    return OWM_ECUDA;
+  }
+  int64_t n = 0;
+  rc = parse_device_text(c, static_cast<const char*>(dt.ptr), nbytes, data_off, declared, &pts, &n, &c->launches);
+  dt.release(c->stream);
+  if (!rc) rc = finish_parsed_cloud(c, pts, n, declared, hb, out);
+  if (rc) pts.release(c->stream);
+  return rc;
+}
+
+int owm_cloud_load_xyz(owm_ctx* c, const char* path, owm_cloud** out) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
+  if (!c || !path || !out) return OWM_EINVAL;
+  *out = nullptr;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  const int fd = ::open(path, O_RDONLY);
+  if (fd < 0) return OWM_EIO;
+  struct stat sb;
+  if (::fstat(fd, &sb) != 0 || sb.st_size <= 0) {
+    ::close(fd);
+    return OWM_EIO;
+  }
+  const int64_t nbytes = (int64_t)sb.st_size;
+  // the file moves through two pinned chunks: reading chunk k + 1 overlaps the
+  // device copy of chunk k
+  constexpr int64_t kChunk = (int64_t)64 << 20;
+  char* pin[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  DeviceBuffer dt, pts;
+  int rc = OWM_OK;
+  int64_t data_off = 0, declared = -1;
+  owm_bbox hb{};
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < 2; ++i) {
+      if (pin[i]) cudaFreeHost(pin[i]);
+      if (done[i]) cudaEventDestroy(done[i]);
+    }
+    dt.release(c->stream);
+    ::close(fd);
+  };
+  for (int i = 0; i < 2 && !rc; ++i) {
+    if (cudaHostAlloc(reinterpret_cast<void**>(&pin[i]), (size_t)kChunk, cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) != cudaSuccess)
+      rc = OWM_ENOMEM;
+  }
+  if (!rc) rc = dt.reserve((size_t)((nbytes + 15) & ~(int64_t)15) + 32, c->stream);
+  for (int64_t off = 0, k = 0; !rc && off < nbytes; off += kChunk, ++k) {
+    const int b = (int)(k & 1);
+    if (k >= 2 && cudaEventSynchronize(done[b]) != cudaSuccess) rc = OWM_ECUDA;
+    const int64_t len = std::min<int64_t>(kChunk, nbytes - off);
+    for (int64_t got = 0; !rc && got < len;) {
+      const ssize_t r = ::pread(fd, pin[b] + got, (size_t)(len - got), (off_t)(off + got));
+      if (r <= 0) rc = OWM_EIO;
+      got += r > 0 ? r : 0;
+    }
+    if (!rc && k == 0) rc = xyz_header(pin[0], len, &data_off, &declared, &hb);  // the header lies in the first chunk
+    if (!rc && (cudaMemcpyAsync(static_cast<char*>(dt.ptr) + off, pin[b], (size_t)len, cudaMemcpyHostToDevice,
+                                c->stream) != cudaSuccess ||
+                cudaEventRecord(done[b], c->stream) != cudaSuccess))
+      rc = OWM_ECUDA;
+  }
+  int64_t n = 0;
+  if (!rc)
+    rc = parse_device_text(c, static_cast<const char*>(dt.ptr), nbytes, data_off, declared, &pts, &n, &c->launches);
+  cleanup();
+  if (!rc) rc = finish_parsed_cloud(c, pts, n, declared, hb, out);
+  if (rc) pts.release(c->stream);
+  return rc;
+}
 
 int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm_tree** out) {
   ProfScope prof_scope(c ? c->active_prof() : nullptr);

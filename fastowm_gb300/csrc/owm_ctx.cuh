@@ -24,6 +24,12 @@ constexpr int kS3Slot = 4;
 constexpr int kBboxSlot = 8;  // 4 x int64 (8-byte aligned)
 
 bool is_device_ptr(const void* p);
+// Device ingest of .xyz text (owm_ingest.cu): the header of host text, and
+// the parse of device text (16-byte aligned, 16 readable bytes of slack) into
+// a point buffer of *n_out points.
+int xyz_header(const char* text, int64_t nbytes, int64_t* data_off, int64_t* declared, owm_bbox* hb);
+int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t data_off, int64_t declared,
+                      DeviceBuffer* out_mem, int64_t* n_out, int64_t* launches);
 int64_t total_launches();
 int tree_alloc(TreeStore* t, DeviceBuffer* mem, int64_t n, const owm_tree_cfg& cfg, cudaStream_t s);
 int validate_tree_cfg(const owm_tree_cfg* cfg);

@@ -111,12 +111,18 @@ void owm_host_free(void* p) { std::free(p); }
 
 // readXYZfile (optim3_func.cpp:665-722), header variant: "N minx maxx miny
 // maxy" then "x y z ..." lines.  Without a header the bbox is the data's.
+// A line is the text up to its newline, however long (getline).
 int owm_xyz_read(const char* path, double** xyz_out, int64_t* n_out, owm_bbox* bbox) {
   if (!path || !xyz_out || !n_out || !bbox) return OWM_EINVAL;
   FILE* f = std::fopen(path, "r");
   if (!f) return OWM_EIO;
-  std::vector<char> line(1 << 16);
-  auto next_line = [&](void) -> bool { return std::fgets(line.data(), (int)line.size(), f) != nullptr; };
+  struct LineBuf {
+    char* p = nullptr;
+    size_t cap = 0;
+    ~LineBuf() { std::free(p); }
+    char* data() { return p; }
+  } line;
+  auto next_line = [&](void) -> bool { return ::getline(&line.p, &line.cap, f) >= 0; };
   // Decide header vs no header from the first non-empty line.
   if (!next_line()) {
     std::fclose(f);

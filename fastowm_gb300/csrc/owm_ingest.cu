@@ -1,0 +1,775 @@
+// Cloud ingest on the device: the text of an .xyz file, parsed by GPU threads
+// into a device cloud.  The file format and its rules are those of
+// readXYZfile (CPP-TBB-CPU/src/optim3_func.cpp:665-722) as owm_xyz_read
+// restates it line by line: an optional header (the point count, then
+// min x, max x, min y, max y, one value per line), then one "x y z ..." line
+// per point read with sscanf("%lf %lf %lf"); blank lines are skipped, any
+// other line with fewer than three numbers is an error, non-finite values
+// are rejected, and with a header the points after the declared count are
+// not read.  map_file_atof_tbb_th (SYCL-CUDA-GPU/basic/utils.h:338-395) is
+// the reference's fixed-column form of the same loader.
+//
+// Pipeline (text resident on the device, 16 bytes of readable slack):
+//   k_nl_count   newlines per 64 KB tile
+//   scan         tile offsets
+//   k_nl_starts  line start positions (one thread per 256 bytes, block scan)
+//   k_parse      one thread per line: the sscanf grammar on 16-byte loads,
+//                values by Clinger's exact fast path (significand <= 2^53,
+//                |decimal exponent| <= 22: one correctly rounded IEEE
+//                multiply or divide), hex floats by exact rounding; a line
+//                with any other decimal field is queued
+//   k_parse_slow the queued lines again, every decimal field correctly
+//                rounded by big-integer comparison with the halfway points
+//                of the candidate doubles (a candidate from a table of
+//                correctly rounded powers of ten, moved one double at a time)
+//   resolve      first error line, points before it, compaction of blank
+//                lines (skipped when there are none)
+// The values equal what the C library's correctly rounded conversion gives
+// for the same text, bit for bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "owm_ctx.cuh"
+
+namespace owm {
+
+namespace {
+
+constexpr int kLinePoint = 0, kLineBlank = 1, kLineError = 2, kLineSlow = 3;
+constexpr int64_t kTileBytes = 65536;  // newline-count tile: 256 threads x 256 bytes
+constexpr int kPowMin = -300, kPowMax = 300;
+
+__constant__ double c_pow10[kPowMax - kPowMin + 1];  // correctly rounded 10^k, k = -300..300
+
+// ---- text access ---------------------------------------------------------------
+// Byte p of the line being parsed, through one cached 16-byte word; 0 past
+// the line's end (a NUL byte also ends what sscanf sees).
+struct TextCursor {
+  const uint4* __restrict__ base;
+  int64_t end;
+  int64_t wi;
+  uint4 w;
+  __device__ __forceinline__ TextCursor(const char* text, int64_t e) : base(reinterpret_cast<const uint4*>(text)), end(e), wi(-1) {}
+  __device__ __forceinline__ uint32_t at(int64_t p) {
+    if (p >= end) return 0;
+    const int64_t i = p >> 4;
+    if (i != wi) {
+      w = __ldg(base + i);
+      wi = i;
+    }
+    const uint32_t q = (uint32_t)(p >> 2) & 3u;
+    const uint32_t word = q == 0 ? w.x : q == 1 ? w.y : q == 2 ? w.z : w.w;
+    return (word >> ((uint32_t)(p & 3) * 8u)) & 0xFFu;
+  }
+};
+
+__device__ __forceinline__ bool is_space(uint32_t c) { return c == ' ' || (c >= 9 && c <= 13); }
+__device__ __forceinline__ bool is_digit(uint32_t c) { return c - '0' < 10u; }
+__device__ __forceinline__ int hex_val(uint32_t c) {
+  if (c - '0' < 10u) return (int)(c - '0');
+  const uint32_t l = c | 0x20u;
+  if (l - 'a' < 6u) return (int)(l - 'a') + 10;
+  return -1;
+}
+
+// ---- exact rounding of m * 2^e2 (+ sticky: the value is a little above) -----
+__device__ double round_bits(uint64_t m, bool sticky, int64_t e2, bool neg) {
+  const uint64_t sign = neg ? 0x8000000000000000ull : 0ull;
+  if (m == 0) return __longlong_as_double((long long)sign);
+  const int bl = 64 - __clzll((long long)m);
+  const int64_t E = e2 + bl - 1;  // the value lies in [2^E, 2^(E+1))
+  if (E > 1023) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+  const int64_t prec = E >= -1022 ? 53 : E + 1075;  // significant bits kept
+  if (prec <= 0) {
+    // below 2^-1074: 0, or the smallest subnormal when above half of it
+    const bool up = prec == 0 && (sticky || (m & (m - 1)) != 0);
+    return __longlong_as_double((long long)(sign | (up ? 1ull : 0ull)));
+  }
+  const int shift = bl - (int)prec;
+  uint64_t mant;
+  if (shift <= 0) {
+    mant = m << (-shift);
+  } else {
+    mant = m >> shift;
+    const uint64_t rem = m & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+    if (rem > half || (rem == half && (sticky || (mant & 1)))) ++mant;
+  }
+  uint64_t bits;
+  if (E >= -1022)
+    bits = ((uint64_t)(E + 1022) << 52) + mant;  // a carry to 2^53 moves into the exponent (inf past 1023)
+  else
+    bits = mant;  // subnormal: mant counts units of 2^-1074 (2^52 = smallest normal)
+  return __longlong_as_double((long long)(sign | bits));
+}
+
+// ---- big integers for the exact decimal path ----------------------------------
+constexpr int kBigWords = 160;    // 5120 bits: decimal significands of up to 800 digits, scaled
+constexpr int kMaxBigDigits = 800;
+
+struct Big {
+  uint32_t w[kBigWords];
+  int n;
+  __device__ void set_u64(uint64_t v) {
+    w[0] = (uint32_t)v;
+    w[1] = (uint32_t)(v >> 32);
+    n = w[1] ? 2 : (w[0] ? 1 : 0);
+  }
+  __device__ void mul_add(uint32_t m, uint32_t a) {
+    uint64_t carry = a;
+    for (int i = 0; i < n; ++i) {
+      const uint64_t t = (uint64_t)w[i] * m + carry;
+      w[i] = (uint32_t)t;
+      carry = t >> 32;
+    }
+    if (carry && n < kBigWords) w[n++] = (uint32_t)carry;
+  }
+  __device__ void mul_pow5(int64_t e) {
+    while (e >= 13) {
+      mul_add(1220703125u, 0);  // 5^13
+      e -= 13;
+    }
+    uint32_t p = 1;
+    while (e-- > 0) p *= 5u;
+    if (p != 1) mul_add(p, 0);
+  }
+  __device__ void shl(int64_t bits) {
+    if (n == 0 || bits <= 0) return;
+    const int ws = (int)(bits >> 5), bs = (int)(bits & 31);
+    int nn = n + ws + 1;
+    if (nn > kBigWords) nn = kBigWords;  // sized so this never truncates (see the bounds in exact_decimal)
+    for (int i = nn - 1; i >= 0; --i) {
+      const int s = i - ws;
+      uint32_t v = 0;
+      if (s >= 0 && s < n) v = w[s] << bs;
+      if (bs && s - 1 >= 0 && s - 1 < n) v |= w[s - 1] >> (32 - bs);
+      w[i] = v;
+    }
+    n = nn;
+    while (n > 0 && w[n - 1] == 0) --n;
+  }
+};
+
+__device__ int big_cmp(const Big& a, const Big& b) {
+  if (a.n != b.n) return a.n < b.n ? -1 : 1;
+  for (int i = a.n - 1; i >= 0; --i)
+    if (a.w[i] != b.w[i]) return a.w[i] < b.w[i] ? -1 : 1;
+  return 0;
+}
+
+// Sign of D * 10^E - (2m + 1) * 2^(q - 1), D with `sticky` nonzero digits
+// beyond it: the value against the halfway point above the double m * 2^q.
+__device__ int cmp_halfway(const Big& D, int64_t E, bool sticky, uint64_t m, int64_t q, Big& L, Big& R) {
+  L = D;
+  R.set_u64(2 * m + 1);
+  if (E >= 0)
+    L.mul_pow5(E);
+  else
+    R.mul_pow5(-E);
+  const int64_t e2 = E - (q - 1);
+  if (e2 >= 0)
+    L.shl(e2);
+  else
+    R.shl(-e2);
+  int c = big_cmp(L, R);
+  if (c == 0 && sticky) c = 1;
+  return c;
+}
+
+__device__ __forceinline__ void split_double(uint64_t bits, uint64_t* m, int64_t* q) {
+  const uint64_t ef = bits >> 52, fr = bits & 0xFFFFFFFFFFFFFull;
+  if (ef == 0) {
+    *m = fr;
+    *q = -1074;
+  } else {
+    *m = fr | 0x10000000000000ull;
+    *q = (int64_t)ef - 1075;
+  }
+}
+
+// ---- field grammar -------------------------------------------------------------
+constexpr int kFieldOk = 0, kFieldFail = 1, kFieldNonFinite = 2, kFieldSlow = 3;
+
+struct Decimal {
+  uint64_t w;     // first (up to) 19 significant digits
+  int64_t nd;     // significant digits in all
+  int64_t dexp;   // value = (w + fraction of the dropped digits) * 10^dexp
+  bool sticky;    // a dropped digit is nonzero
+};
+
+// Exact decimal conversion of the mantissa at [ms, me) (digits and at most
+// one '.') times 10^ev; `dec` is its 19-digit summary.
+__device__ double exact_decimal(TextCursor& tc, int64_t ms, int64_t me, int64_t ev, const Decimal& dec, bool neg,
+                                Big* big) {
+  const uint64_t sign = neg ? 0x8000000000000000ull : 0ull;
+  const int64_t lead = (dec.nd < 19 ? dec.nd : 19) - 1 + dec.dexp;  // value in [10^lead, 10^(lead+1))
+  if (lead >= 309) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+  if (lead <= -325) return __longlong_as_double((long long)sign);
+  // D: the first kMaxBigDigits significant digits; E: its decimal exponent
+  Big& D = big[0];
+  D.n = 0;
+  int64_t nd = 0, E = 0;
+  bool seen_dot = false, sticky = false;
+  uint32_t chunk = 0, cmul = 1;
+  for (int64_t p = ms; p < me; ++p) {
+    const uint32_t c = tc.at(p);
+    if (c == '.') {
+      seen_dot = true;
+      continue;
+    }
+    const uint32_t d = c - '0';
+    if (nd == 0 && d == 0) {
+      if (seen_dot) --E;
+      continue;
+    }
+    if (nd < kMaxBigDigits) {
+      chunk = chunk * 10u + d;
+      cmul *= 10u;
+      if (cmul == 1000000000u) {
+        D.mul_add(cmul, chunk);
+        chunk = 0;
+        cmul = 1;
+      }
+      ++nd;
+      if (seen_dot) --E;
+    } else {
+      if (d) sticky = true;
+      if (!seen_dot) ++E;
+    }
+  }
+  if (cmul != 1) D.mul_add(cmul, chunk);
+  E += ev;
+  // candidate: w * 10^dexp in two correctly rounded steps (within a few units
+  // in the last place, subnormal and overflowing results included)
+  const int64_t a = dec.dexp < kPowMin ? kPowMin : (dec.dexp > kPowMax ? kPowMax : dec.dexp);
+  const int64_t b = dec.dexp - a;  // |b| <= 50 by the lead bounds above
+  double cand = __dmul_rn(__dmul_rn((double)dec.w, c_pow10[a - kPowMin]), c_pow10[b - kPowMin]);
+  uint64_t bits = (uint64_t)__double_as_longlong(cand);
+  if (bits == 0) bits = 1;                                   // start from the smallest subnormal
+  if (bits >= 0x7FF0000000000000ull) bits = 0x7FEFFFFFFFFFFFFFull;  // ... or the largest finite double
+  Big& L = big[1];
+  Big& R = big[2];
+  for (int it = 0; it < 64; ++it) {
+    uint64_t m;
+    int64_t q;
+    split_double(bits, &m, &q);
+    const int up = cmp_halfway(D, E, sticky, m, q, L, R);
+    if (up > 0 || (up == 0 && (m & 1))) {
+      if (bits == 0x7FEFFFFFFFFFFFFFull) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+      ++bits;
+      continue;
+    }
+    uint64_t pm;
+    int64_t pq;
+    split_double(bits - 1, &pm, &pq);  // bits - 1 == 0: the halfway point 2^-1075 below the smallest subnormal
+    const int down = cmp_halfway(D, E, sticky, pm, pq, L, R);
+    if (down < 0 || (down == 0 && !(pm & 1))) {
+      if (bits == 1) return __longlong_as_double((long long)sign);
+      --bits;
+      continue;
+    }
+    return __longlong_as_double((long long)(sign | bits));
+  }
+  return __longlong_as_double((long long)(sign | 0x7FF8000000000000ull));  // unreachable: a NaN fails the load
+}
+
+// One sscanf %lf conversion at p (whitespace already skipped).  On success
+// *v and *end are set.  kExact: decimal fields that need the slow path are
+// converted here (big = 3 scratch integers); otherwise they report
+// kFieldSlow.
+template <bool kExact>
+__device__ int parse_field(TextCursor& tc, int64_t p, double* v, int64_t* end, Big* big) {
+  bool neg = false;
+  uint32_t c = tc.at(p);
+  if (c == '+' || c == '-') {
+    neg = c == '-';
+    c = tc.at(++p);
+  }
+  const uint32_t lc = c | 0x20u;
+  if (lc == 'i' || lc == 'n') return kFieldNonFinite;  // inf/nan (or a failed match): the load fails either way
+  if (c == '0' && (tc.at(p + 1) | 0x20u) == 'x') {
+    // hex: [hex digits][. [hex digits]], then p[+-][digits]; fails only when
+    // nothing follows "0x"
+    p += 2;
+    uint64_t m = 0;
+    int hd = 0;
+    int64_t bexp = 0;
+    bool sticky = false, seen_dot = false, consumed = false;
+    for (;;) {
+      c = tc.at(p);
+      const int hv = hex_val(c);
+      if (hv >= 0) {
+        consumed = true;
+        if (hd == 0 && hv == 0) {
+          if (seen_dot) bexp -= 4;
+        } else if (hd < 16) {
+          m = m * 16u + (uint64_t)hv;
+          ++hd;
+          if (seen_dot) bexp -= 4;
+        } else {
+          ++hd;
+          if (hv) sticky = true;
+          if (!seen_dot) bexp += 4;
+        }
+        ++p;
+      } else if (c == '.' && !seen_dot) {
+        seen_dot = consumed = true;
+        ++p;
+      } else {
+        break;
+      }
+    }
+    if (!consumed) return kFieldFail;
+    if ((tc.at(p) | 0x20u) == 'p') {
+      c = tc.at(++p);
+      bool eneg = false;
+      if (c == '+' || c == '-') {
+        eneg = c == '-';
+        ++p;
+      }
+      int64_t ev = 0;
+      while (is_digit(c = tc.at(p))) {
+        if (ev < 100000000) ev = ev * 10 + (c - '0');
+        ++p;
+      }
+      bexp += eneg ? -ev : ev;
+    }
+    *v = round_bits(m, sticky, bexp, neg);
+    *end = p;
+    return isfinite(*v) ? kFieldOk : kFieldNonFinite;
+  }
+  // decimal: [digits][. [digits]] with at least one digit, then e[+-][digits]
+  const int64_t ms = p;
+  Decimal dec{0, 0, 0, false};
+  bool any = false, seen_dot = false;
+  for (;;) {
+    c = tc.at(p);
+    if (is_digit(c)) {
+      any = true;
+      const uint32_t d = c - '0';
+      if (dec.nd == 0 && d == 0) {
+        if (seen_dot) --dec.dexp;
+      } else if (dec.nd < 19) {
+        dec.w = dec.w * 10u + d;
+        ++dec.nd;
+        if (seen_dot) --dec.dexp;
+      } else {
+        ++dec.nd;
+        if (d) dec.sticky = true;
+        if (!seen_dot) ++dec.dexp;
+      }
+      ++p;
+    } else if (c == '.' && !seen_dot) {
+      seen_dot = true;
+      ++p;
+    } else {
+      break;
+    }
+  }
+  if (!any) return kFieldFail;
+  const int64_t me = p;
+  int64_t ev = 0;
+  if ((tc.at(p) | 0x20u) == 'e') {
+    c = tc.at(++p);
+    bool eneg = false;
+    if (c == '+' || c == '-') {
+      eneg = c == '-';
+      ++p;
+    }
+    while (is_digit(c = tc.at(p))) {
+      if (ev < 100000000) ev = ev * 10 + (c - '0');
+      ++p;
+    }
+    if (eneg) ev = -ev;
+  }
+  *end = p;
+  dec.dexp += ev;
+  if (dec.w == 0) {  // every digit is zero
+    *v = neg ? -0.0 : 0.0;
+    return kFieldOk;
+  }
+  if (!dec.sticky && dec.w <= (1ull << 53)) {
+    int64_t e = dec.dexp;
+    uint64_t w = dec.w;
+    while (e > 22 && w <= (1ull << 53) / 10) {  // move powers of ten into an exact significand
+      w *= 10;
+      --e;
+    }
+    if (e >= -22 && e <= 22) {
+      const double x = (double)w;  // exact: w <= 2^53
+      const double r = e >= 0 ? __dmul_rn(x, c_pow10[e - kPowMin]) : __ddiv_rn(x, c_pow10[-e - kPowMin]);
+      *v = neg ? -r : r;
+      return isfinite(r) ? kFieldOk : kFieldNonFinite;
+    }
+  }
+  if (!kExact) return kFieldSlow;
+  *v = exact_decimal(tc, ms, me, ev, dec, neg, big);
+  return isfinite(*v) ? kFieldOk : kFieldNonFinite;
+}
+
+// sscanf(line, "%lf %lf %lf") and owm_xyz_read's verdict on the line.
+template <bool kExact>
+__device__ int parse_line(const char* text, int64_t s, int64_t e, double* out, Big* big) {
+  TextCursor tc(text, e);
+  int64_t p = s;
+  int f = 0;
+  for (; f < 3; ++f) {
+    uint32_t c;
+    while ((c = tc.at(p)) != 0 && is_space(c)) ++p;
+    if (c == 0) break;
+    int64_t end;
+    const int r = parse_field<kExact>(tc, p, out + f, &end, big);
+    if (r == kFieldSlow) return kLineSlow;
+    if (r == kFieldNonFinite) return kLineError;
+    if (r == kFieldFail) break;
+    p = end;
+  }
+  if (f == 3) return kLinePoint;
+  // blank lines (spaces, tabs, CR only, up to a NUL) are skipped
+  for (p = s;; ++p) {
+    const uint32_t c = tc.at(p);
+    if (c == 0) return kLineBlank;
+    if (c != ' ' && c != '\t' && c != '\r' && c != '\n') return kLineError;
+  }
+}
+
+// ---- kernels -------------------------------------------------------------------
+__device__ __forceinline__ uint32_t count_nl_word(uint32_t x) {
+  return (uint32_t)__popc(__vcmpeq4(x, 0x0A0A0A0Au)) >> 3;  // one 0xFF byte per match
+}
+
+// Newlines of tile blockIdx.x ([begin + t*kTileBytes, ...) within [begin, end)):
+// per thread 256 bytes, 16 at a time.  begin is 16-byte aligned.
+__global__ void __launch_bounds__(256) k_nl_count(const char* __restrict__ text, int64_t begin, int64_t end,
+                                                  uint32_t* __restrict__ tile_count) {
+  const int64_t b = begin + (int64_t)blockIdx.x * kTileBytes + (int64_t)threadIdx.x * 256;
+  uint32_t cnt = 0;
+  for (int k = 0; k < 16; ++k) {
+    const int64_t o = b + k * 16;
+    if (o >= end) break;
+    const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
+    if (o + 16 <= end) {
+      cnt += count_nl_word(w.x) + count_nl_word(w.y) + count_nl_word(w.z) + count_nl_word(w.w);
+    } else {
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+      for (int j = 0; j < 16 && o + j < end; ++j) cnt += ((ws[j >> 2] >> ((j & 3) * 8)) & 0xFFu) == '\n';
+    }
+  }
+  for (int o = 16; o >= 1; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  __shared__ uint32_t ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < 8; ++i) t += ws[i];
+    tile_count[blockIdx.x] = t;
+  }
+}
+
+// starts[k + 1] = position after the k-th newline of [begin, end) (k from 0),
+// in order; tile_off = scanned tile counts.
+__global__ void __launch_bounds__(256) k_nl_starts(const char* __restrict__ text, int64_t begin, int64_t end,
+                                                   const uint32_t* __restrict__ tile_off,
+                                                   int64_t* __restrict__ starts) {
+  const int64_t b = begin + (int64_t)blockIdx.x * kTileBytes + (int64_t)threadIdx.x * 256;
+  uint32_t cnt = 0;
+  for (int k = 0; k < 16; ++k) {
+    const int64_t o = b + k * 16;
+    if (o >= end) break;
+    const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
+    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+    for (int j = 0; j < 16 && o + j < end; ++j) cnt += ((ws[j >> 2] >> ((j & 3) * 8)) & 0xFFu) == '\n';
+  }
+  // exclusive scan of the per-thread counts over the block
+  __shared__ uint32_t wsum[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (int i = 0; i < wid; ++i) wbase += wsum[i];
+  int64_t k = (int64_t)tile_off[blockIdx.x] + wbase + inc - cnt;
+  for (int kk = 0; kk < 16; ++kk) {
+    const int64_t o = b + kk * 16;
+    if (o >= end) break;
+    const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
+    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+    for (int j = 0; j < 16 && o + j < end; ++j)
+      if (((ws[j >> 2] >> ((j & 3) * 8)) & 0xFFu) == '\n') starts[++k] = o + j + 1;
+  }
+}
+
+struct ParseOut {
+  double* vals;             // [nlines][3]
+  uint8_t* status;          // [nlines]
+  int64_t* slow;            // queued line indices
+  unsigned long long* nslow;
+};
+
+// One thread per line i: [starts[i], starts[i+1] - 1) (the newline excluded).
+__global__ void __launch_bounds__(256) k_parse(const char* __restrict__ text, const int64_t* __restrict__ starts,
+                                               int64_t nlines, ParseOut o) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlines;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v[3];
+    const int st = parse_line<false>(text, starts[i], starts[i + 1] - 1, v, nullptr);
+    o.status[i] = (uint8_t)st;
+    if (st == kLinePoint) {
+      o.vals[3 * i] = v[0];
+      o.vals[3 * i + 1] = v[1];
+      o.vals[3 * i + 2] = v[2];
+    } else if (st == kLineSlow) {
+      o.slow[atomicAdd(o.nslow, 1ull)] = i;
+    }
+  }
+}
+
+// The queued lines, every field correctly rounded (three big integers of
+// scratch per thread, in local memory: this kernel alone carries them).
+__global__ void __launch_bounds__(128) k_parse_slow(const char* __restrict__ text,
+                                                    const int64_t* __restrict__ starts, ParseOut o) {
+  Big big[3];
+  const int64_t ns = (int64_t)*o.nslow;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = o.slow[k];
+    double v[3];
+    const int st = parse_line<true>(text, starts[i], starts[i + 1] - 1, v, big);
+    o.status[i] = (uint8_t)st;
+    if (st == kLinePoint) {
+      o.vals[3 * i] = v[0];
+      o.vals[3 * i + 1] = v[1];
+      o.vals[3 * i + 2] = v[2];
+    }
+  }
+}
+
+// First error line (atomic min) and point flags.
+__global__ void k_line_flags(const uint8_t* __restrict__ status, int64_t nlines, uint32_t* __restrict__ is_point,
+                             unsigned long long* __restrict__ first_error) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlines;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int st = status[i];
+    is_point[i] = st == kLinePoint;
+    if (st == kLineError || st == kLineSlow) atomicMin(first_error, (unsigned long long)i);
+  }
+}
+
+// Points [0, n) of the flagged lines, in line order, into out (AoS).
+__global__ void k_compact_points(const double* __restrict__ vals, const uint32_t* __restrict__ is_point,
+                                 const uint32_t* __restrict__ pos, int64_t nlines, int64_t n, double* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlines;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (!is_point[i] || pos[i] >= (uint64_t)n) continue;
+    const int64_t j = pos[i];
+    out[3 * j] = vals[3 * i];
+    out[3 * j + 1] = vals[3 * i + 1];
+    out[3 * j + 2] = vals[3 * i + 2];
+  }
+}
+
+int grid_of(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
+}
+
+size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Powers of ten for the device, once per device: the C library's correctly
+// rounded conversion of "1e<k>".
+std::mutex g_pow_mu;
+std::vector<int> g_pow_ready;
+
+int ensure_pow10(int device) {
+  std::lock_guard<std::mutex> lk(g_pow_mu);
+  if ((int)g_pow_ready.size() <= device) g_pow_ready.resize(device + 1, 0);
+  if (g_pow_ready[device]) return OWM_OK;
+  double tab[kPowMax - kPowMin + 1];
+  char buf[16];
+  for (int k = kPowMin; k <= kPowMax; ++k) {
+    std::snprintf(buf, sizeof(buf), "1e%d", k);
+    tab[k - kPowMin] = std::strtod(buf, nullptr);
+  }
+  OWM_CUDA_TRY(cudaMemcpyToSymbol(c_pow10, tab, sizeof(tab)));
+  g_pow_ready[device] = 1;
+  return OWM_OK;
+}
+
+// First line [s, e) of host text at or after `from` (e excludes '\n');
+// false at the end of the text.
+bool host_line(const char* text, int64_t nbytes, int64_t from, int64_t* s, int64_t* e) {
+  if (from >= nbytes) return false;
+  const void* nl = std::memchr(text + from, '\n', (size_t)(nbytes - from));
+  *s = from;
+  *e = nl ? (const char*)nl - text : nbytes;
+  return true;
+}
+
+}  // namespace
+
+// Header of owm_xyz_read on host text: *data_off = first data byte,
+// *declared = -1 without a header.  Same sscanf calls as the host loader.
+int xyz_header(const char* text, int64_t nbytes, int64_t* data_off, int64_t* declared, owm_bbox* hb) {
+  int64_t s, e;
+  if (!host_line(text, nbytes, 0, &s, &e)) return OWM_EIO;
+  std::vector<char> line((size_t)(e - s) + 2);
+  auto load = [&](int64_t a, int64_t b) {
+    line.assign((size_t)(b - a) + 2, 0);
+    std::memcpy(line.data(), text + a, (size_t)(b - a));
+    line[(size_t)(b - a)] = '\n';
+  };
+  load(s, e);
+  double a[3];
+  const int k = std::sscanf(line.data(), "%lf %lf %lf", &a[0], &a[1], &a[2]);
+  if (k == 3) {
+    *data_off = 0;
+    *declared = -1;
+    return OWM_OK;
+  }
+  if (k != 1) return OWM_EIO;
+  if (!(a[0] >= 1.0 && a[0] < 9.2e18)) return OWM_EIO;
+  *declared = (int64_t)a[0];
+  double v[4];
+  int64_t from = e + 1;
+  for (int i = 0; i < 4; ++i) {
+    if (!host_line(text, nbytes, from, &s, &e)) return OWM_EIO;
+    load(s, e);
+    if (std::sscanf(line.data(), "%lf", &v[i]) != 1) return OWM_EIO;
+    from = e + 1;
+  }
+  hb->min_x = v[0];
+  hb->max_x = v[1];
+  hb->min_y = v[2];
+  hb->max_y = v[3];
+  *data_off = from < nbytes ? from : nbytes;
+  return OWM_OK;
+}
+
+// Parses device text [0, nbytes) (16 bytes of slack after it, 16-byte
+// aligned) whose data lines start at data_off, into the cloud's buffer.
+int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t data_off, int64_t declared,
+                      DeviceBuffer* out_mem, int64_t* n_out, int64_t* launches) {
+  cudaStream_t s = c->stream;
+  int rc = ensure_pow10(c->device);
+  if (rc) return rc;
+  // tiles start at a 16-byte boundary below data_off; bytes before it are not counted
+  const int64_t begin = data_off & ~(int64_t)15;
+  const int64_t span = nbytes - begin;
+  const int64_t ntiles = std::max<int64_t>(1, (span + kTileBytes - 1) / kTileBytes);
+  // newline positions in [begin, data_off) must not count: the count runs from data_off
+  // itself, so tiles use the exact byte range [data_off, nbytes)
+  DeviceBuffer tmp;
+  const size_t tb = a256((size_t)ntiles * 4) * 2 + a256(scan_temp_bytes(ntiles)) + 256;
+  rc = tmp.reserve(tb, s);
+  if (rc) return rc;
+  char* tp = static_cast<char*>(tmp.ptr);
+  uint32_t* tcount = reinterpret_cast<uint32_t*>(tp);
+  uint32_t* toff = reinterpret_cast<uint32_t*>(tp + a256((size_t)ntiles * 4));
+  void* stemp = tp + 2 * a256((size_t)ntiles * 4);
+  uint32_t* d_total = reinterpret_cast<uint32_t*>(c->d_small + kCountSlot);
+  OWM_LAUNCH("k_nl_count", s, k_nl_count<<<(unsigned)ntiles, 256, 0, s>>>(dtext + 0, begin, nbytes, tcount));
+  count_launch(launches);
+  // newlines between begin and data_off belong to the header: subtract them on the host
+  OWM_CUDA_TRY(exclusive_scan_u32(tcount, toff, ntiles, d_total, stemp, scan_temp_bytes(ntiles), s, launches));
+  uint32_t total_nl = 0;
+  OWM_CUDA_TRY(cudaMemcpyAsync(&total_nl, d_total, 4, cudaMemcpyDeviceToHost, s));
+  OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  // header newlines inside [begin, data_off): at most 15 bytes, counted on the device copy's host twin
+  int64_t hdr_nl = 0;
+  if (data_off > begin) {
+    char hb[16];
+    OWM_CUDA_TRY(cudaMemcpy(hb, dtext + begin, (size_t)(data_off - begin), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < data_off - begin; ++i) hdr_nl += hb[i] == '\n';
+  }
+  const int64_t nl = (int64_t)total_nl - hdr_nl;
+  char last = '\n';
+  if (nbytes > data_off) OWM_CUDA_TRY(cudaMemcpy(&last, dtext + nbytes - 1, 1, cudaMemcpyDeviceToHost));
+  const int64_t nlines = nl + (nbytes > data_off && last != '\n' ? 1 : 0);
+  if (nlines <= 0) {
+    tmp.release(s);
+    return OWM_EIO;
+  }
+  // line starts: starts[0] = data_off; starts[k] (k >= 1) after the k-th data newline
+  // (k_nl_starts numbers newlines from begin, so its index is shifted by hdr_nl)
+  const size_t lb = a256((size_t)(nlines + 1 + hdr_nl + 1) * 8) + a256((size_t)nlines * 24) + a256((size_t)nlines) +
+                    2 * a256((size_t)nlines * 4) + a256((size_t)nlines * 8) + a256(scan_temp_bytes(nlines)) + 1024;
+  DeviceBuffer work;
+  rc = work.reserve(lb, s);
+  if (rc) {
+    tmp.release(s);
+    return rc;
+  }
+  char* wp = static_cast<char*>(work.ptr);
+  auto take = [&](size_t b) {
+    void* q = wp;
+    wp += a256(b);
+    return q;
+  };
+  int64_t* starts_all = (int64_t*)take((size_t)(nlines + 1 + hdr_nl + 1) * 8);
+  double* vals = (double*)take((size_t)nlines * 24);
+  uint8_t* status = (uint8_t*)take((size_t)nlines);
+  uint32_t* is_point = (uint32_t*)take((size_t)nlines * 4);
+  uint32_t* pos = (uint32_t*)take((size_t)nlines * 4);
+  int64_t* slow = (int64_t*)take((size_t)nlines * 8);
+  void* ctemp = take(scan_temp_bytes(nlines));
+  unsigned long long* dwords = reinterpret_cast<unsigned long long*>(c->d_small + kBboxSlot);  // [0] nslow, [1] first error
+  OWM_LAUNCH("k_nl_starts", s, k_nl_starts<<<(unsigned)ntiles, 256, 0, s>>>(dtext, begin, nbytes, toff, starts_all));
+  count_launch(launches);
+  int64_t* starts = starts_all + hdr_nl;  // starts[0] is the slot before the first data newline
+  const int64_t first = data_off, endpos = nbytes + 1;
+  OWM_CUDA_TRY(cudaMemcpyAsync(starts, &first, 8, cudaMemcpyHostToDevice, s));
+  if (nlines > nl) OWM_CUDA_TRY(cudaMemcpyAsync(starts + nlines, &endpos, 8, cudaMemcpyHostToDevice, s));
+  const unsigned long long init[2] = {0ull, ~0ull};
+  OWM_CUDA_TRY(cudaMemcpyAsync(dwords, init, 16, cudaMemcpyHostToDevice, s));
+  ParseOut po{vals, status, slow, dwords};
+  OWM_LAUNCH("k_parse", s, k_parse<<<grid_of(nlines, 256), 256, 0, s>>>(dtext, starts, nlines, po));
+  OWM_LAUNCH("k_parse_slow", s, k_parse_slow<<<152 * 2, 128, 0, s>>>(dtext, starts, po));
+  OWM_LAUNCH("k_line_flags", s, k_line_flags<<<grid_of(nlines, 256), 256, 0, s>>>(status, nlines, is_point, dwords + 1));
+  count_launch(launches, 3);
+  uint32_t* d_npts = reinterpret_cast<uint32_t*>(c->d_small + kCountSlot);
+  OWM_CUDA_TRY(exclusive_scan_u32(is_point, pos, nlines, d_npts, ctemp, scan_temp_bytes(nlines), s, launches));
+  unsigned long long h[2];
+  uint32_t npts = 0;
+  OWM_CUDA_TRY(cudaMemcpyAsync(h, dwords, 16, cudaMemcpyDeviceToHost, s));
+  OWM_CUDA_TRY(cudaMemcpyAsync(&npts, d_npts, 4, cudaMemcpyDeviceToHost, s));
+  OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  // points before the first error line: the loader stops at that line unless
+  // the declared count was reached before it
+  int64_t before = npts;
+  if (h[1] != ~0ull) {
+    uint32_t pb = 0;
+    OWM_CUDA_TRY(cudaMemcpy(&pb, pos + h[1], 4, cudaMemcpyDeviceToHost));
+    before = pb;
+  }
+  int64_t n;
+  if (declared >= 0) {
+    if (before < declared) rc = OWM_EIO;  // an error line or a short file before the declared count
+    n = declared;
+  } else {
+    if (h[1] != ~0ull) rc = OWM_EIO;
+    n = npts;
+  }
+  if (!rc && (n <= 0 || n >= 0x7FFFFFFFLL)) rc = OWM_EIO;
+  if (!rc) rc = out_mem->reserve((size_t)n * 24 + kXyzSlack, s);
+  if (!rc) {
+    OWM_LAUNCH("k_compact_points", s, k_compact_points<<<grid_of(nlines, 256), 256, 0, s>>>(
+        vals, is_point, pos, nlines, n, static_cast<double*>(out_mem->ptr)));
+    count_launch(launches);
+    OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  work.release(s);
+  tmp.release(s);
+  if (!rc) *n_out = n;
+  return rc;
+}
+
+}  // namespace owm

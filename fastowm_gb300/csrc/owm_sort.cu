@@ -479,8 +479,10 @@ cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout
 }  // namespace
 
 size_t scan_temp_bytes(int64_t n) {
-  int64_t parts = (n + kScanChunk - 1) / kScanChunk;
-  return (size_t)(parts + 64) * sizeof(uint32_t);
+  const int64_t parts = (n + kScanChunk - 1) / kScanChunk;
+  size_t b = ((size_t)(parts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
+  if (parts > (int64_t)kScanChunk) b += scan_temp_bytes(parts);  // the partial sums are scanned the same way
+  return b;
 }
 
 namespace {
@@ -513,13 +515,21 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
     if (total) return cudaMemsetAsync(total, 0, sizeof(uint32_t), s);
     return cudaSuccess;
   }
-  int64_t parts = (n + kScanChunk - 1) / kScanChunk;
-  if (parts > (int64_t)kScanChunk || temp_bytes < scan_temp_bytes(n)) return cudaErrorInvalidValue;
+  const int64_t parts = (n + kScanChunk - 1) / kScanChunk;
+  if (temp_bytes < scan_temp_bytes(n) || n >= ((int64_t)1 << 40)) return cudaErrorInvalidValue;
   uint32_t* part = static_cast<uint32_t*>(temp);
   OWM_LAUNCH("k_scan_reduce", s, k_scan_reduce<<<(unsigned)parts, kScanBlock, 0, s>>>(in, n, part));
-  OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(part, parts, total));
+  count_launch(launches, 2);
+  if (parts <= (int64_t)kScanChunk) {
+    OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(part, parts, total));
+    count_launch(launches);
+  } else {  // more than 2^26 values: scan the partial sums in place, recursively
+    const size_t pb = ((size_t)(parts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
+    cudaError_t e = exclusive_scan_u32(part, part, parts, total, static_cast<char*>(temp) + pb, temp_bytes - pb, s,
+                                       launches);
+    if (e != cudaSuccess) return e;
+  }
   OWM_LAUNCH("k_scan_down", s, k_scan_down<<<(unsigned)parts, kScanBlock, 0, s>>>(in, out, n, part));
-  count_launch(launches, 3);
   return cudaGetLastError();
 }
 

@@ -148,6 +148,23 @@ int owm_cloud_create(owm_ctx* ctx, const double* xyz, int64_t n, const owm_bbox*
                      owm_cloud** out);
 int owm_cloud_destroy(owm_cloud* cloud);
 int64_t owm_cloud_size(const owm_cloud* cloud);
+/* The cloud's bbox (the header's or the data's, as the cloud was made). */
+int owm_cloud_bbox(const owm_cloud* cloud, owm_bbox* out);
+/* Copies the cloud's first n points (AoS x, y, z) to host memory. */
+int owm_cloud_copy_out(const owm_cloud* cloud, double* xyz, int64_t n);
+/* Cloud ingest on the GPU, replacing readXYZfile (optim3_func.cpp:665-722)
+ * and map_file_atof_tbb_th (SYCL-CUDA-GPU/basic/utils.h:338-395).  Parses
+ * the text of an .xyz file on the device with owm_xyz_read's rules (optional
+ * header "N", "minx", "maxx", "miny", "maxy" on five lines; then one line
+ * per point read as sscanf("%lf %lf %lf"); blank lines skipped; other short
+ * lines, non-finite values and a short file are OWM_EIO; with a header the
+ * lines after the declared count are not read).  Values are the correctly
+ * rounded doubles of the C library's conversion, bit for bit.  bbox = the
+ * header's, else the data's min/max.  `text` is host memory. */
+int owm_cloud_parse_xyz(owm_ctx* ctx, const char* text, int64_t nbytes, owm_cloud** out);
+/* Same for a file: read through pinned memory in 64 MB chunks, each chunk's
+ * copy to the device overlapping the read of the next. */
+int owm_cloud_load_xyz(owm_ctx* ctx, const char* path, owm_cloud** out);
 
 /* ---- spatial index ----------------------------------------------------- */
 #define OWM_TREE_MAX_NUMBER 1 /* leaves of <= max_number points (o4maxnum) */

@@ -75,6 +75,8 @@ def _oracle():
                                   P(C.c_int64), P(C.c_int64), C.c_int]
         _o.oracle_run.restype = C.c_int64
         _o.oracle_window_box.argtypes = [P(OracleParams), C.c_int64, C.c_int64, P(C.c_double)]
+        _o.oracle_xyz_parse.argtypes = [C.c_char_p, C.c_int64, P(C.c_double), C.c_int64, P(C.c_int64),
+                                        P(C.c_double), P(C.c_int)]
         _o.oracle_cell_box.argtypes = [P(OracleParams), C.c_int64, C.c_int64, P(C.c_double)]
     return _o
 
@@ -112,6 +114,8 @@ def _ref():
             raise OSError("reference runner not built (needs the reference sources)")
         _r = C.CDLL(str(LIB_REF))
         P = C.POINTER
+        _r.owmref_read_xyz.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_double)]
         _r.owmref_run.argtypes = [P(C.c_double), C.c_int64, P(C.c_double), C.c_uint32, C.c_uint32, C.c_double,
                                   C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int),
                                   C.c_int64, P(C.c_int), C.c_int64, P(RefResult)]
@@ -212,3 +216,33 @@ def port_run(xyz, bbox, W: int, O: float, B: int, policy: int = 1, max_number: i
     if n < 0:
         raise RuntimeError("reference port run failed")
     return out[:n].copy(), nllp.value, tt.value, to.value
+
+
+def xyz_parse(text: bytes):
+    """readXYZfile's rules on .xyz text (oracle_xyz_parse): (points [n, 3],
+    bbox (min_x, min_y, max_x, max_y), has_header), or None where the loader
+    fails."""
+    o = _oracle()
+    cap = text.count(b"\n") + 2
+    out = np.empty((cap, 3), dtype=np.float64)
+    n = C.c_int64()
+    bb = np.zeros(4, dtype=np.float64)
+    hh = C.c_int()
+    rc = o.oracle_xyz_parse(bytes(text), len(text), _d(out), cap, C.byref(n), _d(bb), C.byref(hh))
+    if rc != 0:
+        return None
+    return out[: n.value].copy(), tuple(bb.tolist()), bool(hh.value)
+
+
+def ref_read_xyz(path: str, cap: int):
+    """The reference's own readXYZfile on a header file (its name must carry
+    one of the reference's header names, e.g. ...ArzuaH.xyz): (points, bbox)
+    or None where it fails."""
+    r = _ref()
+    out = np.empty((cap, 3), dtype=np.float64)
+    n = C.c_int64()
+    bb = np.zeros(4, dtype=np.float64)
+    rc = r.owmref_read_xyz(str(path).encode(), _d(out), cap, C.byref(n), _d(bb))
+    if rc != 0:
+        return None
+    return out[: n.value].copy(), tuple(bb.tolist())

@@ -18,6 +18,8 @@
  *           whose box holds no LLP strictly inside get the min point of the
  *           cell when the cell holds any point.
  *  output   owm_optim3.cpp:229-230: stage-3 ids, then the LLPs.
+ *  ingest   optim3_func.cpp:665-722 (readXYZfile): oracle_xyz_parse, the
+ *           checker of the device text parser.
  *
  * Tie rule: the reference keeps the first minimum its tree visits (strict
  * `<` on z).  This restatement orders points by (z, id) lexicographically,
@@ -38,6 +40,7 @@
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -386,4 +389,101 @@ int64_t oracle_run(const double* xyz, int64_t n, const double* bbox, uint32_t W,
   free(win);
   free(s3);
   return n3 + n_llp;
+}
+
+/* Cloud text (test infrastructure): readXYZfile (optim3_func.cpp:665-722)
+ * restated line by line on a text buffer, with the C library's own sscanf
+ * conversions, as the device ingest must reproduce them:
+ *   * the first line decides: one number = header (the point count, then one
+ *     value per line: min x, max x, min y, max y; :694-699), three or more =
+ *     no header (the bbox is then the data's);
+ *   * every later line is sscanf("%lf %lf %lf") (:711, the rest of the line
+ *     skipped as at :715); lines of spaces, tabs and CRs are skipped, any
+ *     other line with fewer than three numbers fails;
+ *   * with a header, reading stops at the declared count (:710), and fewer
+ *     points fail; non-finite values fail.
+ * A line is the text up to its newline (a NUL ends what sscanf sees).
+ * Returns 0 (points in out[0..3n), bbox4 = {min_x, min_y, max_x, max_y}) or
+ * -5 (the loader's error) / -2 (cap too small). */
+int oracle_xyz_parse(const char* text, int64_t nbytes, double* out, int64_t cap, int64_t* n_out, double* bbox4,
+                     int* has_header) {
+  int64_t pos = 0, n = 0, declared = -1;
+  size_t lcap = 256;
+  char* line = (char*)malloc(lcap);
+  int rc = 0;
+  int first = 1;
+  double hb[4] = {0, 0, 0, 0};
+  int hdr_left = 0;
+  if (!line) return -5;
+  *has_header = 0;
+  while (pos < nbytes) {
+    const char* nl = (const char*)memchr(text + pos, '\n', (size_t)(nbytes - pos));
+    int64_t e = nl ? (int64_t)(nl - text) : nbytes;
+    size_t len = (size_t)(e - pos);
+    if (len + 2 > lcap) {
+      lcap = len + 2;
+      line = (char*)realloc(line, lcap);
+      if (!line) return -5;
+    }
+    memcpy(line, text + pos, len);
+    line[len] = '\n';
+    line[len + 1] = 0;
+    pos = e + 1;
+    double a[3];
+    if (first) {
+      int k = sscanf(line, "%lf %lf %lf", &a[0], &a[1], &a[2]);
+      first = 0;
+      if (k == 1) {
+        if (!(a[0] >= 1.0 && a[0] < 9.2e18)) { rc = -5; break; }
+        declared = (int64_t)a[0];
+        *has_header = 1;
+        hdr_left = 4;
+        continue;
+      }
+      if (k != 3) { rc = -5; break; }
+    } else if (hdr_left > 0) {
+      if (sscanf(line, "%lf", &hb[4 - hdr_left]) != 1) { rc = -5; break; }
+      --hdr_left;
+      continue;
+    } else {
+      if (declared >= 0 && n >= declared) break;
+      if (sscanf(line, "%lf %lf %lf", &a[0], &a[1], &a[2]) != 3) {
+        int blank = 1;
+        for (char* c = line; *c; ++c)
+          if (*c != ' ' && *c != '\n' && *c != '\r' && *c != '\t') blank = 0;
+        if (blank) continue;
+        rc = -5;
+        break;
+      }
+    }
+    if (!isfinite(a[0]) || !isfinite(a[1]) || !isfinite(a[2])) { rc = -5; break; }
+    if (n >= cap) { rc = -2; break; }
+    out[3 * n] = a[0];
+    out[3 * n + 1] = a[1];
+    out[3 * n + 2] = a[2];
+    ++n;
+  }
+  free(line);
+  if (rc) return rc;
+  if (hdr_left > 0 || n == 0 || (declared >= 0 && n < declared)) return -5;
+  if (declared >= 0) {
+    bbox4[0] = hb[0];  /* min x */
+    bbox4[1] = hb[2];  /* min y */
+    bbox4[2] = hb[1];  /* max x */
+    bbox4[3] = hb[3];  /* max y */
+  } else {
+    double x0 = out[0], x1 = out[0], y0 = out[1], y1 = out[1];
+    for (int64_t i = 1; i < n; ++i) {
+      x0 = out[3 * i] < x0 ? out[3 * i] : x0;
+      x1 = out[3 * i] > x1 ? out[3 * i] : x1;
+      y0 = out[3 * i + 1] < y0 ? out[3 * i + 1] : y0;
+      y1 = out[3 * i + 1] > y1 ? out[3 * i + 1] : y1;
+    }
+    bbox4[0] = x0;
+    bbox4[1] = y0;
+    bbox4[2] = x1;
+    bbox4[3] = y1;
+  }
+  *n_out = n;
+  return 0;
 }

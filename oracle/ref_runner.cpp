@@ -23,6 +23,7 @@
 #include <cfloat>
 #include <cstdint>
 #include <cstring>
+#include <string>
 
 extern "C" {
 
@@ -152,6 +153,36 @@ int owmref_run(const double* xyz, int64_t n, const double* bbox, uint32_t Wsize,
   delete[] minIDs;
   deleteQtree(qtreeIn);
   delete qtreeIn;
+  free(cloud);
+  return rc;
+}
+
+// The reference's own loader on a file: readXYZfile (optim3_func.cpp:665-722)
+// accepts header files whose name contains one of its known header names
+// (e.g. "ArzuaH.xyz").  out gets the n points after the sentinel, bbox4 =
+// {min_x, min_y, max_x, max_y} from the header.  Returns 0, -1 when the
+// reference's loader fails, -2 if cap is too small.
+int owmref_read_xyz(const char* path, double* out, int64_t cap, int64_t* n, double* bbox4) {
+  Lpoint* cloud = nullptr;
+  uint32_t np = 0;
+  Vector2D mn{0, 0}, mx{0, 0};
+  if (readXYZfile(std::string(path), cloud, np, mn, mx) != 0) return -1;
+  const int64_t pts = (int64_t)np - 1;  // np counts the sentinel
+  int rc = 0;
+  if (pts > cap) {
+    rc = -2;
+  } else {
+    for (int64_t i = 0; i < pts; ++i) {
+      out[3 * i] = cloud[i + 1].x;
+      out[3 * i + 1] = cloud[i + 1].y;
+      out[3 * i + 2] = cloud[i + 1].z;
+    }
+    *n = pts;
+    bbox4[0] = mn.x;
+    bbox4[1] = mn.y;
+    bbox4[2] = mx.x;
+    bbox4[3] = mx.y;
+  }
   free(cloud);
   return rc;
 }
