@@ -255,7 +255,9 @@ def main():
     ap.add_argument("--leaf", type=int, default=0,
                     help="leaf size (maxNumber) of the main workload; 0 = tuned by fastowm_gb300.autotune, "
                          "-1 = the workload's configured value")
-    ap.add_argument("--only", choices=["batched", "served"], default=None,
+    ap.add_argument("--no-ingest", action="store_true")
+    ap.add_argument("--ingest-n", type=int, default=20_000_000, help="points of the ingest leg's text")
+    ap.add_argument("--only", choices=["batched", "served", "ingest"], default=None,
                     help="run that leg alone and print its JSON (profiling and tuning runs)")
     args = ap.parse_args()
     ws, rank, local = dist_setup(args)
@@ -272,8 +274,9 @@ def main():
     torch.cuda.set_device(local)
     if args.only:
         ctx = F.Context(local)
-        leg = run_batched(F, torch, ctx, args, local, ws) if args.only == "batched" else \
-            run_served(F, torch, ctx, args, local)
+        leg = {"batched": lambda: run_batched(F, torch, ctx, args, local, ws),
+               "served": lambda: run_served(F, torch, ctx, args, local),
+               "ingest": lambda: run_ingest(F, torch, ctx, args, local)}[args.only]()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "unit": UNIT, "impl": "ours", "only": args.only, args.only: leg}),
                   flush=True)
@@ -382,6 +385,7 @@ def main():
 
     batched = None if args.no_batched else run_batched(F, torch, ctx, args, local, ws)
     served = None if (args.no_served or ws > 1) else run_served(F, torch, ctx, args, local)
+    ingest = None if (args.no_ingest or ws > 1) else run_ingest(F, torch, ctx, args, local)
 
     # ---- roofline of the dominant kernel --------------------------------------------------------
     peak, peak_kind = peaks()
@@ -436,7 +440,7 @@ def main():
                                 "launches_per_step": v[1] / args.steps} for k, v in
                             sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
                 "roofline": roof, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-                "batched": batched, "served": served,
+                "batched": batched, "served": served, "ingest": ingest,
                 "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     cloud.close()
@@ -546,6 +550,131 @@ def run_batched(F, torch, ctx, args, local, ws):
                         for k, v in sorted(kb.items(), key=lambda kv: -kv[1][0])},
             "timing": "host clock around synchronous calls, device-resident inputs; kernels: one extra "
                       "untimed run without graphs, CUDA events per launch"}
+
+
+def lidar_text(n: int, seed: int):
+    """Synthetic .xyz text in the reference's header format: the point count
+    and the bbox on five lines, then fixed-width "%.3f" x y z lines (31
+    bytes) over the 2 km x 2 km workload area.  Returns (text bytes as a
+    uint8 array, the exact points X/1000 etc. as float64 [n, 3])."""
+    rng = np.random.default_rng(seed)
+    X = rng.integers(600_000_000, 602_000_000, n)
+    Y = rng.integers(4_500_000_000, 4_502_000_000, n)
+    Z = rng.integers(80_000, 160_000, n)
+    L = 31
+    body = np.full((n, L), ord(" "), dtype=np.uint8)
+
+    tab = np.array([[ord(ch) for ch in f"{i:03d}"] for i in range(1000)], dtype=np.uint8)
+
+    def put(col, ndig, v):  # ndig digits of v, the last three after a '.' (three at a time)
+        c = col + ndig + 1  # one past the field
+        v = v.astype(np.uint32) if v.max() < 2 ** 32 else v.copy()
+        first = True
+        while ndig > 0:
+            v, g = np.divmod(v, 1000)
+            k = min(3, ndig)
+            body[:, c - k:c] = tab[g][:, 3 - k:]
+            c -= k
+            ndig -= k
+            if first:
+                body[:, c - 1] = ord(".")
+                c -= 1
+                first = False
+
+    put(0, 9, X)
+    put(11, 10, Y)
+    put(23, 6, Z)
+    small = Z < 100_000  # "%7.3f": a blank instead of the leading zero
+    body[small, 23] = ord(" ")
+    body[:, L - 1] = ord("\n")
+    pts = np.column_stack([X / 1000.0, Y / 1000.0, Z / 1000.0])  # correctly rounded, as a parse must give
+    lo_x, hi_x, lo_y, hi_y = (float(v) / 1000.0 for v in (X.min(), X.max(), Y.min(), Y.max()))
+    head = f"{n}\n{lo_x!r}\n{hi_x!r}\n{lo_y!r}\n{hi_y!r}\n".encode()
+    return np.concatenate([np.frombuffer(head, dtype=np.uint8), body.reshape(-1)]), pts
+
+
+def run_ingest(F, torch, ctx, args, local):
+    """Cloud ingest on the device: .xyz text parsed by owm_cloud_parse_xyz,
+    from device-resident text (value) and from pinned host text (e2e, the copy
+    to the device timed), against the C library's sscanf loop on the host."""
+    import ctypes as C
+
+    n = args.ingest_n
+    text, pts = lidar_text(n, 7)
+    host = torch.empty(text.size, dtype=torch.uint8, pin_memory=True)
+    host.numpy()[:] = text
+    dev = host.to(f"cuda:{local}")
+    torch.cuda.synchronize()
+    dptr = C.c_char_p(dev.data_ptr())
+    hptr = C.c_char_p(host.data_ptr())
+
+    def parse(ptr):
+        h = C.c_void_p()
+        rc = F.lib().owm_cloud_parse_xyz(ctx.handle, ptr, text.size, C.byref(h))
+        if rc:
+            raise RuntimeError(f"owm_cloud_parse_xyz: {rc}")
+        return h
+
+    # parity: every parsed point equals the exact decimal value, bit for bit
+    c = ctx._parsed_cloud(parse(dptr))
+    got = c.points()
+    parity = bool(got.shape == pts.shape and np.array_equal(got.view(np.uint64), pts.view(np.uint64)))
+    c.close()
+    del got
+    reps, warm = 5, 2
+
+    def timed(ptr):
+        for _ in range(warm):
+            F.lib().owm_cloud_destroy(parse(ptr))
+        t = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h = parse(ptr)
+            t.append(time.perf_counter() - t0)
+            F.lib().owm_cloud_destroy(h)
+        return float(np.median(t))
+
+    t_dev = timed(dptr)
+    t_host = timed(hptr)
+    # per-kernel split of one device-text parse
+    F.lib().owm_ctx_set_profiling(ctx.handle, 1)
+    F.lib().owm_cloud_destroy(parse(dptr))
+    kt = kernel_times(F, ctx)  # before profiling is switched off (that clears the records)
+    F.lib().owm_ctx_set_profiling(ctx.handle, 0)
+    ktot = sum(v[0] for v in kt.values()) or 1.0
+    kernels = {k: {"ms": round(v[0], 4), "share": round(v[0] / ktot, 4), "launches": v[1]}
+               for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])}
+    peak, peak_kind = peaks()
+    # the parse kernel reads its lines' text once and writes 24 B per point
+    kp = kt.get("k_parse", (None, 0))[0]
+    parse_bytes = float(text.size) + 24.0 * n
+    roof = None
+    if kp:
+        ach = parse_bytes / (kp / 1e3) / 1e9
+        roof = {"kernel": "k_parse", "bound": "hbm", "achieved": round(ach, 1), "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": round(ach / peak, 4),
+                "bytes_per_launch": parse_bytes, "ms_per_launch": round(kp, 4)}
+    # CPU: the C library's sscanf per line under readXYZfile's rules, on a sample
+    from oracle import oracle as O
+    ns = min(n, 2_000_000)
+    sample_head = (f"{ns}\n0\n1\n0\n1\n").encode()
+    body_off = text.size - n * 31
+    sample = sample_head + text[body_off:body_off + ns * 31].tobytes()
+    t0 = time.perf_counter()
+    r = O.xyz_parse(sample)
+    t_cpu = time.perf_counter() - t0
+    cpu_ok = r is not None and np.array_equal(r[0].view(np.uint64), pts[:ns].view(np.uint64))
+    return {"workload": f"{n} points of .xyz text ({text.size / 1e9:.3f} GB, header + fixed-width %.3f lines, "
+                        f"31 B/line)",
+            "value": round(n / t_dev / 1e6, 1), "unit": "Mpts/s", "text_gbs": round(text.size / t_dev / 1e9, 1),
+            "ms": round(1e3 * t_dev, 3),
+            "e2e": {"value": round(n / t_host / 1e6, 1), "unit": "Mpts/s", "ms": round(1e3 * t_host, 3),
+                    "h2d_bytes": int(text.size), "from": "pinned host text (owm_cloud_parse_xyz)"},
+            "parity_bit_exact": parity, "kernels": kernels, "roofline": roof,
+            "cpu_baseline": {"value": round(ns / t_cpu / 1e6, 3), "unit": "Mpts/s", "cores": 1, "kind": "port",
+                             "sample": f"{ns} lines of the same text, sscanf per line (oracle_xyz_parse)",
+                             "equal": bool(cpu_ok)}}
 
 
 def run_served(F, torch, ctx, args, local):

@@ -405,14 +405,27 @@ int owm_cloud_parse_xyz(owm_ctx* c, const char* text, int64_t nbytes, owm_cloud*
   *out = nullptr;
   if (nbytes == 0) return OWM_EIO;  // like an empty file
   OWM_CUDA_TRY(cudaSetDevice(c->device));
+  // device text: the header is read from a host copy of its first MB (the
+  // header's lines are short; a first data line only needs three numbers)
+  const bool on_device = is_device_ptr(text);
+  std::vector<char> head;
+  const char* htext = text;
+  int64_t hbytes = nbytes;
+  if (on_device) {
+    hbytes = std::min<int64_t>(nbytes, (int64_t)1 << 20);
+    head.resize((size_t)hbytes);
+    OWM_CUDA_TRY(cudaMemcpy(head.data(), text, (size_t)hbytes, cudaMemcpyDeviceToHost));
+    htext = head.data();
+  }
   int64_t data_off = 0, declared = -1;
   owm_bbox hb{};
-  int rc = xyz_header(text, nbytes, &data_off, &declared, &hb);
+  int rc = xyz_header(htext, hbytes, &data_off, &declared, &hb);
   if (rc) return rc;
   DeviceBuffer dt, pts;
+  // the parser's 16-byte loads want an aligned copy with readable slack
   rc = dt.reserve((size_t)((nbytes + 15) & ~(int64_t)15) + 32, c->stream);
   if (rc) return rc;
-  cudaError_t e = cudaMemcpyAsync(dt.ptr, text, (size_t)nbytes, cudaMemcpyHostToDevice, c->stream);
+  cudaError_t e = cudaMemcpyAsync(dt.ptr, text, (size_t)nbytes, cudaMemcpyDefault, c->stream);
   if (e != cudaSuccess) {
     set_last_cuda_error(e, "text copy", __FILE__, __LINE__);
     dt.release(c->stream);

@@ -10,9 +10,9 @@
 // the reference's fixed-column form of the same loader.
 //
 // Pipeline (text resident on the device, 16 bytes of readable slack):
-//   k_nl_count   newlines per 64 KB tile
-//   scan         tile offsets
-//   k_nl_starts  line start positions (one thread per 256 bytes, block scan)
+//   k_nl_count   newlines per 2 KB segment (one warp, coalesced 16-byte loads)
+//   scan         segment offsets
+//   k_nl_starts  line start positions (byte masks, warp scan per round)
 //   k_parse      one thread per line: the sscanf grammar on 16-byte loads,
 //                values by Clinger's exact fast path (significand <= 2^53,
 //                |decimal exponent| <= 22: one correctly rounded IEEE
@@ -22,8 +22,9 @@
 //                rounded by big-integer comparison with the halfway points
 //                of the candidate doubles (a candidate from a table of
 //                correctly rounded powers of ten, moved one double at a time)
-//   resolve      first error line, points before it, compaction of blank
-//                lines (skipped when there are none)
+//   resolve      first error line, points before it; the per-line values
+//                become the cloud as they are when the first n lines are all
+//                points, else blank lines are compacted out
 // The values equal what the C library's correctly rounded conversion gives
 // for the same text, bit for bit.
 #include <cuda_runtime.h>
@@ -43,7 +44,6 @@ namespace owm {
 namespace {
 
 constexpr int kLinePoint = 0, kLineBlank = 1, kLineError = 2, kLineSlow = 3;
-constexpr int64_t kTileBytes = 65536;  // newline-count tile: 256 threads x 256 bytes
 constexpr int kPowMin = -300, kPowMax = 300;
 
 __constant__ double c_pow10[kPowMax - kPowMin + 1];  // correctly rounded 10^k, k = -300..300
@@ -107,6 +107,25 @@ __device__ double round_bits(uint64_t m, bool sticky, int64_t e2, bool neg) {
   else
     bits = mant;  // subnormal: mant counts units of 2^-1074 (2^52 = smallest normal)
   return __longlong_as_double((long long)(sign | bits));
+}
+
+__device__ __forceinline__ void split_double(uint64_t bits, uint64_t* m, int64_t* q) {
+  const uint64_t ef = bits >> 52, fr = bits & 0xFFFFFFFFFFFFFull;
+  if (ef == 0) {
+    *m = fr;
+    *q = -1074;
+  } else {
+    *m = fr | 0x10000000000000ull;
+    *q = (int64_t)ef - 1075;
+  }
+}
+
+// ---- exact w / 10^k on 32-bit multiplies (1 <= k <= 13) ----------------------------
+// The double of an integer w <= 2^53, from its bits (no FP64 instruction).
+__device__ __forceinline__ double u53_to_double(uint64_t w) {
+  if (w == 0) return 0.0;
+  const int lz = __clzll((long long)w);
+  return __longlong_as_double((long long)(((uint64_t)(1085 - lz) << 52) + ((w << lz) >> 11)));
 }
 
 // ---- big integers for the exact decimal path ----------------------------------
@@ -180,17 +199,6 @@ __device__ int cmp_halfway(const Big& D, int64_t E, bool sticky, uint64_t m, int
   int c = big_cmp(L, R);
   if (c == 0 && sticky) c = 1;
   return c;
-}
-
-__device__ __forceinline__ void split_double(uint64_t bits, uint64_t* m, int64_t* q) {
-  const uint64_t ef = bits >> 52, fr = bits & 0xFFFFFFFFFFFFFull;
-  if (ef == 0) {
-    *m = fr;
-    *q = -1074;
-  } else {
-    *m = fr | 0x10000000000000ull;
-    *q = (int64_t)ef - 1075;
-  }
 }
 
 // ---- field grammar -------------------------------------------------------------
@@ -401,8 +409,8 @@ __device__ int parse_field(TextCursor& tc, int64_t p, double* v, int64_t* end, B
       w *= 10;
       --e;
     }
-    if (e >= -22 && e <= 22) {
-      const double x = (double)w;  // exact: w <= 2^53
+    if (e >= -22 && e <= 22) {  // Clinger: one correctly rounded IEEE multiply or divide of exact operands
+      const double x = u53_to_double(w);
       const double r = e >= 0 ? __dmul_rn(x, c_pow10[e - kPowMin]) : __ddiv_rn(x, c_pow10[-e - kPowMin]);
       *v = neg ? -r : r;
       return isfinite(r) ? kFieldOk : kFieldNonFinite;
@@ -419,6 +427,7 @@ __device__ int parse_line(const char* text, int64_t s, int64_t e, double* out, B
   TextCursor tc(text, e);
   int64_t p = s;
   int f = 0;
+#pragma unroll
   for (; f < 3; ++f) {
     uint32_t c;
     while ((c = tc.at(p)) != 0 && is_space(c)) ++p;
@@ -440,72 +449,80 @@ __device__ int parse_line(const char* text, int64_t s, int64_t e, double* out, B
 }
 
 // ---- kernels -------------------------------------------------------------------
-__device__ __forceinline__ uint32_t count_nl_word(uint32_t x) {
-  return (uint32_t)__popc(__vcmpeq4(x, 0x0A0A0A0Au)) >> 3;  // one 0xFF byte per match
-}
+constexpr int64_t kSegBytes = 2048;  // one warp per segment: four rounds of 32 lanes x 16 bytes
 
-// Newlines of tile blockIdx.x ([begin + t*kTileBytes, ...) within [begin, end)):
-// per thread 256 bytes, 16 at a time.  begin is 16-byte aligned.
-__global__ void __launch_bounds__(256) k_nl_count(const char* __restrict__ text, int64_t begin, int64_t end,
-                                                  uint32_t* __restrict__ tile_count) {
-  const int64_t b = begin + (int64_t)blockIdx.x * kTileBytes + (int64_t)threadIdx.x * 256;
-  uint32_t cnt = 0;
-  for (int k = 0; k < 16; ++k) {
-    const int64_t o = b + k * 16;
-    if (o >= end) break;
-    const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
-    if (o + 16 <= end) {
-      cnt += count_nl_word(w.x) + count_nl_word(w.y) + count_nl_word(w.z) + count_nl_word(w.w);
-    } else {
-      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-      for (int j = 0; j < 16 && o + j < end; ++j) cnt += ((ws[j >> 2] >> ((j & 3) * 8)) & 0xFFu) == '\n';
+// 0xFF in every byte of x that is a newline.
+__device__ __forceinline__ uint32_t nl_bytes(uint32_t x) { return __vcmpeq4(x, 0x0A0A0A0Au); }
+
+// Newline masks of lane's 16 bytes at o (bytes at or past `end` masked off).
+__device__ __forceinline__ void nl_masks(const char* __restrict__ text, int64_t o, int64_t end, uint32_t m[4]) {
+  if (o >= end) {
+    m[0] = m[1] = m[2] = m[3] = 0;
+    return;
+  }
+  const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
+  m[0] = nl_bytes(w.x);
+  m[1] = nl_bytes(w.y);
+  m[2] = nl_bytes(w.z);
+  m[3] = nl_bytes(w.w);
+  const int64_t valid = end - o;  // bytes of this word inside the range
+  if (valid < 16) {
+    for (int j = 0; j < 4; ++j) {
+      const int64_t vb = valid - 4 * j;  // valid bytes of word j
+      if (vb <= 0)
+        m[j] = 0;
+      else if (vb < 4)
+        m[j] &= (1u << (8 * vb)) - 1;
     }
   }
-  for (int o = 16; o >= 1; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-  __shared__ uint32_t ws[8];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t t = 0;
-    for (int i = 0; i < 8; ++i) t += ws[i];
-    tile_count[blockIdx.x] = t;
+}
+
+// Newlines of segment s = [begin + s*kSegBytes, ...) within [begin, end); one
+// warp per segment, coalesced 16-byte loads.  begin is 16-byte aligned.
+__global__ void __launch_bounds__(256) k_nl_count(const char* __restrict__ text, int64_t begin, int64_t end,
+                                                  int64_t nseg, uint32_t* __restrict__ seg_count) {
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= nseg) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  uint32_t cnt = 0;
+  for (int r = 0; r < 4; ++r) {
+    uint32_t m[4];
+    nl_masks(text, begin + s * kSegBytes + r * 512 + lane * 16, end, m);
+    cnt += (__popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3])) >> 3;
   }
+  for (int o = 16; o >= 1; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (lane == 0) seg_count[s] = cnt;
 }
 
 // starts[k + 1] = position after the k-th newline of [begin, end) (k from 0),
-// in order; tile_off = scanned tile counts.
+// in order; seg_off = scanned segment counts.
 __global__ void __launch_bounds__(256) k_nl_starts(const char* __restrict__ text, int64_t begin, int64_t end,
-                                                   const uint32_t* __restrict__ tile_off,
+                                                   int64_t nseg, const uint32_t* __restrict__ seg_off,
                                                    int64_t* __restrict__ starts) {
-  const int64_t b = begin + (int64_t)blockIdx.x * kTileBytes + (int64_t)threadIdx.x * 256;
-  uint32_t cnt = 0;
-  for (int k = 0; k < 16; ++k) {
-    const int64_t o = b + k * 16;
-    if (o >= end) break;
-    const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
-    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-    for (int j = 0; j < 16 && o + j < end; ++j) cnt += ((ws[j >> 2] >> ((j & 3) * 8)) & 0xFFu) == '\n';
-  }
-  // exclusive scan of the per-thread counts over the block
-  __shared__ uint32_t wsum[8];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t inc = cnt;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += t;
-  }
-  if (lane == 31) wsum[wid] = inc;
-  __syncthreads();
-  uint32_t wbase = 0;
-  for (int i = 0; i < wid; ++i) wbase += wsum[i];
-  int64_t k = (int64_t)tile_off[blockIdx.x] + wbase + inc - cnt;
-  for (int kk = 0; kk < 16; ++kk) {
-    const int64_t o = b + kk * 16;
-    if (o >= end) break;
-    const uint4 w = __ldg(reinterpret_cast<const uint4*>(text + o));
-    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-    for (int j = 0; j < 16 && o + j < end; ++j)
-      if (((ws[j >> 2] >> ((j & 3) * 8)) & 0xFFu) == '\n') starts[++k] = o + j + 1;
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= nseg) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  int64_t base = seg_off[s];
+  for (int r = 0; r < 4; ++r) {
+    const int64_t o = begin + s * kSegBytes + r * 512 + lane * 16;
+    uint32_t m[4];
+    nl_masks(text, o, end, m);
+    const uint32_t c = (__popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3])) >> 3;
+    uint32_t inc = c;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+    int64_t k = base + inc - c;  // this lane's first newline index
+    for (int j = 0; j < 4; ++j) {
+      uint32_t mj = m[j];
+      while (mj) {
+        const int byte = (__ffs(mj) - 1) >> 3;
+        starts[++k] = o + 4 * j + byte + 1;
+        mj &= ~(0xFFu << (8 * byte));
+      }
+    }
+    base += __shfl_sync(0xffffffffu, inc, 31);
   }
 }
 
@@ -664,7 +681,7 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   // tiles start at a 16-byte boundary below data_off; bytes before it are not counted
   const int64_t begin = data_off & ~(int64_t)15;
   const int64_t span = nbytes - begin;
-  const int64_t ntiles = std::max<int64_t>(1, (span + kTileBytes - 1) / kTileBytes);
+  const int64_t ntiles = std::max<int64_t>(1, (span + kSegBytes - 1) / kSegBytes);  // segments
   // newline positions in [begin, data_off) must not count: the count runs from data_off
   // itself, so tiles use the exact byte range [data_off, nbytes)
   DeviceBuffer tmp;
@@ -676,7 +693,8 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   uint32_t* toff = reinterpret_cast<uint32_t*>(tp + a256((size_t)ntiles * 4));
   void* stemp = tp + 2 * a256((size_t)ntiles * 4);
   uint32_t* d_total = reinterpret_cast<uint32_t*>(c->d_small + kCountSlot);
-  OWM_LAUNCH("k_nl_count", s, k_nl_count<<<(unsigned)ntiles, 256, 0, s>>>(dtext + 0, begin, nbytes, tcount));
+  const unsigned seg_blocks = (unsigned)((ntiles * 32 + 255) / 256);  // one warp per segment
+  OWM_LAUNCH("k_nl_count", s, k_nl_count<<<seg_blocks, 256, 0, s>>>(dtext, begin, nbytes, ntiles, tcount));
   count_launch(launches);
   // newlines between begin and data_off belong to the header: subtract them on the host
   OWM_CUDA_TRY(exclusive_scan_u32(tcount, toff, ntiles, d_total, stemp, scan_temp_bytes(ntiles), s, launches));
@@ -700,7 +718,15 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   }
   // line starts: starts[0] = data_off; starts[k] (k >= 1) after the k-th data newline
   // (k_nl_starts numbers newlines from begin, so its index is shifted by hdr_nl)
-  const size_t lb = a256((size_t)(nlines + 1 + hdr_nl + 1) * 8) + a256((size_t)nlines * 24) + a256((size_t)nlines) +
+  // per-line values in their own buffer: when the first n lines are all
+  // points it becomes the cloud as it is (no compaction)
+  DeviceBuffer vbuf;
+  rc = vbuf.reserve((size_t)nlines * 24 + kXyzSlack, s);
+  if (rc) {
+    tmp.release(s);
+    return rc;
+  }
+  const size_t lb = a256((size_t)(nlines + 1 + hdr_nl + 1) * 8) + a256((size_t)nlines) +
                     2 * a256((size_t)nlines * 4) + a256((size_t)nlines * 8) + a256(scan_temp_bytes(nlines)) + 1024;
   DeviceBuffer work;
   rc = work.reserve(lb, s);
@@ -715,14 +741,14 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
     return q;
   };
   int64_t* starts_all = (int64_t*)take((size_t)(nlines + 1 + hdr_nl + 1) * 8);
-  double* vals = (double*)take((size_t)nlines * 24);
+  double* vals = static_cast<double*>(vbuf.ptr);
   uint8_t* status = (uint8_t*)take((size_t)nlines);
   uint32_t* is_point = (uint32_t*)take((size_t)nlines * 4);
   uint32_t* pos = (uint32_t*)take((size_t)nlines * 4);
   int64_t* slow = (int64_t*)take((size_t)nlines * 8);
   void* ctemp = take(scan_temp_bytes(nlines));
   unsigned long long* dwords = reinterpret_cast<unsigned long long*>(c->d_small + kBboxSlot);  // [0] nslow, [1] first error
-  OWM_LAUNCH("k_nl_starts", s, k_nl_starts<<<(unsigned)ntiles, 256, 0, s>>>(dtext, begin, nbytes, toff, starts_all));
+  OWM_LAUNCH("k_nl_starts", s, k_nl_starts<<<seg_blocks, 256, 0, s>>>(dtext, begin, nbytes, ntiles, toff, starts_all));
   count_launch(launches);
   int64_t* starts = starts_all + hdr_nl;  // starts[0] is the slot before the first data newline
   const int64_t first = data_off, endpos = nbytes + 1;
@@ -759,13 +785,27 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
     n = npts;
   }
   if (!rc && (n <= 0 || n >= 0x7FFFFFFFLL)) rc = OWM_EIO;
-  if (!rc) rc = out_mem->reserve((size_t)n * 24 + kXyzSlack, s);
-  if (!rc) {
-    OWM_LAUNCH("k_compact_points", s, k_compact_points<<<grid_of(nlines, 256), 256, 0, s>>>(
-        vals, is_point, pos, nlines, n, static_cast<double*>(out_mem->ptr)));
-    count_launch(launches);
-    OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  bool in_place = false;  // the first n lines are all points
+  if (!rc && n <= nlines) {
+    uint32_t pn = npts;
+    if (n < nlines) OWM_CUDA_TRY(cudaMemcpy(&pn, pos + n, 4, cudaMemcpyDeviceToHost));
+    in_place = (int64_t)pn == n;
   }
+  if (!rc && in_place) {
+    out_mem->release(s);
+    *out_mem = vbuf;
+    vbuf.ptr = nullptr;
+    vbuf.cap = 0;
+  } else if (!rc) {
+    rc = out_mem->reserve((size_t)n * 24 + kXyzSlack, s);
+    if (!rc) {
+      OWM_LAUNCH("k_compact_points", s, k_compact_points<<<grid_of(nlines, 256), 256, 0, s>>>(
+          vals, is_point, pos, nlines, n, static_cast<double*>(out_mem->ptr)));
+      count_launch(launches);
+    }
+  }
+  OWM_CUDA_TRY(cudaStreamSynchronize(s));
+  vbuf.release(s);
   work.release(s);
   tmp.release(s);
   if (!rc) *n_out = n;

@@ -160,7 +160,7 @@ int owm_cloud_copy_out(const owm_cloud* cloud, double* xyz, int64_t n);
  * lines, non-finite values and a short file are OWM_EIO; with a header the
  * lines after the declared count are not read).  Values are the correctly
  * rounded doubles of the C library's conversion, bit for bit.  bbox = the
- * header's, else the data's min/max.  `text` is host memory. */
+ * header's, else the data's min/max.  `text` is host or device memory. */
 int owm_cloud_parse_xyz(owm_ctx* ctx, const char* text, int64_t nbytes, owm_cloud** out);
 /* Same for a file: read through pinned memory in 64 MB chunks, each chunk's
  * copy to the device overlapping the read of the next. */
