@@ -134,12 +134,20 @@ __device__ __forceinline__ void write_leaf_seg(Node* nd, const LeafAcc& a, int32
 // third fewer random requests in the build's gather): the point's 24 bytes lie
 // in the 32 bytes from the 16-byte boundary at or below x.  Needs a 16-byte
 // aligned xyz with kXyzSlack readable bytes after the last point.
+// Read-only 16-byte load whose L2 miss asks for 64 bytes (the prefetch-size
+// hint), for gathers of random points.
+__device__ __forceinline__ double2 ldg_l2_64(const double2* p) {
+  double2 r;
+  asm("ld.global.nc.L2::64B.v2.f64 {%0, %1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+  return r;
+}
+
 __device__ __forceinline__ bool load_point16(const double* __restrict__ xyz, uint32_t src, int64_t& x, int64_t& y,
                                              int64_t& z) {
   const int64_t e = 3 * (int64_t)src;
   const int odd = (int)(e & 1);
   const double2* w = reinterpret_cast<const double2*>(xyz + (e - odd));
-  const double2 a = __ldg(w), b = __ldg(w + 1);
+  const double2 a = ldg_l2_64(w), b = ldg_l2_64(w + 1);
   const double dx = odd ? a.y : a.x, dy = odd ? b.x : a.y, dz = odd ? b.y : b.x;
   x = dkey(dx);
   y = dkey(dy);
