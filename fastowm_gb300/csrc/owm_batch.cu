@@ -67,6 +67,84 @@ __global__ void k_b_morton(const double* __restrict__ xyz, int64_t n, const int6
   }
 }
 
+// (tile, Morton) key of point i of tile m (the tile's integer or FP64 form).
+struct TileKey {
+  int64_t kx0, ky0, qm;
+  double ox, oy, scale;
+  float qmax;
+  int shx, shy, mint;
+  uint32_t tile_bits_key;  // t << (2 * mbits)
+  __device__ __forceinline__ void load(const TileMeta& m, int t, int mbits) {
+    kx0 = m.mkx0;
+    ky0 = m.mky0;
+    shx = m.mshx;
+    shy = m.mshy;
+    mint = m.mint;
+    ox = m.mox;
+    oy = m.moy;
+    scale = m.mscale;
+    qm = (1ll << mbits) - 1;
+    qmax = (float)((1u << mbits) - 1u);
+    tile_bits_key = (uint32_t)t << (2 * mbits);
+  }
+  __device__ __forceinline__ uint32_t operator()(const double* __restrict__ p) const {
+    const double x = __ldg(p), y = __ldg(p + 1);
+    uint32_t qx, qy;
+    if (mint) {  // order keys are linear over the tile's domain: no FP64 arithmetic
+      const int64_t a = (dkey(x) - kx0) >> shx, b = (dkey(y) - ky0) >> shy;
+      qx = (uint32_t)(a < 0 ? 0 : (a > qm ? qm : a));
+      qy = (uint32_t)(b < 0 ? 0 : (b > qm ? qm : b));
+    } else {
+      const float fx = (float)((x - ox) * scale), fy = (float)((y - oy) * scale);
+      qx = (uint32_t)fminf(fmaxf(fx, 0.0f), qmax);
+      qy = (uint32_t)fminf(fmaxf(fy, 0.0f), qmax);
+    }
+    return tile_bits_key | (spread_bits16(qx) << 1) | spread_bits16(qy);
+  }
+};
+
+// Keys of part blockIdx.x of the batch's sort (sort_part_range, contiguous
+// points), with the part's counts of the first radix digit into
+// counts[d * gridDim.x + blockIdx.x].  Each thread finds its tile once and
+// walks forward with the tile's key parameters in registers.
+__global__ void __launch_bounds__(256) k_b_morton_counts(const double* __restrict__ xyz, int64_t n,
+                                                         const int64_t* __restrict__ pt_off,
+                                                         const TileMeta* __restrict__ meta, int ntiles, int mbits,
+                                                         int64_t ntiles_sort, uint32_t* __restrict__ keys,
+                                                         uint32_t* __restrict__ counts) {
+  __shared__ uint32_t h[8][256];
+  for (int i = threadIdx.x; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
+  __syncthreads();
+  int64_t b, e;
+  sort_part_range(n, ntiles_sort, gridDim.x, blockIdx.x, &b, &e);
+  uint32_t* hw = h[threadIdx.x >> 5];
+  int64_t i = b + threadIdx.x;
+  if (i < e) {
+    int t = tile_of(pt_off, ntiles, i);
+    int64_t tend = __ldg(pt_off + t + 1);
+    TileKey key;
+    key.load(meta[t], t, mbits);
+    for (; i < e; i += 256) {
+      while (i >= tend) {  // next tile (tiles are contiguous; empty ones skipped)
+        ++t;
+        tend = __ldg(pt_off + t + 1);
+        key.load(meta[t], t, mbits);
+      }
+      const uint32_t k = key(xyz + 3 * i);
+      keys[i] = k;
+      atomicAdd(hw + (k & 255u), 1u);
+    }
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;
+    uint32_t s = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) s += h[w][d];
+    counts[(int64_t)d * gridDim.x + blockIdx.x] = s;
+  }
+}
+
 // One warp per global leaf: gather its points into sorted order as keys and
 // reduce the leaf summary.
 __global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restrict__ xyz,
@@ -320,6 +398,57 @@ __global__ void k_b_s2_flags(const uint32_t* __restrict__ keys, int64_t n, int i
   }
 }
 
+// Stage 2 of a batch whose tiles all have overlap > 0, by occupancy bitmaps:
+// tile t owns words [bm_off[t], bm_off[t+1]) for its ids 0..n, so emitting
+// the set bits in word order lists the LLPs tile by tile, ids ascending --
+// the (tile, id)-sorted list with every id of run length >= 2 (the first
+// atomic OR of an id's bit returns the old word; a second occurrence sets
+// the bit in `twice`).
+__global__ void k_b_s2_mark(const uint32_t* __restrict__ win, int64_t nw, const int64_t* __restrict__ win_off,
+                            int ntiles, const TileMeta* __restrict__ meta, uint32_t* __restrict__ once,
+                            uint32_t* __restrict__ twice) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = win[i];
+    if (v == kNone) continue;
+    const TileMeta& m = meta[tile_of(win_off, ntiles, i)];
+    if (v > (uint32_t)m.n) continue;  // not an id of the tile (cannot happen)
+    const int64_t idx = m.bm_word * 32 + v;
+    const uint32_t bit = 1u << (idx & 31);
+    const uint32_t old = atomicOr(once + (idx >> 5), bit);
+    if (old & bit) atomicOr(twice + (idx >> 5), bit);
+  }
+}
+
+__global__ void k_b_s2_popc(const uint32_t* __restrict__ bm, int64_t nw, uint32_t* __restrict__ cnt) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x)
+    cnt[w] = (uint32_t)__popc(bm[w]);
+}
+
+__global__ void k_b_s2_emit(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ pos, int64_t nw,
+                            const int64_t* __restrict__ bm_off, int ntiles, int idbits, uint32_t* __restrict__ llp) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t b = bm[w];
+    if (!b) continue;
+    const int t = tile_of(bm_off, ntiles, w);
+    const uint32_t base = (uint32_t)((w - bm_off[t]) * 32);
+    uint32_t p = pos[w];
+    while (b) {
+      llp[p++] = ((uint32_t)t << idbits) | (base + (uint32_t)(__ffs(b) - 1));
+      b &= b - 1;
+    }
+  }
+}
+
+// LLPs per tile: the scanned word counts at the tile's word boundaries.
+__global__ void k_b_s2_tilecount(const uint32_t* __restrict__ pos, const int64_t* __restrict__ bm_off, int ntiles,
+                                 int64_t nw, const uint32_t* __restrict__ total, uint32_t* __restrict__ cnt) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+    const uint32_t a = bm_off[t] < nw ? pos[bm_off[t]] : *total;
+    const uint32_t b = bm_off[t + 1] < nw ? pos[bm_off[t + 1]] : *total;
+    cnt[t] = b - a;
+  }
+}
+
 __global__ void k_b_compact(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ flags,
                             const uint32_t* __restrict__ pos, int64_t n, uint32_t* __restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -408,6 +537,11 @@ struct Plan {
   int tile_bits = 1, mbits = 8, idbits = 1;
   std::vector<TileMeta> meta;
   std::vector<int64_t> pt_off, win_off, cell_off;
+  // stage 2 by bitmaps when every tile has overlap > 0 (ids 0..n per tile, word-aligned)
+  bool s2_bitmap = true;
+  int64_t bm_words = 0;
+  std::vector<int64_t> bm_off;
+  size_t o_bm1 = 0, o_bm2 = 0, o_bmc = 0, o_bmp = 0, o_bmt = 0, o_bmoff = 0;
   std::vector<int32_t> leaf_off, node_off, int_off, ex_off, ey_off, cx_off, cy_off;
   // stage 1 by window classes (when no tile asks for the tree walk)
   struct ClsLayout {
@@ -433,6 +567,9 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
   P->ntiles = ntiles;
   P->meta.resize(ntiles);
   P->pt_off.assign(ntiles + 1, 0);
+  P->bm_off.assign(ntiles + 1, 0);
+  P->s2_bitmap = true;
+  P->bm_words = 0;
   P->win_off.assign(ntiles + 1, 0);
   P->cell_off.assign(ntiles + 1, 0);
   for (auto* v : {&P->leaf_off, &P->node_off, &P->int_off, &P->ex_off, &P->ey_off, &P->cx_off, &P->cy_off})
@@ -498,6 +635,10 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
     m.bsize = (uint16_t)p.bsize;
     m.thr = p.min_num_points;
     m.need_dup = p.overlap > 0.0 ? 1 : 0;
+    if (!m.need_dup) P->s2_bitmap = false;  // overlap 0 keeps every valid minimum: the sort path
+    m.bm_word = P->bm_words;
+    P->bm_off[t] = P->bm_words;
+    P->bm_words += ((int64_t)d.n + 1 + 31) / 32;
     m.win_off = P->nwin;
     m.cell_off = P->ncell;
     m.ex_off = (int32_t)P->ex;
@@ -565,6 +706,7 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
     P->cls_grid_x = std::min(64, (cls_span + 255) / 256);
   }
   P->pt_off[ntiles] = P->npts;
+  P->bm_off[ntiles] = P->bm_words;
   P->leaf_off[ntiles] = (int32_t)P->nleaves;
   P->node_off[ntiles] = (int32_t)P->nnodes;
   P->int_off[ntiles] = (int32_t)P->ninternal;
@@ -609,6 +751,15 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
   P->o_s2p = take((size_t)NW * 4);
   P->o_s2t = take(a256(radix_sort_temp_bytes(NW)) + scan_temp_bytes(std::max(NW, NC)) + 256);
   P->o_llp = take((size_t)NW * 4);
+  if (P->s2_bitmap) {
+    const int64_t BW = std::max<int64_t>(P->bm_words, 1);
+    P->o_bm1 = take((size_t)BW * 4);
+    P->o_bm2 = take((size_t)BW * 4);  // adjacent to o_bm1: one memset clears both
+    P->o_bmc = take((size_t)BW * 4);
+    P->o_bmp = take((size_t)BW * 4);
+    P->o_bmt = take(scan_temp_bytes(BW) + 256);
+    P->o_bmoff = take((size_t)T1 * 8);
+  }
   P->o_mark = take((size_t)NC);
   P->o_cmin = take((size_t)NC * 4);
   P->o_cf = take((size_t)NC * 4);
@@ -717,8 +868,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   // would first wait for this stream's queued point copies, holding the
   // caller (the server's worker) for the whole transfer.
   const size_t T1 = (size_t)ntiles + 1;
-  const size_t stage_need = 16 * 16 + (size_t)ntiles * (sizeof(TileMeta) + 2 * sizeof(QueryJob) + sizeof(ClassArgs)) +
-                            T1 * (8 * 4 + 4 * 7);
+  const size_t stage_need = 20 * 16 + (size_t)ntiles * (sizeof(TileMeta) + 2 * sizeof(QueryJob) + sizeof(ClassArgs)) +
+                            T1 * (8 * 5 + 4 * 7);
   if (stage_cap < stage_need) {
     if (h_stage) cudaFreeHost(h_stage);
     h_stage = nullptr;
@@ -775,6 +926,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   OWM_CUDA_TRY(stage_copy(d_cyoff, P.cy_off.data(), T1 * 4));
   OWM_CUDA_TRY(stage_copy(d_winoff, P.win_off.data(), T1 * 8));
   OWM_CUDA_TRY(stage_copy(d_celloff, P.cell_off.data(), T1 * 8));
+  int64_t* d_bmoff = P.s2_bitmap ? (int64_t*)at(P.o_bmoff) : nullptr;
+  if (P.s2_bitmap) OWM_CUDA_TRY(stage_copy(d_bmoff, P.bm_off.data(), T1 * 8));
 
   // query jobs (host-built: pointers are known here)
   TreeView base_view;
@@ -912,11 +1065,17 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     do {
       if (cudaMemsetAsync(words, 0, 256, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
       const int key_bits = P.tile_bits + 2 * P.mbits;
-      OWM_LAUNCH("k_b_morton", s, k_b_morton<<<gsz(N), 256, 0, s>>>(xyz, N, d_ptoff, d_meta, ntiles, P.mbits, k0));
+      const RadixSortPlan sp = radix_sort_plan(N);
+      if (sp.parts) {  // the Morton pass also counts the sort's first digit
+        OWM_LAUNCH("k_b_morton", s, k_b_morton_counts<<<(unsigned)sp.parts, 256, 0, s>>>(
+            xyz, N, d_ptoff, d_meta, ntiles, P.mbits, sp.ntiles, k0, (uint32_t*)at(P.o_sort)));
+      } else {
+        OWM_LAUNCH("k_b_morton", s, k_b_morton<<<gsz(N), 256, 0, s>>>(xyz, N, d_ptoff, d_meta, ntiles, P.mbits, k0));
+      }
       count_launch(L);
       bool alt = false;
-      if (radix_sort(k0, v0, k1, v1, N, key_bits, true, at(P.o_sort), radix_sort_temp_bytes(N), s, &alt, L) !=
-          cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      if (radix_sort(k0, v0, k1, v1, N, key_bits, true, at(P.o_sort), radix_sort_temp_bytes(N), s, &alt, L,
+                     sp.parts > 0) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
       const uint32_t* mk = alt ? k1 : k0;
       const uint32_t* perm = alt ? v1 : v0;
       // edge tables (before the gather: the class fold needs the window edges)
@@ -984,7 +1143,28 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
         rc2 = OWM_ECUDA;
         break;
       }
-      if (NW > 0) {
+      if (NW > 0 && P.s2_bitmap) {
+        const int64_t BW = P.bm_words;
+        uint32_t* bm1 = (uint32_t*)at(P.o_bm1);
+        uint32_t* bm2 = (uint32_t*)at(P.o_bm2);
+        uint32_t* bmc = (uint32_t*)at(P.o_bmc);
+        uint32_t* bmp = (uint32_t*)at(P.o_bmp);
+        if (cudaMemsetAsync(bm1, 0, (size_t)(P.o_bm2 - P.o_bm1) + (size_t)BW * 4, s) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
+        }
+        OWM_LAUNCH("k_b_s2_mark", s, k_b_s2_mark<<<gsz(NW), 256, 0, s>>>(win, NW, d_winoff, ntiles, d_meta, bm1, bm2));
+        OWM_LAUNCH("k_b_s2_popc", s, k_b_s2_popc<<<gsz(BW), 256, 0, s>>>(bm2, BW, bmc));
+        count_launch(L, 2);
+        if (exclusive_scan_u32(bmc, bmp, BW, words + 1, at(P.o_bmt), scan_temp_bytes(BW) + 256, s, L) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
+        }
+        OWM_LAUNCH("k_b_s2_emit", s, k_b_s2_emit<<<gsz(BW), 256, 0, s>>>(bm2, bmp, BW, d_bmoff, ntiles, P.idbits, llp));
+        OWM_LAUNCH("k_b_s2_tilecount", s, k_b_s2_tilecount<<<(ntiles + 255) / 256, 256, 0, s>>>(bmp, d_bmoff, ntiles, BW,
+                                                                                             words + 1, cnt2));
+        count_launch(L, 2);
+      } else if (NW > 0) {
         OWM_LAUNCH("k_b_s2_keys", s, k_b_s2_keys<<<gsz(NW), 256, 0, s>>>(win, NW, d_winoff, ntiles, P.idbits, none, s2k0));
         count_launch(L);
         bool a2 = false;

@@ -29,6 +29,7 @@ struct TileMeta {
   int32_t pad;
   int64_t win_off, cell_off;
   int32_t ex_off, ey_off, cx_off, cy_off;
+  int64_t bm_word;  // first 32-bit word of the tile's stage-2 bitmaps (ids 0..n)
 };
 
 // Host-side shape of one tile (what a batch signature is made of).
