@@ -684,7 +684,15 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   const int64_t ntiles = std::max<int64_t>(1, (span + kSegBytes - 1) / kSegBytes);  // segments
   // newline positions in [begin, data_off) must not count: the count runs from data_off
   // itself, so tiles use the exact byte range [data_off, nbytes)
-  DeviceBuffer tmp;
+  // working buffers, released on every return (early CUDA-error returns included)
+  DeviceBuffer tmp, vbuf, work;
+  struct Release {
+    DeviceBuffer* b[3];
+    cudaStream_t s;
+    ~Release() {
+      for (DeviceBuffer* x : b) x->release(s);
+    }
+  } release_all{{&tmp, &vbuf, &work}, s};
   const size_t tb = a256((size_t)ntiles * 4) * 2 + a256(scan_temp_bytes(ntiles)) + 256;
   rc = tmp.reserve(tb, s);
   if (rc) return rc;
@@ -712,28 +720,17 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   char last = '\n';
   if (nbytes > data_off) OWM_CUDA_TRY(cudaMemcpy(&last, dtext + nbytes - 1, 1, cudaMemcpyDeviceToHost));
   const int64_t nlines = nl + (nbytes > data_off && last != '\n' ? 1 : 0);
-  if (nlines <= 0) {
-    tmp.release(s);
-    return OWM_EIO;
-  }
+  if (nlines <= 0) return OWM_EIO;
   // line starts: starts[0] = data_off; starts[k] (k >= 1) after the k-th data newline
   // (k_nl_starts numbers newlines from begin, so its index is shifted by hdr_nl)
   // per-line values in their own buffer: when the first n lines are all
   // points it becomes the cloud as it is (no compaction)
-  DeviceBuffer vbuf;
   rc = vbuf.reserve((size_t)nlines * 24 + kXyzSlack, s);
-  if (rc) {
-    tmp.release(s);
-    return rc;
-  }
+  if (rc) return rc;
   const size_t lb = a256((size_t)(nlines + 1 + hdr_nl + 1) * 8) + a256((size_t)nlines) +
                     2 * a256((size_t)nlines * 4) + a256((size_t)nlines * 8) + a256(scan_temp_bytes(nlines)) + 1024;
-  DeviceBuffer work;
   rc = work.reserve(lb, s);
-  if (rc) {
-    tmp.release(s);
-    return rc;
-  }
+  if (rc) return rc;
   char* wp = static_cast<char*>(work.ptr);
   auto take = [&](size_t b) {
     void* q = wp;
@@ -805,9 +802,6 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
     }
   }
   OWM_CUDA_TRY(cudaStreamSynchronize(s));
-  vbuf.release(s);
-  work.release(s);
-  tmp.release(s);
   if (!rc) *n_out = n;
   return rc;
 }
