@@ -182,3 +182,22 @@ def test_parsed_cloud_runs_the_path(owm, ctx):
     np.testing.assert_array_equal(ctx.run(a, cfg), ctx.run(b, cfg))
     a.close()
     b.close()
+
+
+def test_load_file_larger_than_a_staging_chunk(owm, ctx, tmp_path):
+    """A file of several 64 MB staging chunks: the chunked read / copy
+    pipeline gives the exact values (the generator's X / 1000.0 etc.)."""
+    import importlib.util
+    from pathlib import Path
+
+    spec = importlib.util.spec_from_file_location("bench", Path(__file__).resolve().parents[1] / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    text, pts = bench.lidar_text(2_700_000, 3)  # 84 MB: two chunks
+    f = tmp_path / "big.xyz"
+    f.write_bytes(text.tobytes())
+    assert f.stat().st_size > (64 << 20)
+    c = ctx.cloud_load_xyz(f)
+    got = c.points()
+    c.close()
+    np.testing.assert_array_equal(got.view(np.uint64), pts.view(np.uint64))
