@@ -409,7 +409,8 @@ __device__ int parse_field(TextCursor& tc, int64_t p, double* v, int64_t* end, B
       w *= 10;
       --e;
     }
-    if (e >= -22 && e <= 22) {  // Clinger: one correctly rounded IEEE multiply or divide of exact operands
+    if (e >= -22 && e <= 22) {
+      // Clinger: one correctly rounded IEEE multiply or divide of exact operands
       const double x = u53_to_double(w);
       const double r = e >= 0 ? __dmul_rn(x, c_pow10[e - kPowMin]) : __ddiv_rn(x, c_pow10[-e - kPowMin]);
       *v = neg ? -r : r;
