@@ -70,6 +70,14 @@ struct TextCursor {
   }
 };
 
+// The same view of text staged in shared memory: bytes [origin, ...) of the
+// text at base.
+struct SmemCursor {
+  const unsigned char* base;
+  int64_t origin, end;
+  __device__ __forceinline__ uint32_t at(int64_t p) const { return p < end ? (uint32_t)base[p - origin] : 0u; }
+};
+
 __device__ __forceinline__ bool is_space(uint32_t c) { return c == ' ' || (c >= 9 && c <= 13); }
 __device__ __forceinline__ bool is_digit(uint32_t c) { return c - '0' < 10u; }
 __device__ __forceinline__ int hex_val(uint32_t c) {
@@ -206,14 +214,15 @@ constexpr int kFieldOk = 0, kFieldFail = 1, kFieldNonFinite = 2, kFieldSlow = 3;
 
 struct Decimal {
   uint64_t w;     // first (up to) 19 significant digits
-  int64_t nd;     // significant digits in all
-  int64_t dexp;   // value = (w + fraction of the dropped digits) * 10^dexp
+  int32_t nd;     // significant digits in all (a line is shorter than 2^31 bytes)
+  int32_t dexp;   // value = (w + fraction of the dropped digits) * 10^dexp (|exponent| saturates at 10^8)
   bool sticky;    // a dropped digit is nonzero
 };
 
 // Exact decimal conversion of the mantissa at [ms, me) (digits and at most
 // one '.') times 10^ev; `dec` is its 19-digit summary.
-__device__ double exact_decimal(TextCursor& tc, int64_t ms, int64_t me, int64_t ev, const Decimal& dec, bool neg,
+template <class Cursor>
+__device__ double exact_decimal(Cursor& tc, int64_t ms, int64_t me, int64_t ev, const Decimal& dec, bool neg,
                                 Big* big) {
   const uint64_t sign = neg ? 0x8000000000000000ull : 0ull;
   const int64_t lead = (dec.nd < 19 ? dec.nd : 19) - 1 + dec.dexp;  // value in [10^lead, 10^(lead+1))
@@ -291,8 +300,8 @@ __device__ double exact_decimal(TextCursor& tc, int64_t ms, int64_t me, int64_t 
 // *v and *end are set.  kExact: decimal fields that need the slow path are
 // converted here (big = 3 scratch integers); otherwise they report
 // kFieldSlow.
-template <bool kExact>
-__device__ int parse_field(TextCursor& tc, int64_t p, double* v, int64_t* end, Big* big) {
+template <bool kExact, class Cursor>
+__device__ int parse_field(Cursor& tc, int64_t p, double* v, int64_t* end, Big* big) {
   bool neg = false;
   uint32_t c = tc.at(p);
   if (c == '+' || c == '-') {
@@ -422,10 +431,10 @@ __device__ int parse_field(TextCursor& tc, int64_t p, double* v, int64_t* end, B
   return isfinite(*v) ? kFieldOk : kFieldNonFinite;
 }
 
-// sscanf(line, "%lf %lf %lf") and owm_xyz_read's verdict on the line.
-template <bool kExact>
-__device__ int parse_line(const char* text, int64_t s, int64_t e, double* out, Big* big) {
-  TextCursor tc(text, e);
+// sscanf(line, "%lf %lf %lf") and owm_xyz_read's verdict on the line
+// [s, e) read through tc.
+template <bool kExact, class Cursor>
+__device__ int parse_line(Cursor& tc, int64_t s, double* out, Big* big) {
   int64_t p = s;
   int f = 0;
 #pragma unroll
@@ -434,7 +443,7 @@ __device__ int parse_line(const char* text, int64_t s, int64_t e, double* out, B
     while ((c = tc.at(p)) != 0 && is_space(c)) ++p;
     if (c == 0) break;
     int64_t end;
-    const int r = parse_field<kExact>(tc, p, out + f, &end, big);
+    const int r = parse_field<kExact, Cursor>(tc, p, out + f, &end, big);
     if (r == kFieldSlow) return kLineSlow;
     if (r == kFieldNonFinite) return kLineError;
     if (r == kFieldFail) break;
@@ -535,20 +544,49 @@ struct ParseOut {
 };
 
 // One thread per line i: [starts[i], starts[i+1] - 1) (the newline excluded).
+// A warp takes 32 consecutive lines: their text is one contiguous span, which
+// the warp stages in shared memory with coalesced 16-byte loads, so every
+// lane then reads its line a byte per load (spans over kStageBytes are read
+// from global memory instead).
+constexpr int kStageBytes = 4096;
+
 __global__ void __launch_bounds__(256) k_parse(const char* __restrict__ text, const int64_t* __restrict__ starts,
-                                               int64_t nlines, ParseOut o) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlines;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double v[3];
-    const int st = parse_line<false>(text, starts[i], starts[i + 1] - 1, v, nullptr);
-    o.status[i] = (uint8_t)st;
-    if (st == kLinePoint) {
-      o.vals[3 * i] = v[0];
-      o.vals[3 * i + 1] = v[1];
-      o.vals[3 * i + 2] = v[2];
-    } else if (st == kLineSlow) {
-      o.slow[atomicAdd(o.nslow, 1ull)] = i;
+                                               int64_t nlines, int64_t nbytes, ParseOut o) {
+  __shared__ __align__(16) unsigned char stage[8][kStageBytes];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t l0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; l0 < nlines; l0 += nwarps * 32) {
+    const int64_t l1 = l0 + 32 < nlines ? l0 + 32 : nlines;
+    const int64_t b0 = starts[l0] & ~(int64_t)15;  // 16-byte aligned start of the span
+    const int64_t b1 = starts[l1] - 1 < nbytes ? starts[l1] - 1 : nbytes;  // end of the last line
+    const bool staged = b1 - b0 <= kStageBytes;     // warp-uniform
+    if (staged) {
+      for (int64_t q = b0 + lane * 16; q < b1; q += 512)  // q - b0 <= kStageBytes - 16
+        *reinterpret_cast<uint4*>(stage[wib] + (q - b0)) = __ldg(reinterpret_cast<const uint4*>(text + q));
+      __syncwarp();
     }
+    const int64_t i = l0 + lane;
+    if (i < nlines) {
+      const int64_t s = starts[i], e = starts[i + 1] - 1;
+      double v[3];
+      int st;
+      if (staged) {
+        SmemCursor tc{stage[wib], b0, e};
+        st = parse_line<false>(tc, s, v, nullptr);
+      } else {
+        TextCursor tc(text, e);
+        st = parse_line<false>(tc, s, v, nullptr);
+      }
+      o.status[i] = (uint8_t)st;
+      if (st == kLinePoint) {
+        o.vals[3 * i] = v[0];
+        o.vals[3 * i + 1] = v[1];
+        o.vals[3 * i + 2] = v[2];
+      } else if (st == kLineSlow) {
+        o.slow[atomicAdd(o.nslow, 1ull)] = i;
+      }
+    }
+    __syncwarp();  // the stage is refilled in the next round
   }
 }
 
@@ -561,7 +599,8 @@ __global__ void __launch_bounds__(128) k_parse_slow(const char* __restrict__ tex
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = o.slow[k];
     double v[3];
-    const int st = parse_line<true>(text, starts[i], starts[i + 1] - 1, v, big);
+    TextCursor tc(text, starts[i + 1] - 1);
+    const int st = parse_line<true>(tc, starts[i], v, big);
     o.status[i] = (uint8_t)st;
     if (st == kLinePoint) {
       o.vals[3 * i] = v[0];
@@ -755,7 +794,7 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   const unsigned long long init[2] = {0ull, ~0ull};
   OWM_CUDA_TRY(cudaMemcpyAsync(dwords, init, 16, cudaMemcpyHostToDevice, s));
   ParseOut po{vals, status, slow, dwords};
-  OWM_LAUNCH("k_parse", s, k_parse<<<grid_of(nlines, 256), 256, 0, s>>>(dtext, starts, nlines, po));
+  OWM_LAUNCH("k_parse", s, k_parse<<<grid_of((nlines + 31) / 32 * 32, 256), 256, 0, s>>>(dtext, starts, nlines, nbytes, po));
   OWM_LAUNCH("k_parse_slow", s, k_parse_slow<<<152 * 2, 128, 0, s>>>(dtext, starts, po));
   OWM_LAUNCH("k_line_flags", s, k_line_flags<<<grid_of(nlines, 256), 256, 0, s>>>(status, nlines, is_point, dwords + 1));
   count_launch(launches, 3);
