@@ -52,6 +52,7 @@ __constant__ double c_pow10[kPowMax - kPowMin + 1];  // correctly rounded 10^k, 
 // Byte p of the line being parsed, through one cached 16-byte word; 0 past
 // the line's end (a NUL byte also ends what sscanf sees).
 struct TextCursor {
+  using Pos = int64_t;  // positions in the text
   const uint4* __restrict__ base;
   int64_t end;
   int64_t wi;
@@ -73,9 +74,10 @@ struct TextCursor {
 // The same view of text staged in shared memory: bytes [origin, ...) of the
 // text at base.
 struct SmemCursor {
+  using Pos = int32_t;  // positions relative to the start of the staged span
   const unsigned char* base;
-  int64_t origin, end;
-  __device__ __forceinline__ uint32_t at(int64_t p) const { return p < end ? (uint32_t)base[p - origin] : 0u; }
+  int32_t end;
+  __device__ __forceinline__ uint32_t at(int32_t p) const { return p < end ? (uint32_t)base[p] : 0u; }
 };
 
 __device__ __forceinline__ bool is_space(uint32_t c) { return c == ' ' || (c >= 9 && c <= 13); }
@@ -222,7 +224,8 @@ struct Decimal {
 // Exact decimal conversion of the mantissa at [ms, me) (digits and at most
 // one '.') times 10^ev; `dec` is its 19-digit summary.
 template <class Cursor>
-__device__ double exact_decimal(Cursor& tc, int64_t ms, int64_t me, int64_t ev, const Decimal& dec, bool neg,
+__device__ double exact_decimal(Cursor& tc, typename Cursor::Pos ms, typename Cursor::Pos me, int64_t ev,
+                                const Decimal& dec, bool neg,
                                 Big* big) {
   const uint64_t sign = neg ? 0x8000000000000000ull : 0ull;
   const int64_t lead = (dec.nd < 19 ? dec.nd : 19) - 1 + dec.dexp;  // value in [10^lead, 10^(lead+1))
@@ -234,7 +237,7 @@ __device__ double exact_decimal(Cursor& tc, int64_t ms, int64_t me, int64_t ev, 
   int64_t nd = 0, E = 0;
   bool seen_dot = false, sticky = false;
   uint32_t chunk = 0, cmul = 1;
-  for (int64_t p = ms; p < me; ++p) {
+  for (typename Cursor::Pos p = ms; p < me; ++p) {
     const uint32_t c = tc.at(p);
     if (c == '.') {
       seen_dot = true;
@@ -301,7 +304,7 @@ __device__ double exact_decimal(Cursor& tc, int64_t ms, int64_t me, int64_t ev, 
 // converted here (big = 3 scratch integers); otherwise they report
 // kFieldSlow.
 template <bool kExact, class Cursor>
-__device__ int parse_field(Cursor& tc, int64_t p, double* v, int64_t* end, Big* big) {
+__device__ int parse_field(Cursor& tc, typename Cursor::Pos p, double* v, typename Cursor::Pos* end, Big* big) {
   bool neg = false;
   uint32_t c = tc.at(p);
   if (c == '+' || c == '-') {
@@ -362,7 +365,7 @@ __device__ int parse_field(Cursor& tc, int64_t p, double* v, int64_t* end, Big* 
     return isfinite(*v) ? kFieldOk : kFieldNonFinite;
   }
   // decimal: [digits][. [digits]] with at least one digit, then e[+-][digits]
-  const int64_t ms = p;
+  const typename Cursor::Pos ms = p;
   Decimal dec{0, 0, 0, false};
   bool any = false, seen_dot = false;
   for (;;) {
@@ -390,7 +393,7 @@ __device__ int parse_field(Cursor& tc, int64_t p, double* v, int64_t* end, Big* 
     }
   }
   if (!any) return kFieldFail;
-  const int64_t me = p;
+  const typename Cursor::Pos me = p;
   int64_t ev = 0;
   if ((tc.at(p) | 0x20u) == 'e') {
     c = tc.at(++p);
@@ -434,15 +437,15 @@ __device__ int parse_field(Cursor& tc, int64_t p, double* v, int64_t* end, Big* 
 // sscanf(line, "%lf %lf %lf") and owm_xyz_read's verdict on the line
 // [s, e) read through tc.
 template <bool kExact, class Cursor>
-__device__ int parse_line(Cursor& tc, int64_t s, double* out, Big* big) {
-  int64_t p = s;
+__device__ int parse_line(Cursor& tc, typename Cursor::Pos s, double* out, Big* big) {
+  typename Cursor::Pos p = s;
   int f = 0;
 #pragma unroll
   for (; f < 3; ++f) {
     uint32_t c;
     while ((c = tc.at(p)) != 0 && is_space(c)) ++p;
     if (c == 0) break;
-    int64_t end;
+    typename Cursor::Pos end;
     const int r = parse_field<kExact, Cursor>(tc, p, out + f, &end, big);
     if (r == kFieldSlow) return kLineSlow;
     if (r == kFieldNonFinite) return kLineError;
@@ -571,8 +574,8 @@ __global__ void __launch_bounds__(256) k_parse(const char* __restrict__ text, co
       double v[3];
       int st;
       if (staged) {
-        SmemCursor tc{stage[wib], b0, e};
-        st = parse_line<false>(tc, s, v, nullptr);
+        SmemCursor tc{stage[wib], (int32_t)(e - b0)};
+        st = parse_line<false>(tc, (int32_t)(s - b0), v, nullptr);
       } else {
         TextCursor tc(text, e);
         st = parse_line<false>(tc, s, v, nullptr);
