@@ -138,6 +138,35 @@ __device__ __forceinline__ double u53_to_double(uint64_t w) {
   return __longlong_as_double((long long)(((uint64_t)(1085 - lz) << 52) + ((w << lz) >> 11)));
 }
 
+// ---- w / 10^k with one multiply and an exact residual -------------------------------
+// For an integer w <= 2^53 and 1 <= k <= 22, q0 = RN(w * RN(10^-k)) lies within
+// 1.5 units in the last place of q* = w / 10^k.  With q0 = M * 2^E (E + k < 0
+// here), w - 10^k * q0 = 2^(E+k) * I for an integer |I| <= 2.5 * 5^k < 2^53
+// (also after a step of one unit), so the FMA residual
+// rem = fma(-q0, 10^k, w) is exact and rem / 10^k = q* - q0.  Half a unit of
+// q0 is 10^k * 2^(E-1) in residual terms (a power-of-two multiple of 10^k:
+// exact); comparing |rem| with it as bit patterns (positive doubles order like
+// their bits) moves q0 to the correctly rounded quotient, ties to even.  Two
+// FP64 operations per step instead of a divide: on GB300 the FP64 pipe is the
+// parse kernel's limit.
+__device__ __forceinline__ double div_pow10_fma(uint64_t w, double dk, double rk) {
+  const double x = u53_to_double(w);
+  uint64_t qb = (uint64_t)__double_as_longlong(__dmul_rn(x, rk));
+  const uint64_t db = (uint64_t)__double_as_longlong(dk);
+  for (int it = 0; it < 4; ++it) {
+    const double q = __longlong_as_double((long long)qb);
+    const uint64_t rb = (uint64_t)__double_as_longlong(__fma_rn(-q, dk, x));
+    const uint64_t ra = rb & 0x7FFFFFFFFFFFFFFFull;
+    const uint64_t hb = db + ((uint64_t)((int64_t)(qb >> 52) - 1076) << 52);  // q is normal (q* >= 10^-22)
+    const bool below = (rb >> 63) != 0;  // q > q*
+    // the interval below a power of two is half as wide
+    const uint64_t h = (below && !(qb & 0xFFFFFFFFFFFFFull)) ? hb - (1ull << 52) : hb;
+    if (ra < h || (ra == h && !(qb & 1))) break;
+    qb += below ? ~0ull : 1ull;  // one double towards q* (ties towards the even neighbour)
+  }
+  return __longlong_as_double((long long)qb);
+}
+
 // ---- big integers for the exact decimal path ----------------------------------
 constexpr int kBigWords = 160;    // 5120 bits: decimal significands of up to 800 digits, scaled
 constexpr int kMaxBigDigits = 800;
@@ -422,9 +451,10 @@ __device__ int parse_field(Cursor& tc, typename Cursor::Pos p, double* v, typena
       --e;
     }
     if (e >= -22 && e <= 22) {
-      // Clinger: one correctly rounded IEEE multiply or divide of exact operands
-      const double x = u53_to_double(w);
-      const double r = e >= 0 ? __dmul_rn(x, c_pow10[e - kPowMin]) : __ddiv_rn(x, c_pow10[-e - kPowMin]);
+      // e >= 0: one correctly rounded multiply of exact operands (Clinger);
+      // e < 0: the quotient from an exact residual (div_pow10_fma)
+      const double r = e >= 0 ? __dmul_rn(u53_to_double(w), c_pow10[e - kPowMin])
+                              : div_pow10_fma(w, c_pow10[-e - kPowMin], c_pow10[e - kPowMin]);
       *v = neg ? -r : r;
       return isfinite(r) ? kFieldOk : kFieldNonFinite;
     }
@@ -553,7 +583,7 @@ struct ParseOut {
 // from global memory instead).
 constexpr int kStageBytes = 4096;
 
-__global__ void __launch_bounds__(256) k_parse(const char* __restrict__ text, const int64_t* __restrict__ starts,
+__global__ void __launch_bounds__(256, 4) k_parse(const char* __restrict__ text, const int64_t* __restrict__ starts,
                                                int64_t nlines, int64_t nbytes, ParseOut o) {
   __shared__ __align__(16) unsigned char stage[8][kStageBytes];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
