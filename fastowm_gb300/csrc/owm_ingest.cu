@@ -574,6 +574,8 @@ struct ParseOut {
   uint8_t* status;          // [nlines]
   int64_t* slow;            // queued line indices
   unsigned long long* nslow;
+  unsigned long long* first_error;  // lowest error line (atomic min)
+  unsigned long long* nblank;       // blank lines
 };
 
 // One thread per line i: [starts[i], starts[i+1] - 1) (the newline excluded).
@@ -599,10 +601,10 @@ __global__ void __launch_bounds__(256, 4) k_parse(const char* __restrict__ text,
       __syncwarp();
     }
     const int64_t i = l0 + lane;
+    int st = -1;
     if (i < nlines) {
       const int64_t s = starts[i], e = starts[i + 1] - 1;
       double v[3];
-      int st;
       if (staged) {
         SmemCursor tc{stage[wib], (int32_t)(e - b0)};
         st = parse_line<false>(tc, (int32_t)(s - b0), v, nullptr);
@@ -617,8 +619,12 @@ __global__ void __launch_bounds__(256, 4) k_parse(const char* __restrict__ text,
         o.vals[3 * i + 2] = v[2];
       } else if (st == kLineSlow) {
         o.slow[atomicAdd(o.nslow, 1ull)] = i;
+      } else if (st == kLineError) {
+        atomicMin(o.first_error, (unsigned long long)i);
       }
     }
+    const uint32_t blank = __ballot_sync(0xffffffffu, st == kLineBlank);
+    if (lane == 0 && blank) atomicAdd(o.nblank, (unsigned long long)__popc(blank));
     __syncwarp();  // the stage is refilled in the next round
   }
 }
@@ -639,6 +645,8 @@ __global__ void __launch_bounds__(128) k_parse_slow(const char* __restrict__ tex
       o.vals[3 * i] = v[0];
       o.vals[3 * i + 1] = v[1];
       o.vals[3 * i + 2] = v[2];
+    } else {
+      atomicMin(o.first_error, (unsigned long long)i);  // a queued line is a point or an error
     }
   }
 }
@@ -824,27 +832,36 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   const int64_t first = data_off, endpos = nbytes + 1;
   OWM_CUDA_TRY(cudaMemcpyAsync(starts, &first, 8, cudaMemcpyHostToDevice, s));
   if (nlines > nl) OWM_CUDA_TRY(cudaMemcpyAsync(starts + nlines, &endpos, 8, cudaMemcpyHostToDevice, s));
-  const unsigned long long init[2] = {0ull, ~0ull};
-  OWM_CUDA_TRY(cudaMemcpyAsync(dwords, init, 16, cudaMemcpyHostToDevice, s));
-  ParseOut po{vals, status, slow, dwords};
+  const unsigned long long init[3] = {0ull, ~0ull, 0ull};  // queued lines, first error line, blank lines
+  OWM_CUDA_TRY(cudaMemcpyAsync(dwords, init, 24, cudaMemcpyHostToDevice, s));
+  ParseOut po{vals, status, slow, dwords, dwords + 1, dwords + 2};
   OWM_LAUNCH("k_parse", s, k_parse<<<grid_of((nlines + 31) / 32 * 32, 256), 256, 0, s>>>(dtext, starts, nlines, nbytes, po));
   OWM_LAUNCH("k_parse_slow", s, k_parse_slow<<<152 * 2, 128, 0, s>>>(dtext, starts, po));
-  OWM_LAUNCH("k_line_flags", s, k_line_flags<<<grid_of(nlines, 256), 256, 0, s>>>(status, nlines, is_point, dwords + 1));
-  count_launch(launches, 3);
-  uint32_t* d_npts = reinterpret_cast<uint32_t*>(c->d_small + kCountSlot);
-  OWM_CUDA_TRY(exclusive_scan_u32(is_point, pos, nlines, d_npts, ctemp, scan_temp_bytes(nlines), s, launches));
-  unsigned long long h[2];
-  uint32_t npts = 0;
-  OWM_CUDA_TRY(cudaMemcpyAsync(h, dwords, 16, cudaMemcpyDeviceToHost, s));
-  OWM_CUDA_TRY(cudaMemcpyAsync(&npts, d_npts, 4, cudaMemcpyDeviceToHost, s));
+  count_launch(launches, 2);
+  unsigned long long h[3];
+  OWM_CUDA_TRY(cudaMemcpyAsync(h, dwords, 24, cudaMemcpyDeviceToHost, s));
   OWM_CUDA_TRY(cudaStreamSynchronize(s));
   // points before the first error line: the loader stops at that line unless
-  // the declared count was reached before it
+  // the declared count was reached before it.  Without blank lines every line
+  // before it is a point; with blank lines the point flags are scanned.
+  const bool scanned = h[2] != 0;
+  int64_t npts = h[1] != ~0ull ? (int64_t)h[1] : nlines;
   int64_t before = npts;
-  if (h[1] != ~0ull) {
-    uint32_t pb = 0;
-    OWM_CUDA_TRY(cudaMemcpy(&pb, pos + h[1], 4, cudaMemcpyDeviceToHost));
-    before = pb;
+  if (scanned) {
+    OWM_LAUNCH("k_line_flags", s, k_line_flags<<<grid_of(nlines, 256), 256, 0, s>>>(status, nlines, is_point, dwords + 1));
+    count_launch(launches);
+    uint32_t* d_npts = reinterpret_cast<uint32_t*>(c->d_small + kCountSlot);
+    OWM_CUDA_TRY(exclusive_scan_u32(is_point, pos, nlines, d_npts, ctemp, scan_temp_bytes(nlines), s, launches));
+    uint32_t np = 0;
+    OWM_CUDA_TRY(cudaMemcpyAsync(&np, d_npts, 4, cudaMemcpyDeviceToHost, s));
+    OWM_CUDA_TRY(cudaStreamSynchronize(s));
+    npts = np;
+    before = np;
+    if (h[1] != ~0ull) {
+      uint32_t pb = 0;
+      OWM_CUDA_TRY(cudaMemcpy(&pb, pos + h[1], 4, cudaMemcpyDeviceToHost));
+      before = pb;
+    }
   }
   int64_t n;
   if (declared >= 0) {
@@ -856,8 +873,10 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   }
   if (!rc && (n <= 0 || n >= 0x7FFFFFFFLL)) rc = OWM_EIO;
   bool in_place = false;  // the first n lines are all points
-  if (!rc && n <= nlines) {
-    uint32_t pn = npts;
+  if (!rc && !scanned) {
+    in_place = n <= before;  // no blank line: lines before the first error are points
+  } else if (!rc && n <= nlines) {
+    uint32_t pn = (uint32_t)npts;
     if (n < nlines) OWM_CUDA_TRY(cudaMemcpy(&pn, pos + n, 4, cudaMemcpyDeviceToHost));
     in_place = (int64_t)pn == n;
   }
