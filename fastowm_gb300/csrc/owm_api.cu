@@ -143,9 +143,7 @@ int tree_alloc(TreeStore* t, DeviceBuffer* mem, int64_t n, const owm_tree_cfg& c
 int validate_tree_cfg(const owm_tree_cfg* cfg) {
   if (!cfg) return OWM_EINVAL;
   if (cfg->policy == OWM_TREE_MAX_NUMBER) {
-    int m = cfg->max_number;
-    if (m < 1 || m > 256 || (m & (m - 1)) != 0) return OWM_EINVAL;
-    return OWM_OK;
+    return cfg->max_number >= 1 ? OWM_OK : OWM_EINVAL;  // any capacity; leaves use leaf_size()
   }
   if (cfg->policy == OWM_TREE_MIN_RADIUS) return cfg->min_radius > 0.0f && std::isfinite(cfg->min_radius) ? OWM_OK : OWM_EINVAL;
   return OWM_EINVAL;

@@ -605,7 +605,7 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
     std::memset(&m, 0, sizeof(m));
     m.pt_off = P->npts;
     m.n = (int32_t)d.n;
-    m.leaf = br.leaf_for(d.n, d.cfg.tree.max_number);
+    m.leaf = leaf_size(br.leaf_for(d.n, d.cfg.tree.max_number));
     int32_t nl = (int32_t)((d.n + m.leaf - 1) / m.leaf);
     m.leaf_off = (int32_t)P->nleaves;
     m.nleaves = nl;

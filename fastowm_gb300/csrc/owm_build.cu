@@ -498,7 +498,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   const uint32_t* mk = alt ? k1 : k0;
   const uint32_t* perm = alt ? v1 : v0;
 
-  int32_t L = cfg.max_number;
+  int32_t L = leaf_size(cfg.max_number);
   int32_t nl;
   const int32_t* lstarts = nullptr;
   bool fixed = cfg.policy == OWM_TREE_MAX_NUMBER;
@@ -546,7 +546,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
       case 128: launch_gather_leaves<128>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
       case 256: launch_gather_leaves<256>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
       default:
-        return OWM_EINVAL;  // the API only admits powers of two up to 256
+        return OWM_EINVAL;  // unreachable: leaf_size() gives powers of two up to 256
     }
     count_launch(launches);
     if (fused && cls) *fused = true;

@@ -33,9 +33,21 @@ struct TreeStore {
   }
 };
 
+// Leaf size of the max-number policy: the largest power of two not above
+// max_number (nor above 256, the largest leaf the gather is built for), so
+// every leaf holds at most max_number points.  The seeds do not depend on it;
+// the reference's maxNumber takes any value.
+constexpr int32_t kMaxLeaf = 256;
+inline int32_t leaf_size(int32_t max_number) {
+  int32_t L = 1;
+  while (L * 2 <= max_number && L * 2 <= kMaxLeaf) L *= 2;
+  return L;
+}
+
 // Node slots needed for n points under a tree configuration.
 inline int64_t tree_node_cap(int64_t n, const owm_tree_cfg& cfg) {
-  int64_t nl = cfg.policy == OWM_TREE_MAX_NUMBER ? (n + cfg.max_number - 1) / cfg.max_number : n;
+  const int64_t L = leaf_size(cfg.max_number);
+  int64_t nl = cfg.policy == OWM_TREE_MAX_NUMBER ? (n + L - 1) / L : n;
   return 2 * nl - 1;
 }
 

@@ -172,7 +172,9 @@ int owm_cloud_load_xyz(owm_ctx* ctx, const char* path, owm_cloud** out);
 
 typedef struct {
   int32_t policy;     /* OWM_TREE_MAX_NUMBER or OWM_TREE_MIN_RADIUS */
-  int32_t max_number; /* leaf capacity, 1..1024 (reference -s, default 32) */
+  int32_t max_number; /* leaf capacity, any value >= 1 (reference -s, default 32); leaves
+                         hold at most this many points: the largest power of two not
+                         above it, up to 256 (the seeds do not depend on it) */
   float min_radius;   /* reference -r, default 0.1 */
   int32_t level;      /* reference -L (CPU task split level); accepted, unused */
 } owm_tree_cfg;

@@ -47,7 +47,7 @@ def test_async_runs_equal_sync(owm, ctx):
 def test_async_failed_submit_leaves_context_usable(owm, ctx):
     a = _cloud(owm, 200_000, 13)
     xyz, bb, cfg = a
-    bad = owm.run_cfg(cfg.wsize, cfg.overlap, cfg.bsize, 3)  # leaf size must be a power of two
+    bad = owm.run_cfg(cfg.wsize, cfg.overlap, cfg.bsize, 0)  # a leaf capacity below 1 is invalid
     with pytest.raises(owm.OwmError) as e:
         ctx.run_host_submit(xyz, bb, bad)
     assert e.value.status == -1  # OWM_EINVAL, after the copy was queued: submit waited for it

@@ -82,7 +82,8 @@ def test_config3_ties_holes_strips(owm, oracle, ctx, overlap):
 
 
 @pytest.mark.parametrize("policy,mn,mr", [(1, 1, 0.1), (1, 4, 0.1), (1, 16, 0.1), (1, 64, 0.1), (1, 128, 0.1),
-                                          (1, 256, 0.1), (0, 32, 0.1), (0, 32, 0.5), (0, 32, 3.0)])
+                                          (1, 256, 0.1), (1, 3, 0.1), (1, 100, 0.1), (1, 1000, 0.1),
+                                          (0, 32, 0.1), (0, 32, 0.5), (0, 32, 3.0)])
 def test_tree_policies_same_result(owm, oracle, ctx, policy, mn, mr):
     xyz, bb, W, Ov, B, _ = _cloud(owm, 1, n=150_000, w=70, h=90)
     got, want, _ = _run_both(owm, oracle, ctx, xyz, bb, W, Ov, B, mn, policy, mr)
