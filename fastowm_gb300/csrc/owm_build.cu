@@ -395,9 +395,10 @@ bool morton_int_shifts(double lo, double hi, int bits, int64_t* klo, int* shift)
   return true;
 }
 
-int choose_key_bits(int64_t n, int policy, double side, float min_radius) {
-  int b = n <= (1 << 18) ? 8 : 12;
+int choose_key_bits(int64_t n, int policy, double side, float min_radius, int32_t leaf) {
+  int b;
   if (policy == OWM_TREE_MIN_RADIUS && min_radius > 0.0f) {
+    b = n <= (1 << 18) ? 8 : 12;
     // quadtree depth where half-side <= 2*min_radius (insertPoint's split
     // rule, optim3_func.cpp:107: split while radius*0.5 > minRadius)
     double r = side * 0.5;
@@ -407,6 +408,14 @@ int choose_key_bits(int64_t n, int policy, double side, float min_radius) {
       ++d;
     }
     if (d > b) b = d <= 12 ? 12 : 16;
+  } else {
+    // Leaves are runs of `leaf` points in key order.  The fewest bits per
+    // axis (8..12) that leave at most half a leaf of points per finest cell
+    // of an evenly spread cloud keep every leaf compact; fewer key bits make
+    // the last sort digit narrower (20 bits: 8 + 8 + 4).
+    const int64_t per_cell = std::max<int32_t>(leaf / 2, 1);
+    b = 8;
+    while (b < 12 && n > per_cell * ((int64_t)1 << (2 * b))) ++b;
   }
   return 2 * b;
 }
@@ -460,7 +469,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   double R = rx >= ry ? rx : ry;
   if (!(R > 0.0)) R = 0.5;
   double ox = bb.min_x + rx - R, oy = bb.min_y + ry - R;
-  int key_bits = choose_key_bits(n, cfg.policy, 2.0 * R, cfg.min_radius);
+  int key_bits = choose_key_bits(n, cfg.policy, 2.0 * R, cfg.min_radius, leaf_size(cfg.max_number));
   int bits_axis = key_bits / 2;
   double scale = (double)(1u << bits_axis) / (2.0 * R);
   t->ox = bb.min_x;  // float boxes are offsets from the bbox corner

@@ -55,7 +55,7 @@ size_t tree_scratch_bytes(int64_t n);
 // Integer Morton quantisation of [lo, hi]: true (and the key origin and
 // shift) when lo, hi > 0 share their exponent, so order keys are linear.
 bool morton_int_shifts(double lo, double hi, int bits, int64_t* klo, int* shift);
-int choose_key_bits(int64_t n, int policy, double side, float min_radius);
+int choose_key_bits(int64_t n, int policy, double side, float min_radius, int32_t leaf);
 
 // Builds the tree of n device points (AoS xyz, 16-byte aligned, kXyzSlack
 // readable bytes after the last point) into t (whose arrays must be allocated

@@ -138,7 +138,7 @@ size_t radix_sort_temp_bytes(int64_t n);
 size_t scan_temp_bytes(int64_t n);
 
 // LSD radix sort of uint32 keys (and optional uint32 values) on bits
-// [0, end_bit).  Data ping-pongs between (k0,v0) and (k1,v1); *in_alt tells
+// [0, end_bit); higher key bits are ignored.  Data ping-pongs between (k0,v0) and (k1,v1); *in_alt tells
 // where the result is.  If iota_vals, the values of the first pass are the
 // positions 0..n-1 (v0 is not read).  Stable.  With first_counts_given the
 // caller has already written the first pass's digit counts (see

@@ -1,5 +1,6 @@
 // Device-wide primitives: exclusive scan and an on-chip-staged LSD radix sort
-// (8-bit digits, reduce-then-scan).
+// (8-bit digits, the last one narrower when the key width is not a multiple
+// of 8; reduce-then-scan).
 //
 // Radix pass over tiles of 4096 keys.  Large sorts split the tiles into one
 // contiguous chunk per persistent block:
@@ -56,6 +57,21 @@ __device__ __forceinline__ uint32_t match_digit8(uint32_t d, bool valid) {
     const uint32_t bit = (d >> b) & 1u;
     const uint32_t v = __ballot_sync(0xffffffffu, bit);
     m &= bit ? v : ~v;
+  }
+  return m;
+}
+
+// The same for a digit of dbits < 8 bits (d < 2^dbits): one ballot per live
+// bit.  dbits is uniform over the grid.
+__device__ __forceinline__ uint32_t match_digit_n(uint32_t d, bool valid, int dbits) {
+  uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < 7; ++b) {
+    if (b < dbits) {
+      const uint32_t bit = (d >> b) & 1u;
+      const uint32_t v = __ballot_sync(0xffffffffu, bit);
+      m &= bit ? v : ~v;
+    }
   }
   return m;
 }
@@ -145,7 +161,7 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restric
 
 // ---- radix sort --------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restrict__ keys, int64_t n,
-                                                       int shift, uint32_t* __restrict__ hist,
+                                                       int shift, uint32_t dmask, uint32_t* __restrict__ hist,
                                                        int64_t ntiles) {
   __shared__ uint32_t h[kWarps][kRadix];
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) (&h[0][0])[i] = 0;
@@ -157,15 +173,15 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restric
 #pragma unroll
     for (int it = 0; it < kTile / 4 / kBlock; ++it) {
       uint4 q = __ldg(k4 + it * kBlock + threadIdx.x);
-      atomicAdd(&h[w][(q.x >> shift) & 255u], 1u);
-      atomicAdd(&h[w][(q.y >> shift) & 255u], 1u);
-      atomicAdd(&h[w][(q.z >> shift) & 255u], 1u);
-      atomicAdd(&h[w][(q.w >> shift) & 255u], 1u);
+      atomicAdd(&h[w][(q.x >> shift) & dmask], 1u);
+      atomicAdd(&h[w][(q.y >> shift) & dmask], 1u);
+      atomicAdd(&h[w][(q.z >> shift) & dmask], 1u);
+      atomicAdd(&h[w][(q.w >> shift) & dmask], 1u);
     }
   } else {
     for (int i = threadIdx.x; i < kTile; i += kBlock) {
       int64_t p = base + i;
-      if (p < n) atomicAdd(&h[w][(keys[p] >> shift) & 255u], 1u);
+      if (p < n) atomicAdd(&h[w][(keys[p] >> shift) & dmask], 1u);
     }
   }
   __syncthreads();
@@ -182,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restric
 // hist[d * gridDim.x + blockIdx.x].  The scanned entry of a chunk's first
 // part is then that chunk's output base.  Keys are 16-byte aligned.
 __global__ void __launch_bounds__(kBlock) k_rs_upsweep_chunk(const uint32_t* __restrict__ keys, int64_t n,
-                                                             int shift, uint32_t* __restrict__ hist,
+                                                             int shift, uint32_t dmask, uint32_t* __restrict__ hist,
                                                              int64_t ntiles) {
   __shared__ uint32_t h[kWarps][kRadix];
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) (&h[0][0])[i] = 0;
@@ -194,12 +210,12 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep_chunk(const uint32_t* __r
   const uint4* k4 = reinterpret_cast<const uint4*>(keys + b);
   for (int64_t i = threadIdx.x; i < (e4 - b) / 4; i += kBlock) {
     const uint4 q = __ldg(k4 + i);
-    atomicAdd(&h[w][(q.x >> shift) & 255u], 1u);
-    atomicAdd(&h[w][(q.y >> shift) & 255u], 1u);
-    atomicAdd(&h[w][(q.z >> shift) & 255u], 1u);
-    atomicAdd(&h[w][(q.w >> shift) & 255u], 1u);
+    atomicAdd(&h[w][(q.x >> shift) & dmask], 1u);
+    atomicAdd(&h[w][(q.y >> shift) & dmask], 1u);
+    atomicAdd(&h[w][(q.z >> shift) & dmask], 1u);
+    atomicAdd(&h[w][(q.w >> shift) & dmask], 1u);
   }
-  for (int64_t p = e4 + threadIdx.x; p < e; p += kBlock) atomicAdd(&h[w][(__ldg(keys + p) >> shift) & 255u], 1u);
+  for (int64_t p = e4 + threadIdx.x; p < e; p += kBlock) atomicAdd(&h[w][(__ldg(keys + p) >> shift) & dmask], 1u);
   __syncthreads();
   for (int d = threadIdx.x; d < kRadix; d += kBlock) {
     uint32_t s = 0;
@@ -214,7 +230,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __re
                                                             const uint32_t* __restrict__ vin,
                                                             uint32_t* __restrict__ kout,
                                                             uint32_t* __restrict__ vout, int64_t n, int shift,
-                                                            const uint32_t* __restrict__ hist, int64_t ntiles) {
+                                                            uint32_t dmask, const uint32_t* __restrict__ hist,
+                                                            int64_t ntiles) {
   __shared__ uint32_t s_keys[kTile];
   __shared__ uint32_t s_vals[kHasVals ? kTile : 1];
   __shared__ uint32_t s_wcnt[kWarps][kRadix];
@@ -243,7 +260,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __re
   for (int i = 0; i < kItems; ++i) {
     int64_t p = warp_base + i * 32 + lane;
     bool valid = full || p < n;
-    uint32_t d = (k[i] >> shift) & 255u;
+    uint32_t d = (k[i] >> shift) & dmask;
     uint32_t peers = match_digit8(d, valid);
     uint32_t before = valid ? s_wcnt[w][d] : 0u;
     __syncwarp();
@@ -275,7 +292,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __re
   for (int i = 0; i < kItems; ++i) {
     int64_t p = warp_base + i * 32 + lane;
     if (full || p < n) {
-      uint32_t d = (k[i] >> shift) & 255u;
+      uint32_t d = (k[i] >> shift) & dmask;
       uint32_t rk = (rank[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
       uint32_t pos = s_start[d] + s_wcnt[w][d] + rk;
       s_keys[pos] = k[i];
@@ -286,7 +303,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_rs_downsweep(const uint32_t* __re
   int64_t tile_n = n - tile_base < kTile ? n - tile_base : kTile;
   for (int j = threadIdx.x; j < tile_n; j += kBlock) {
     uint32_t key = s_keys[j];
-    uint32_t d = (key >> shift) & 255u;
+    uint32_t d = (key >> shift) & dmask;
     uint32_t gp = s_glob[d] + (uint32_t)j - s_start[d];
     kout[gp] = key;
     if (kHasVals) vout[gp] = s_vals[j];
@@ -343,11 +360,12 @@ __device__ __forceinline__ void rs_issue(const uint32_t* __restrict__ kin, const
 // scattered, the next two are already being copied into shared memory with
 // cp.async (double buffer); cp.async.wait_group is a hardware wait on this
 // thread's own copies.
-template <bool kHasVals, bool kIota>
+// kFull: 8-bit digit; otherwise a digit of dbits < 8 bits.
+template <bool kHasVals, bool kIota, bool kFull>
 __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t* __restrict__ kin,
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
-                                                                 uint32_t* __restrict__ vout, int shift,
+                                                                 uint32_t* __restrict__ vout, int shift, int dbits,
                                                                  int64_t ntiles, const uint32_t* __restrict__ hist,
                                                                  int64_t n) {
   constexpr bool kLoadVals = kHasVals && !kIota;
@@ -363,6 +381,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = lanemask_lt();
+  const uint32_t dmask = kFull ? 255u : (1u << dbits) - 1u;
   int64_t t0, t1;
   chunk_tiles(ntiles, gridDim.x, blockIdx.x, &t0, &t1);
   // kBlock == kRadix; the upsweep ran kSubChunks parts per chunk
@@ -393,14 +412,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int32_t lp = w * 32 * kItems + i * 32 + lane;
-      peers[i] = match_digit8((k[i] >> shift) & 255u, full || lp < tn);
+      const uint32_t d = (k[i] >> shift) & dmask;
+      peers[i] = kFull ? match_digit8(d, full || lp < tn) : match_digit_n(d, full || lp < tn, dbits);
     }
     // then the per-warp digit counters, item by item (stable order)
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const int32_t lp = w * 32 * kItems + i * 32 + lane;
       const bool valid = full || lp < tn;
-      const uint32_t d = (k[i] >> shift) & 255u;
+      const uint32_t d = (k[i] >> shift) & dmask;
       const uint32_t before = valid ? wcnt[w * kRadix + d] : 0u;
       __syncwarp();
       const uint32_t r = __popc(peers[i] & lt);
@@ -432,7 +452,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     for (int i = 0; i < kItems; ++i) {
       const int32_t lp = w * 32 * kItems + i * 32 + lane;
       if (full || lp < tn) {
-        const uint32_t d = (k[i] >> shift) & 255u;
+        const uint32_t d = (k[i] >> shift) & dmask;
         const uint32_t rk = (rank[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
         const uint32_t pos = st_[d] + wcnt[w * kRadix + d] + rk;
         out_k[pos] = k[i];
@@ -443,7 +463,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
     for (int i = threadIdx.x; i < kWarps * kRadix; i += kBlock) wcnt[i] = 0;  // for the next tile
     for (int j = threadIdx.x; j < tn; j += kBlock) {
       const uint32_t key = out_k[j];
-      const uint32_t gp = adj[(key >> shift) & 255u] + (uint32_t)j;
+      const uint32_t gp = adj[(key >> shift) & dmask] + (uint32_t)j;
       kout[gp] = key;
       if (kHasVals) vout[gp] = out_v[j];
     }
@@ -460,20 +480,27 @@ size_t pipe_smem_bytes() {
                              kWarps * kRadix + 2 * kRadix);
 }
 
-template <bool kHasVals, bool kIota>
-cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int shift,
-                        int64_t ntiles, int64_t chunks, const uint32_t* hist, int64_t n, cudaStream_t s) {
+template <bool kHasVals, bool kIota, bool kFull>
+cudaError_t launch_pipe_t(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int shift,
+                          int dbits, int64_t ntiles, int64_t chunks, const uint32_t* hist, int64_t n, cudaStream_t s) {
   static bool configured = false;  // per template instance
   const size_t smem = pipe_smem_bytes<kHasVals, kIota>();
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota>,
+    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_pipe<kHasVals, kIota, kFull>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  OWM_LAUNCH("k_rs_downsweep", s, (k_rs_downsweep_pipe<kHasVals, kIota><<<(unsigned)chunks, kBlock, smem, s>>>(
-      kin, vin, kout, vout, shift, ntiles, hist, n)));
+  OWM_LAUNCH("k_rs_downsweep", s, (k_rs_downsweep_pipe<kHasVals, kIota, kFull><<<(unsigned)chunks, kBlock, smem, s>>>(
+      kin, vin, kout, vout, shift, dbits, ntiles, hist, n)));
   return cudaGetLastError();
+}
+
+template <bool kHasVals, bool kIota>
+cudaError_t launch_pipe(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int shift,
+                        int dbits, int64_t ntiles, int64_t chunks, const uint32_t* hist, int64_t n, cudaStream_t s) {
+  return dbits == 8 ? launch_pipe_t<kHasVals, kIota, true>(kin, vin, kout, vout, shift, dbits, ntiles, chunks, hist, n, s)
+                    : launch_pipe_t<kHasVals, kIota, false>(kin, vin, kout, vout, shift, dbits, ntiles, chunks, hist, n, s);
 }
 
 }  // namespace
@@ -551,31 +578,35 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   bool first = true;
   // large sorts: one contiguous chunk of tiles per persistent block (two per SM)
   const int64_t chunks = sort_chunks(ntiles);
-  if (first_counts_given && !chunks) return cudaErrorInvalidValue;
+  // given first-pass counts are of the full low byte
+  if (first_counts_given && (!chunks || end_bit < 8)) return cudaErrorInvalidValue;
   for (int shift = 0; shift < end_bit; shift += 8) {
+    // a pass sorts on bits [shift, shift + dbits); higher key bits are ignored
+    const int dbits = std::min(8, end_bit - shift);
+    const uint32_t dmask = (1u << dbits) - 1u;
     if (chunks) {
       if (!(first && first_counts_given))
         OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep_chunk<<<(unsigned)(chunks * kSubChunks), kBlock, 0, s>>>(
-            ka, n, shift, hist, ntiles));
+            ka, n, shift, dmask, hist, ntiles));
       cudaError_t e = exclusive_scan_u32(hist, hist, chunks * kSubChunks * kRadix, nullptr, stemp, sbytes, s, launches);
       if (e != cudaSuccess) return e;
       cudaError_t e2;
       if (has_vals)
-        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, shift, ntiles, chunks, hist, n, s)
-                                  : launch_pipe<true, false>(ka, va, kb, vb, shift, ntiles, chunks, hist, n, s);
+        e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, shift, dbits, ntiles, chunks, hist, n, s)
+                                  : launch_pipe<true, false>(ka, va, kb, vb, shift, dbits, ntiles, chunks, hist, n, s);
       else
-        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, shift, ntiles, chunks, hist, n, s);
+        e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, shift, dbits, ntiles, chunks, hist, n, s);
       if (e2 != cudaSuccess) return e2;
     } else {  // small sorts: one block per tile, per-tile counts
-      OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, hist, ntiles));
+      OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, dmask, hist, ntiles));
       cudaError_t e = exclusive_scan_u32(hist, hist, hn, nullptr, stemp, sbytes, s, launches);
       if (e != cudaSuccess) return e;
       if (has_vals && first && iota_vals)
-        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
+        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, dmask, hist, ntiles));
       else if (has_vals)
-        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, hist, ntiles));
+        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, dmask, hist, ntiles));
       else
-        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, hist, ntiles));
+        OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<false, false><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, nullptr, kb, nullptr, n, shift, dmask, hist, ntiles));
     }
     count_launch(launches, (chunks && first && first_counts_given) ? 1 : 2);
     first = false;
