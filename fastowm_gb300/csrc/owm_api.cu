@@ -203,6 +203,13 @@ int owm_ctx_create(int device, owm_ctx** out) {
   }
   cudaMemset(c->d_small, 0, 4096);
   for (auto& e : c->ev) cudaEventCreate(&e);
+  if (cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    owm_ctx_destroy(c);
+    return OWM_ECUDA;
+  }
   cudaStreamSynchronize(c->stream);
   *out = c;
   return OWM_OK;
@@ -229,6 +236,12 @@ int owm_ctx_destroy(owm_ctx* c) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
   }
+  if (c->side_stream) {
+    cudaStreamSynchronize(c->side_stream);
+    cudaStreamDestroy(c->side_stream);
+  }
+  if (c->side_fork) cudaEventDestroy(c->side_fork);
+  if (c->side_join) cudaEventDestroy(c->side_join);
   c->prof.clear();
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   c->prof.pool.clear();

@@ -439,7 +439,7 @@ size_t tree_scratch_bytes(int64_t n) {
 
 int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
                void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
-               const ClassArgs* cls, bool* fused) {
+               const ClassArgs* cls, bool* fused, cudaEvent_t cls_ready) {
   if (fused) *fused = false;
   if (n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
   if ((reinterpret_cast<uintptr_t>(d_xyz) & 15u) != 0) return OWM_EINVAL;  // the gather reads 16-byte words
@@ -544,6 +544,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   t->root = 0;
 
   if (fixed) {
+    if (cls && cls_ready) OWM_CUDA_TRY(cudaStreamWaitEvent(s, cls_ready, 0));
     switch (L) {
       case 1: launch_gather_leaves<1>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
       case 2: launch_gather_leaves<2>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;

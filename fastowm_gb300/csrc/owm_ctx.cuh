@@ -88,6 +88,10 @@ struct owm_ctx {
   };
   cudaStream_t copy_stream = nullptr;
   AsyncSlot aslot[2];
+  // owm_run prepares the stage-1 class tables on side_stream while the tree's
+  // keys are sorted on `stream` (fork and join by the two events).
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   int64_t next_ticket = 1;
 };
 

@@ -144,17 +144,29 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   OWM_CUDA_TRY(cudaEventRecord(c->ev[0], s));
   rc = clear_status(c);
   ClassArgs cls;
+  bool forked = false;
   if (!rc && !cfg.stage1_walk) {
-    // window edges and class tables first, so the build's gather can fold
-    // every point into its window class on the fly
-    rc = compute_edges(p, bb.min_x, bb.min_y, false, ex, ey, s, &c->launches);
+    // Window edges and class tables, so that the build's gather can fold
+    // every point into its window class on the fly.  They depend on nothing
+    // the build makes before its gather, so they are prepared on the side
+    // stream (forked after everything already queued on s, which may still
+    // use this scratch) while the Morton pass and the sort run.
+    cudaStream_t ss = c->side_stream;
+    OWM_CUDA_TRY(cudaEventRecord(c->side_fork, s));
+    OWM_CUDA_TRY(cudaStreamWaitEvent(ss, c->side_fork, 0));
+    forked = true;
+    rc = compute_edges(p, bb.min_x, bb.min_y, false, ex, ey, ss, &c->launches);
     if (!rc)
-      rc = classes_prepare(p, ex, ey, static_cast<char*>(c->scratch.ptr) + tbytes, cbytes, n, &cls, s, &c->launches);
+      rc = classes_prepare(p, ex, ey, static_cast<char*>(c->scratch.ptr) + tbytes, cbytes, n, &cls, ss, &c->launches);
+    OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   bool fused = false;
   if (!rc)
     rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
-                    &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused);
+                    &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr);
+  // join (again, if the gather already did): nothing queued on s after this
+  // point overtakes the side stream's work, on success or failure
+  if (forked) OWM_CUDA_TRY(cudaStreamWaitEvent(s, c->side_join, 0));
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[1], s));
   if (cfg.stage1_walk) {
