@@ -439,7 +439,7 @@ size_t tree_scratch_bytes(int64_t n) {
 
 int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
                void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
-               const ClassArgs* cls, bool* fused, cudaEvent_t cls_ready) {
+               const ClassArgs* cls, bool* fused, cudaEvent_t cls_ready, cudaEvent_t gather_done) {
   if (fused) *fused = false;
   if (n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
   if ((reinterpret_cast<uintptr_t>(d_xyz) & 15u) != 0) return OWM_EINVAL;  // the gather reads 16-byte words
@@ -560,6 +560,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     }
     count_launch(launches);
     if (fused && cls) *fused = true;
+    if (cls && gather_done) OWM_CUDA_TRY(cudaEventRecord(gather_done, s));
   } else {
     OWM_LAUNCH("k_gather", s, k_gather<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status));
     count_launch(launches);

@@ -64,11 +64,14 @@ int choose_key_bits(int64_t n, int policy, double side, float min_radius, int32_
 // the fixed-leaf gather also folds every point into the stage-1 window
 // classes (*fused says whether it did; the min-radius build does not); when
 // cls_ready is given, s waits on it right before that gather, so the class
-// tables may be prepared on another stream while the keys are sorted.
+// tables may be prepared on another stream while the keys are sorted, and
+// gather_done (if given) is recorded on s right after that gather, so the
+// classes may be finished on another stream while the hierarchy is built.
 struct ClassArgs;
 int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bbox, const owm_tree_cfg& cfg, TreeStore* t,
                void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
-               const ClassArgs* cls = nullptr, bool* fused = nullptr, cudaEvent_t cls_ready = nullptr);
+               const ClassArgs* cls = nullptr, bool* fused = nullptr, cudaEvent_t cls_ready = nullptr,
+               cudaEvent_t gather_done = nullptr);
 
 // Structural self-check (checkNumPoints); *h_bad = number of bad nodes.
 int check_tree(const TreeStore* t, int32_t* d_bad, cudaStream_t s, int64_t* launches, int32_t* h_bad);

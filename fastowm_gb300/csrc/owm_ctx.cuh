@@ -90,8 +90,11 @@ struct owm_ctx {
   AsyncSlot aslot[2];
   // owm_run prepares the stage-1 class tables on side_stream while the tree's
   // keys are sorted on `stream` (fork and join by the two events).
+  // Then stage 1's last kernels and stage 2 run there too, while the tree's
+  // hierarchy is built on `stream` (stage12_side: the last owm_run did so).
   cudaStream_t side_stream = nullptr;
   cudaEvent_t side_fork = nullptr, side_join = nullptr;
+  bool stage12_side = false;
   int64_t next_ticket = 1;
 };
 

@@ -118,7 +118,10 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   // scratch = [tree build | window classes]; stages 2 and 3 reuse it after stage 1
   const size_t tbytes = (tree_scratch_bytes(n) + 255) & ~(size_t)255;
   const size_t cbytes = cfg.stage1_walk ? 0 : classes_scratch_bytes(n, (int32_t)p.ncols, (int32_t)p.nrows);
-  size_t sbytes = std::max(tbytes + cbytes, std::max(std::max(stage2_bitmap_scratch_bytes(n), stage2_scratch_bytes(nc)), stage3_scratch_bytes(ng)));
+  // stage 2 may run beside the hierarchy build, so it stays clear of the
+  // build's scratch (it may reuse the class scratch: stage 1 is done by then)
+  const size_t s2bytes = p.overlap > 0.0 ? stage2_bitmap_scratch_bytes(n) : stage2_scratch_bytes(nc);
+  size_t sbytes = std::max(tbytes + std::max(cbytes, s2bytes), stage3_scratch_bytes(ng));
   rc = c->scratch.reserve(sbytes, c->stream);
   if (rc) return rc;
   size_t obytes = 2 * al(65536 * sizeof(Edge)) + 2 * al((size_t)nc * 4) + al((size_t)std::max<int64_t>(ng, 1) * 4) +
@@ -161,27 +164,51 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   bool fused = false;
+  c->stage12_side = false;
   if (!rc)
     rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
-                    &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr);
+                    &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr,
+                    forked ? c->ev[6] : nullptr);
+  void* s2scratch = static_cast<char*>(c->scratch.ptr) + tbytes;
+  const size_t s2cap = c->scratch.cap - tbytes;
+  auto stage2 = [&](cudaStream_t st) {
+    return p.overlap > 0.0 ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, st, &c->launches)
+                           : run_stage2(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, st, &c->launches);
+  };
+  if (!rc && fused) {
+    // The gather's class fold is all that stage 1 needs: finish stage 1 and
+    // run stage 2 on the side stream (after its table preparation and the
+    // gather) while s builds the hierarchy; join before stage 3.
+    cudaStream_t ss = c->side_stream;
+    c->stage12_side = true;
+    OWM_CUDA_TRY(cudaStreamWaitEvent(ss, c->ev[6], 0));
+    rc = classes_finish(cls, c->tree.view(), n, p, win, ss, &c->launches);
+    if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[2], ss));
+    if (!rc) rc = stage2(ss);
+    if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[3], ss));
+    OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
+  }
   // join (again, if the gather already did): nothing queued on s after this
   // point overtakes the side stream's work, on success or failure
+  if (forked) OWM_CUDA_TRY(cudaEventRecord(c->ev[1], s));
   if (forked) OWM_CUDA_TRY(cudaStreamWaitEvent(s, c->side_join, 0));
   if (rc) return rc;
-  OWM_CUDA_TRY(cudaEventRecord(c->ev[1], s));
-  if (cfg.stage1_walk) {
-    rc = run_stage1(c, c->tree, p, ex, ey, win);
+  if (c->stage12_side) {
+    OWM_CUDA_TRY(cudaEventRecord(c->ev[7], s));
   } else {
-    if (!fused) rc = classes_aggregate(cls, c->tree.view(), n, s, &c->launches);
-    if (!rc) rc = classes_finish(cls, c->tree.view(), n, p, win, s, &c->launches);
+    if (!forked) OWM_CUDA_TRY(cudaEventRecord(c->ev[1], s));
+    if (cfg.stage1_walk) {
+      rc = run_stage1(c, c->tree, p, ex, ey, win);
+    } else {
+      if (!fused) rc = classes_aggregate(cls, c->tree.view(), n, s, &c->launches);
+      if (!rc) rc = classes_finish(cls, c->tree.view(), n, p, win, s, &c->launches);
+    }
+    if (rc) return rc;
+    OWM_CUDA_TRY(cudaEventRecord(c->ev[2], s));
+    rc = stage2(s);
+    if (rc) return rc;
+    OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
   }
-  if (rc) return rc;
-  OWM_CUDA_TRY(cudaEventRecord(c->ev[2], s));
-  rc = p.overlap > 0.0
-           ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches)
-           : run_stage2(win, nc, n, p.overlap, llp, d_nllp, c->scratch.ptr, c->scratch.cap, s, &c->launches);
-  if (rc) return rc;
-  OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
   rc = run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, c->scratch.ptr, c->scratch.cap, c->d_job,
                   c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
@@ -223,11 +250,14 @@ int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb,
   OWM_CUDA_TRY(cudaEventRecord(c->ev[5], s));
   OWM_CUDA_TRY(cudaStreamSynchronize(s));
   if (info) {
+    // With stages 1-2 beside the hierarchy build, stage 1 counts from the
+    // gather's end and stage 3 from the join, so the phases overlap.
     float a = 0, b = 0, d = 0, e = 0, f = 0;
+    const bool side = c->stage12_side;
     cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
-    cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&b, side ? c->ev[6] : c->ev[1], c->ev[2]);
     cudaEventElapsedTime(&d, c->ev[2], c->ev[3]);
-    cudaEventElapsedTime(&e, c->ev[3], c->ev[4]);
+    cudaEventElapsedTime(&e, side ? c->ev[7] : c->ev[3], c->ev[4]);
     cudaEventElapsedTime(&f, c->ev[0], c->ev[5]);
     info->ms_tree = a;
     info->ms_stage1 = b;
