@@ -435,7 +435,9 @@ def main():
                 "phases_ms": {"tree": round(phase[0] / args.steps, 4), "stage1": round(phase[1] / args.steps, 4),
                               "stage2": round(phase[2] / args.steps, 4), "stage3": round(phase[3] / args.steps, 4)},
                 "kernel_timing": "second pass over the same K steps with CUDA events around every launch "
-                                 "(the value pass runs without them)",
+                                 "(the value pass runs without them); k_edges, k_cls_* and k_s2_* run on a side "
+                                 "stream beside the Morton pass, the sort and the hierarchy build, so their event "
+                                 "times include waiting for SMs and the shares sum to more than one step",
                 "kernels": {k: {"ms": round(v[0] / args.steps, 4), "share": round(v[0] / tot_k, 4),
                                 "launches_per_step": v[1] / args.steps} for k, v in
                             sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
