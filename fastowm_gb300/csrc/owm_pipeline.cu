@@ -115,13 +115,14 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   const int64_t nc = p.ncells, ng = std::max<int64_t>(p.ngrid, 0);
   rc = tree_alloc(&c->tree, &c->tree_mem, n, cfg.tree, c->stream);
   if (rc) return rc;
-  // scratch = [tree build | window classes]; stages 2 and 3 reuse it after stage 1
+  // scratch = [tree build | window classes, then stage 2, then stage 3].
+  // Stage 2 and stage 3's LLP marks may run beside the hierarchy build, so
+  // they stay clear of the build's scratch; each reuses the region after the
+  // previous one is done with it.
   const size_t tbytes = (tree_scratch_bytes(n) + 255) & ~(size_t)255;
   const size_t cbytes = cfg.stage1_walk ? 0 : classes_scratch_bytes(n, (int32_t)p.ncols, (int32_t)p.nrows);
-  // stage 2 may run beside the hierarchy build, so it stays clear of the
-  // build's scratch (it may reuse the class scratch: stage 1 is done by then)
   const size_t s2bytes = p.overlap > 0.0 ? stage2_bitmap_scratch_bytes(n) : stage2_scratch_bytes(nc);
-  size_t sbytes = std::max(tbytes + std::max(cbytes, s2bytes), stage3_scratch_bytes(ng));
+  size_t sbytes = tbytes + std::max(std::max(cbytes, s2bytes), stage3_scratch_bytes(ng));
   rc = c->scratch.reserve(sbytes, c->stream);
   if (rc) return rc;
   size_t obytes = 2 * al(65536 * sizeof(Edge)) + 2 * al((size_t)nc * 4) + al((size_t)std::max<int64_t>(ng, 1) * 4) +
@@ -169,16 +170,17 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
                     &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr,
                     forked ? c->ev[6] : nullptr);
-  void* s2scratch = static_cast<char*>(c->scratch.ptr) + tbytes;
+  void* s2scratch = static_cast<char*>(c->scratch.ptr) + tbytes;  // stages 2 and 3
   const size_t s2cap = c->scratch.cap - tbytes;
   auto stage2 = [&](cudaStream_t st) {
     return p.overlap > 0.0 ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, st, &c->launches)
                            : run_stage2(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, st, &c->launches);
   };
   if (!rc && fused) {
-    // The gather's class fold is all that stage 1 needs: finish stage 1 and
-    // run stage 2 on the side stream (after its table preparation and the
-    // gather) while s builds the hierarchy; join before stage 3.
+    // The gather's class fold is all that stage 1 needs: finish stage 1,
+    // run stage 2 and mark stage 3's LLP cells on the side stream (after its
+    // table preparation and the gather) while s builds the hierarchy; join
+    // before stage 3's queries.
     cudaStream_t ss = c->side_stream;
     c->stage12_side = true;
     OWM_CUDA_TRY(cudaStreamWaitEvent(ss, c->ev[6], 0));
@@ -186,6 +188,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[2], ss));
     if (!rc) rc = stage2(ss);
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[3], ss));
+    if (!rc) rc = run_stage3_mark(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s2scratch, s2cap, ss, &c->launches);
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   // join (again, if the gather already did): nothing queued on s after this
@@ -209,8 +212,10 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     if (rc) return rc;
     OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
   }
-  rc = run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, c->scratch.ptr, c->scratch.cap, c->d_job,
-                  c->d_small + kStatusSlot, s, &c->launches);
+  rc = c->stage12_side
+           ? run_stage3_query(c->tree.view(), p, s3, d_ns3, s2scratch, s2cap, c->d_small + kStatusSlot, s, &c->launches)
+           : run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, s2scratch, s2cap, c->d_job,
+                        c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));
   const int64_t room = nc + ng + 1;

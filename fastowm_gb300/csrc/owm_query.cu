@@ -525,6 +525,48 @@ __global__ void k_flag_valid(const uint32_t* __restrict__ v, int64_t n, uint32_t
     flags[i] = v[i] != kNone ? 1u : 0u;
 }
 
+// The valid entries (!= kNone) of v[0..n), in order, into out and their
+// number into *count, by one block: thread t owns the contiguous range
+// [t*per, (t+1)*per).  For small n it replaces flag + scan + compact.
+constexpr int kCompactBlock = 1024;
+constexpr int64_t kCompactSmallMax = (int64_t)1 << 18;
+__global__ void __launch_bounds__(kCompactBlock) k_compact_small(const uint32_t* __restrict__ v, int64_t n,
+                                                                uint32_t* __restrict__ out,
+                                                                uint32_t* __restrict__ count) {
+  __shared__ uint32_t warp_tot[kCompactBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t per = (n + kCompactBlock - 1) / kCompactBlock;
+  const int64_t b = (int64_t)threadIdx.x * per;
+  const int64_t e = b + per < n ? b + per : n;
+  uint32_t c = 0;
+  for (int64_t i = b; i < e; ++i) c += v[i] != kNone ? 1u : 0u;
+  uint32_t inc = c;  // inclusive warp scan
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const uint32_t x = warp_tot[lane];
+    uint32_t y = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += t;
+    }
+    warp_tot[lane] = y - x;  // exclusive warp offsets
+    if (lane == 31) *count = y;
+  }
+  __syncthreads();
+  uint32_t off = warp_tot[w] + inc - c;
+  for (int64_t i = b; i < e; ++i) {
+    const uint32_t x = v[i];
+    if (x != kNone) out[off++] = x;
+  }
+}
+
 // ---- stage 3 -----------------------------------------------------------------
 // LLP grid (owm_optim3.cpp:192-197 + countNeighbors, optim3_func.cpp:503-539):
 // a cell is occupied when an LLP lies strictly inside its box.
@@ -746,50 +788,90 @@ size_t stage3_scratch_bytes(int64_t ngrid) {
          align256(scan_temp_bytes(m)) + 1024;
 }
 
-int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
-               const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
-               size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches) {
-  int64_t ng = p.ngrid;
-  if (p.bsize == 0 || ng <= 0) {
-    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
-    return OWM_OK;
-  }
-  if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
+namespace {
+struct S3Layout {
+  uint8_t* mark;
+  uint32_t *cellmin, *flags, *pos;
+  Edge *ex, *ey;
+  void* ct;
+  size_t cb;
+};
+S3Layout stage3_layout(void* scratch, int64_t ng) {
   char* sp = static_cast<char*>(scratch);
   auto take = [&](size_t b) {
     void* q = sp;
     sp += align256(b);
     return q;
   };
-  uint8_t* mark = (uint8_t*)take((size_t)ng);
-  uint32_t* cellmin = (uint32_t*)take((size_t)ng * 4);
-  uint32_t* flags = (uint32_t*)take((size_t)ng * 4);
-  uint32_t* pos = (uint32_t*)take((size_t)ng * 4);
-  Edge* ex = (Edge*)take((size_t)65536 * sizeof(Edge));
-  Edge* ey = (Edge*)take((size_t)65536 * sizeof(Edge));
-  size_t cb = scan_temp_bytes(ng);
-  void* ct = take(cb);
-  int rc = compute_edges(p, t.ox, t.oy, true, ex, ey, s, launches);
+  S3Layout L;
+  L.mark = (uint8_t*)take((size_t)ng);
+  L.cellmin = (uint32_t*)take((size_t)ng * 4);
+  L.flags = (uint32_t*)take((size_t)ng * 4);
+  L.pos = (uint32_t*)take((size_t)ng * 4);
+  L.ex = (Edge*)take((size_t)65536 * sizeof(Edge));
+  L.ey = (Edge*)take((size_t)65536 * sizeof(Edge));
+  L.cb = scan_temp_bytes(ng);
+  L.ct = take(L.cb);
+  return L;
+}
+}  // namespace
+
+int run_stage3_mark(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
+                    const uint32_t* d_nllp, int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s,
+                    int64_t* launches) {
+  const int64_t ng = p.ngrid;
+  if (p.bsize == 0 || ng <= 0) return OWM_OK;
+  if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
+  const S3Layout L = stage3_layout(scratch, ng);
+  int rc = compute_edges(p, t.ox, t.oy, true, L.ex, L.ey, s, launches);
   if (rc) return rc;
-  OWM_CUDA_TRY(cudaMemsetAsync(mark, 0, (size_t)ng, s));
+  OWM_CUDA_TRY(cudaMemsetAsync(L.mark, 0, (size_t)ng, s));
   if (llp_cap > 0) {
-    OWM_LAUNCH("k_s3_mark", s, k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, ex, ey, (int32_t)p.ncols_grid,
-                                             (int32_t)p.nrows_grid, p.bbox.min_x, p.bbox.min_y, (double)p.bsize, mark));
+    OWM_LAUNCH("k_s3_mark", s, k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, L.ex, L.ey,
+                                                                       (int32_t)p.ncols_grid, (int32_t)p.nrows_grid,
+                                                                       p.bbox.min_x, p.bbox.min_y, (double)p.bsize,
+                                                                       L.mark));
     count_launch(launches);
   }
-  (void)d_job_slot;
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int run_stage3_query(const TreeView& t, const owm_params& p, uint32_t* d_out, uint32_t* d_count, void* scratch,
+                     size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches) {
+  const int64_t ng = p.ngrid;
+  if (p.bsize == 0 || ng <= 0) {
+    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+    return OWM_OK;
+  }
+  if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
+  const S3Layout L = stage3_layout(scratch, ng);
   const int64_t cblocks = (ng + kS3Warps - 1) / kS3Warps;
   if (cblocks >= 0x7FFFFFFFll) return OWM_ERANGE;
   OWM_LAUNCH("k_query_s3", s, k_query_cells<<<(unsigned)cblocks, kS3Warps * 32, 0, s>>>(
-      t, ex, ey, (int32_t)p.ncols_grid, ng, mark, cellmin, status));
+      t, L.ex, L.ey, (int32_t)p.ncols_grid, ng, L.mark, L.cellmin, status));
   count_launch(launches);
-  OWM_LAUNCH("k_flag_valid", s, k_flag_valid<<<grid1d(ng), 256, 0, s>>>(cellmin, ng, flags));
-  count_launch(launches);
-  OWM_CUDA_TRY(exclusive_scan_u32(flags, pos, ng, d_count, ct, cb, s, launches));
-  OWM_LAUNCH("k_compact", s, k_compact<<<grid1d(ng), 256, 0, s>>>(cellmin, flags, pos, ng, d_out));
-  count_launch(launches);
+  if (ng <= kCompactSmallMax) {
+    OWM_LAUNCH("k_compact_small", s, k_compact_small<<<1, kCompactBlock, 0, s>>>(L.cellmin, ng, d_out, d_count));
+    count_launch(launches);
+  } else {
+    OWM_LAUNCH("k_flag_valid", s, k_flag_valid<<<grid1d(ng), 256, 0, s>>>(L.cellmin, ng, L.flags));
+    count_launch(launches);
+    OWM_CUDA_TRY(exclusive_scan_u32(L.flags, L.pos, ng, d_count, L.ct, L.cb, s, launches));
+    OWM_LAUNCH("k_compact", s, k_compact<<<grid1d(ng), 256, 0, s>>>(L.cellmin, L.flags, L.pos, ng, d_out));
+    count_launch(launches);
+  }
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
+}
+
+int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
+               const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
+               size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches) {
+  (void)d_job_slot;
+  int rc = run_stage3_mark(t, d_xyz, p, d_llp, d_nllp, llp_cap, scratch, scratch_bytes, s, launches);
+  if (rc) return rc;
+  return run_stage3_query(t, p, d_out, d_count, scratch, scratch_bytes, status, s, launches);
 }
 
 int u32_to_i64_ids(const uint32_t* in, const uint32_t* d_count, int64_t cap, int64_t* out, cudaStream_t s,
