@@ -247,7 +247,8 @@ __global__ void k_bc_windows(const ClassArgs* __restrict__ cls, const TileMeta* 
                              uint32_t* __restrict__ win) {
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
     const int t = tile_of(win_off, ntiles, w);
-    win[w] = cls_window_one(cls[t], w - __ldg(win_off + t), meta[t].thr);
+    const int64_t off = __ldg(win_off + t);
+    win[off + cls_window_slot(cls[t], w - off)] = cls_window_one(cls[t], w - off, meta[t].thr);
   }
 }
 

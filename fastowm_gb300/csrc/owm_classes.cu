@@ -76,7 +76,7 @@ __global__ void k_cls_rows(ClassArgs A) {
 __global__ void k_cls_windows(ClassArgs A, uint32_t thr, uint32_t* __restrict__ out) {
   const int64_t total = (int64_t)A.nx * A.ny;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x)
-    out[w] = cls_window_one(A, w, thr);
+    out[cls_window_slot(A, w)] = cls_window_one(A, w, thr);
 }
 
 int grid(int64_t n, int block = 256) {

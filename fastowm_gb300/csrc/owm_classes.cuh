@@ -23,7 +23,7 @@ struct ClassArgs {
   uint32_t* count;                    // [tx*ty] points per sub-cell
   ulonglong2* zid;                    // [tx*ty] (z order key sign-flipped, id): the (z, id)-min
   int32_t *sxl, *sxh, *syl, *syh;     // s-range of every window column / row
-  uint32_t *rc, *ri;                  // row reduction buffers [nx*ty]
+  uint32_t *rc, *ri;                  // row reduction buffers [ty][nx]: sub-cell row t, window column ii
   unsigned long long* rz;
 };
 
@@ -163,7 +163,9 @@ __device__ __forceinline__ bool cls_zu_less(unsigned long long za, uint32_t ia, 
 
 // Row reduction k = ii * ty + t: sub-cells s of window column ii in sub-cell row t.
 __device__ __forceinline__ void cls_row_one(const ClassArgs& A, int64_t k) {
-  const int32_t ii = (int32_t)(k / A.ty), t = (int32_t)(k % A.ty);
+  // k = t * nx + ii: neighbouring threads take neighbouring window columns of
+  // one sub-cell row, so their sub-cell reads and row writes coalesce
+  const int32_t t = (int32_t)(k / A.nx), ii = (int32_t)(k % A.nx);
   uint32_t c = 0, bi = 0xFFFFFFFFu;
   unsigned long long bz = ~0ull;
   const int64_t base = (int64_t)t * A.tx;
@@ -182,22 +184,30 @@ __device__ __forceinline__ void cls_row_one(const ClassArgs& A, int64_t k) {
   A.ri[k] = bi;
 }
 
-// Window w (step = ii * nrows + jj): reduce its rows, apply minNumPoints.  The
-// search starts from the reference's sentinel point 0 {0, 0, DBL_MAX}.
+// Window number w = jj * nx + ii (neighbouring threads take neighbouring
+// window columns, so the row reads coalesce): reduce its rows, apply
+// minNumPoints.  The search starts from the reference's sentinel point 0
+// {0, 0, DBL_MAX}.  The result belongs at cls_window_slot(A, w).
 __device__ __forceinline__ uint32_t cls_window_one(const ClassArgs& A, int64_t w, uint32_t thr) {
   const unsigned long long sentinel = (unsigned long long)kZSentinel ^ 0x8000000000000000ull;
-  const int32_t ii = (int32_t)(w / A.ny), jj = (int32_t)(w % A.ny);
+  const int32_t jj = (int32_t)(w / A.nx), ii = (int32_t)(w % A.nx);
   uint32_t c = 0, bi = 0;
   unsigned long long bz = sentinel;
-  const int64_t base = (int64_t)ii * A.ty;
   for (int32_t t = A.syl[jj]; t <= A.syh[jj]; ++t) {
-    c += A.rc[base + t];
-    if (cls_zu_less(A.rz[base + t], A.ri[base + t], bz, bi)) {
-      bz = A.rz[base + t];
-      bi = A.ri[base + t];
+    const int64_t r = (int64_t)t * A.nx + ii;
+    c += A.rc[r];
+    if (cls_zu_less(A.rz[r], A.ri[r], bz, bi)) {
+      bz = A.rz[r];
+      bi = A.ri[r];
     }
   }
   return c >= thr ? bi : kNone;
+}
+
+// Output slot of window number w: the reference's order, ii * nrows + jj
+// (stage1's step, optim3_func.cpp:541-561).
+__device__ __forceinline__ int64_t cls_window_slot(const ClassArgs& A, int64_t w) {
+  return (w % A.nx) * A.ny + w / A.nx;
 }
 
 // Class-table geometry over [lo, hi]: cells of 2^sh key units no wider than

@@ -497,18 +497,58 @@ __global__ void k_s2_mark(const uint32_t* __restrict__ win, int64_t n, uint32_t 
   }
 }
 
-__global__ void k_s2_popc(const uint32_t* __restrict__ bm, int64_t nw, uint32_t* __restrict__ cnt) {
-  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x)
-    cnt[w] = (uint32_t)__popc(bm[w]);
+// The set bits of a bitmap, in ascending order, by blocks of kS2Chunk words:
+// k_s2_count sums each block's bits, a scan of those sums gives each block's
+// first output slot, and k_s2_emit_chunk ranks its threads' words (thread t
+// owns kS2Words consecutive words, one 16-byte load) and writes their bit
+// indices.  The bitmap is padded to whole chunks (zero words).
+constexpr int kS2Block = 256;
+constexpr int kS2Words = 4;
+constexpr int64_t kS2Chunk = (int64_t)kS2Block * kS2Words;
+
+__device__ __forceinline__ uint32_t block_sum_excl_256(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t ws[kS2Block / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) ws[w] = inc;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+#pragma unroll
+  for (int q = 0; q < kS2Block / 32; ++q) {
+    const uint32_t x = ws[q];
+    before += q < w ? x : 0u;
+    all += x;
+  }
+  if (total) *total = all;
+  return before + inc - v;
 }
 
-__global__ void k_s2_emit(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ pos, int64_t nw,
-                          uint32_t* __restrict__ out) {
-  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
-    uint32_t b = bm[w];
-    uint32_t p = pos[w];
+__global__ void __launch_bounds__(kS2Block) k_s2_count(const uint32_t* __restrict__ bm, uint32_t* __restrict__ part) {
+  const uint4 q = __ldg(reinterpret_cast<const uint4*>(bm) + (int64_t)blockIdx.x * kS2Block + threadIdx.x);
+  const uint32_t c = (uint32_t)(__popc(q.x) + __popc(q.y) + __popc(q.z) + __popc(q.w));
+  uint32_t tot;
+  block_sum_excl_256(c, &tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kS2Block) k_s2_emit_chunk(const uint32_t* __restrict__ bm,
+                                                            const uint32_t* __restrict__ part,
+                                                            uint32_t* __restrict__ out) {
+  const int64_t w0 = (int64_t)blockIdx.x * kS2Chunk + (int64_t)threadIdx.x * kS2Words;
+  const uint4 q = __ldg(reinterpret_cast<const uint4*>(bm + w0));
+  const uint32_t word[4] = {q.x, q.y, q.z, q.w};
+  const uint32_t c = (uint32_t)(__popc(q.x) + __popc(q.y) + __popc(q.z) + __popc(q.w));
+  uint32_t p = block_sum_excl_256(c, nullptr) + part[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kS2Words; ++k) {
+    uint32_t b = word[k];
     while (b) {
-      out[p++] = (uint32_t)(w * 32) + (uint32_t)(__ffs(b) - 1);
+      out[p++] = (uint32_t)((w0 + k) * 32) + (uint32_t)(__ffs(b) - 1);
       b &= b - 1;
     }
   }
@@ -714,39 +754,62 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
   return OWM_OK;
 }
 
-size_t stage2_bitmap_scratch_bytes(int64_t npoints) {
-  const int64_t nw = (npoints + 1 + 31) / 32;
-  return 4 * align256((size_t)nw * 4) + align256(scan_temp_bytes(nw)) + 1024;
-}
-
-int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
-                      uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches) {
-  if (n <= 0) {
-    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
-    return OWM_OK;
-  }
-  if (npoints < 0 || npoints >= (int64_t)kNone || !(overlap > 0.0)) return OWM_EINVAL;
-  if (scratch_bytes < stage2_bitmap_scratch_bytes(npoints)) return OWM_ENOMEM;
-  const int64_t nw = (npoints + 1 + 31) / 32;  // bits for ids 0..npoints
+namespace {
+struct S2Bitmaps {
+  uint32_t *once, *twice, *part;
+  void* ct;
+  size_t cb;
+  int64_t nw, nblocks;
+};
+S2Bitmaps stage2_bitmap_layout(void* scratch, int64_t npoints) {
+  S2Bitmaps B;
+  B.nblocks = ((npoints + 1 + 31) / 32 + kS2Chunk - 1) / kS2Chunk;  // bits for ids 0..npoints
+  B.nw = B.nblocks * kS2Chunk;                                      // whole chunks
   char* sp = static_cast<char*>(scratch);
   auto take = [&](size_t b) {
     void* p = sp;
     sp += align256(b);
     return p;
   };
-  uint32_t* once = (uint32_t*)take((size_t)nw * 4);
-  uint32_t* twice = (uint32_t*)take((size_t)nw * 4);
-  uint32_t* cnt = (uint32_t*)take((size_t)nw * 4);
-  uint32_t* pos = (uint32_t*)take((size_t)nw * 4);
-  size_t cb = scan_temp_bytes(nw);
-  void* ct = take(cb);
-  OWM_CUDA_TRY(cudaMemsetAsync(once, 0, 2 * align256((size_t)nw * 4), s));  // once, then twice
-  OWM_LAUNCH("k_s2_mark", s, k_s2_mark<<<grid1d(n), 256, 0, s>>>(d_win, n, (uint32_t)npoints, once, twice));
-  const uint32_t* sel = twice;
-  OWM_LAUNCH("k_s2_popc", s, k_s2_popc<<<grid1d(nw), 256, 0, s>>>(sel, nw, cnt));
+  B.once = (uint32_t*)take((size_t)B.nw * 4);   // once and twice are adjacent:
+  B.twice = (uint32_t*)take((size_t)B.nw * 4);  // one memset clears both
+  B.part = (uint32_t*)take((size_t)B.nblocks * 4);
+  B.cb = scan_temp_bytes(B.nblocks);
+  B.ct = take(B.cb);
+  return B;
+}
+}  // namespace
+
+size_t stage2_bitmap_scratch_bytes(int64_t npoints) {
+  const int64_t nb = ((npoints + 1 + 31) / 32 + kS2Chunk - 1) / kS2Chunk;
+  const int64_t nw = nb * kS2Chunk;
+  return 2 * align256((size_t)nw * 4) + align256((size_t)nb * 4) + align256(scan_temp_bytes(nb)) + 1024;
+}
+
+int stage2_bitmap_clear(void* scratch, size_t scratch_bytes, int64_t npoints, cudaStream_t s) {
+  if (npoints < 0 || npoints >= (int64_t)kNone) return OWM_EINVAL;
+  if (scratch_bytes < stage2_bitmap_scratch_bytes(npoints)) return OWM_ENOMEM;
+  const S2Bitmaps B = stage2_bitmap_layout(scratch, npoints);
+  OWM_CUDA_TRY(cudaMemsetAsync(B.once, 0, 2 * align256((size_t)B.nw * 4), s));  // once, then twice
+  return OWM_OK;
+}
+
+int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
+                      uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches,
+                      bool cleared) {
+  if (n <= 0) {
+    OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+    return OWM_OK;
+  }
+  if (npoints < 0 || npoints >= (int64_t)kNone || !(overlap > 0.0)) return OWM_EINVAL;
+  if (scratch_bytes < stage2_bitmap_scratch_bytes(npoints)) return OWM_ENOMEM;
+  const S2Bitmaps B = stage2_bitmap_layout(scratch, npoints);
+  if (!cleared) OWM_CUDA_TRY(cudaMemsetAsync(B.once, 0, 2 * align256((size_t)B.nw * 4), s));
+  OWM_LAUNCH("k_s2_mark", s, k_s2_mark<<<grid1d(n), 256, 0, s>>>(d_win, n, (uint32_t)npoints, B.once, B.twice));
+  OWM_LAUNCH("k_s2_count", s, k_s2_count<<<(unsigned)B.nblocks, kS2Block, 0, s>>>(B.twice, B.part));
   count_launch(launches, 2);
-  OWM_CUDA_TRY(exclusive_scan_u32(cnt, pos, nw, d_count, ct, cb, s, launches));
-  OWM_LAUNCH("k_s2_emit", s, k_s2_emit<<<grid1d(nw), 256, 0, s>>>(sel, pos, nw, d_llp));
+  OWM_CUDA_TRY(exclusive_scan_u32(B.part, B.part, B.nblocks, d_count, B.ct, B.cb, s, launches));
+  OWM_LAUNCH("k_s2_emit", s, k_s2_emit_chunk<<<(unsigned)B.nblocks, kS2Block, 0, s>>>(B.twice, B.part, d_llp));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;

@@ -51,10 +51,14 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
                uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
 // Same result, for overlap > 0 and ids known to lie in [0, npoints] (window
 // minima of one cloud of npoints points), by occupancy bitmaps instead of a
-// sort: one marking read of the window list, then work per 32 ids.
+// sort: one marking read of the window list, then work per 32 ids.  With
+// cleared, the two bitmaps at the start of scratch were already zeroed by
+// stage2_bitmap_clear (which may run early, on another stream).
 size_t stage2_bitmap_scratch_bytes(int64_t npoints);
+int stage2_bitmap_clear(void* scratch, size_t scratch_bytes, int64_t npoints, cudaStream_t s);
 int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
-                      uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
+                      uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches,
+                      bool cleared = false);
 // Same with explicit working arrays (n uint32 each; d_llp must not alias
 // them) and a temp block of radix_sort_temp_bytes(n) (256-aligned) +
 // scan_temp_bytes(n).  d_win may equal k0.

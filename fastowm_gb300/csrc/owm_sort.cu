@@ -122,20 +122,21 @@ __global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
-// Single block: exclusive scan of the partial sums (<= kScanChunk of them).
-__global__ void k_scan_parts(uint32_t* part, int64_t nparts, uint32_t* total) {
+// Single block: exclusive scan of <= kScanChunk values (the partial sums of a
+// large scan, or a whole small one); in == out allowed.
+__global__ void k_scan_parts(const uint32_t* in, uint32_t* out, int64_t nparts, uint32_t* total) {
   uint32_t v[kScanItems];
   uint32_t s = 0;
   for (int k = 0; k < kScanItems; ++k) {
     int64_t p = (int64_t)threadIdx.x * kScanItems + k;
-    v[k] = p < nparts ? part[p] : 0u;
+    v[k] = p < nparts ? in[p] : 0u;
     s += v[k];
   }
   uint32_t tot;
   uint32_t off = block_excl_scan(s, &tot);
   for (int k = 0; k < kScanItems; ++k) {
     int64_t p = (int64_t)threadIdx.x * kScanItems + k;
-    if (p < nparts) part[p] = off;
+    if (p < nparts) out[p] = off;
     off += v[k];
   }
   if (threadIdx.x == 0 && total) *total = tot;
@@ -544,11 +545,16 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
   }
   const int64_t parts = (n + kScanChunk - 1) / kScanChunk;
   if (temp_bytes < scan_temp_bytes(n) || n >= ((int64_t)1 << 40)) return cudaErrorInvalidValue;
+  if (parts == 1) {  // one block does it all
+    OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(in, out, n, total));
+    count_launch(launches);
+    return cudaGetLastError();
+  }
   uint32_t* part = static_cast<uint32_t*>(temp);
   OWM_LAUNCH("k_scan_reduce", s, k_scan_reduce<<<(unsigned)parts, kScanBlock, 0, s>>>(in, n, part));
   count_launch(launches, 2);
   if (parts <= (int64_t)kScanChunk) {
-    OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(part, parts, total));
+    OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(part, part, parts, total));
     count_launch(launches);
   } else {  // more than 2^26 values: scan the partial sums in place, recursively
     const size_t pb = ((size_t)(parts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
