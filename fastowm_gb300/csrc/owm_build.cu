@@ -13,10 +13,10 @@
 //   k_leaf_reduce     (min-radius policy) or any other leaf partition
 //   k_karras          binary radix hierarchy over the leaves (Karras 2012) on
 //                     64-bit (leaf Morton key, leaf index) codes
-//   k_escapes         depth-first "escape" link of every node, so that queries
-//                     walk the tree without a stack
 //   k_refit           bottom-up atomic refit: internal count, box and
 //                     (z, id)-min -- the reference's O3 memo (storeMinAndNumPoints)
+//                     -- and the depth-first "escape" link of every node, so
+//                     that queries walk the tree without a stack
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -255,11 +255,15 @@ __device__ __forceinline__ int delta(const uint32_t* __restrict__ mk, int32_t L,
 
 // Karras (2012), Sec. 4: internal node i covers leaves [min(i,j), max(i,j)]
 // and splits after gamma.  Internal nodes are 0..nl-2, leaf li is nl-1+li.
+// Also readies k_refit: the root's parent is -1 and every internal node's
+// arrival counter starts at 0.
 __global__ void k_karras(const uint32_t* __restrict__ mk, int32_t L, const int32_t* __restrict__ starts, int32_t nl,
                          Node* __restrict__ nodes, int32_t* __restrict__ parent, int32_t* __restrict__ right_of,
-                         int32_t* __restrict__ last_of) {
+                         int32_t* __restrict__ last_of, int32_t* __restrict__ flags) {
   int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nl - 1) return;
+  flags[i] = 0;
+  if (i == 0) parent[0] = -1;  // no node has the root as a child
   int d = delta(mk, L, starts, nl, i, i + 1) - delta(mk, L, starts, nl, i, i - 1) > 0 ? 1 : -1;
   int dmin = delta(mk, L, starts, nl, i, i - d);
   int32_t lmax = 2;
@@ -289,12 +293,8 @@ __global__ void k_karras(const uint32_t* __restrict__ mk, int32_t L, const int32
 
 // escape(node covering leaves [a, b]) = right child of the split after b
 // (the unique internal node whose left subtree ends at b), or end.
-__global__ void k_escapes(Node* __restrict__ nodes, const int32_t* __restrict__ right_of,
-                          const int32_t* __restrict__ last_of, int32_t nl) {
-  int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= 2 * nl - 1) return;
-  int32_t last = k < nl - 1 ? last_of[k] : k - (nl - 1);
-  nodes[k].escape = last >= nl - 1 ? kEnd : right_of[last];
+__device__ __forceinline__ int32_t escape_of(int32_t last, const int32_t* __restrict__ right_of, int32_t nl) {
+  return last >= nl - 1 ? kEnd : __ldg(right_of + last);
 }
 
 __device__ __forceinline__ void load_summary(const Node* p, float4& box, int64_t& z, uint32_t& id, uint32_t& pos,
@@ -307,10 +307,13 @@ __device__ __forceinline__ void load_summary(const Node* p, float4& box, int64_t
   cnt = __ldcg(&p->count);
 }
 
+// Bottom-up refit; every node also gets its escape link here (the thread
+// that starts at a leaf, and the second arrival at an internal node).
 __global__ void k_refit(Node* __restrict__ nodes, const int32_t* __restrict__ parent, int32_t* __restrict__ flags,
-                        int32_t nl) {
+                        const int32_t* __restrict__ right_of, const int32_t* __restrict__ last_of, int32_t nl) {
   int32_t li = blockIdx.x * blockDim.x + threadIdx.x;
   if (li >= nl) return;
+  nodes[nl - 1 + li].escape = escape_of(li, right_of, nl);
   int32_t n = parent[nl - 1 + li];
   // a root path has at most nl-1 internal nodes; the bound guards corruption
   for (int32_t guard = 0; n >= 0 && guard < nl; ++guard) {
@@ -332,6 +335,7 @@ __global__ void k_refit(Node* __restrict__ nodes, const int32_t* __restrict__ pa
     __stcg(&o->min_id, bl ? ib : ia);
     __stcg(&o->min_pos, bl ? pb : pa);
     __stcg(&o->count, ca + cb);
+    o->escape = escape_of(__ldg(last_of + n), right_of, nl);
     n = parent[n];
   }
 }
@@ -572,12 +576,10 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   }
 
   if (nl > 1) {
-    OWM_CUDA_TRY(cudaMemsetAsync(parent, 0xFF, (size_t)nnodes * 4, s));
-    OWM_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)nl * 4, s));
-    OWM_LAUNCH("k_karras", s, k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, t->nodes, parent, right_of, last_of));
-    OWM_LAUNCH("k_escapes", s, k_escapes<<<(unsigned)((nnodes + 255) / 256), 256, 0, s>>>(t->nodes, right_of, last_of, nl));
-    OWM_LAUNCH("k_refit", s, k_refit<<<(nl + 255) / 256, 256, 0, s>>>(t->nodes, parent, flags, nl));
-    count_launch(launches, 3);
+    OWM_LAUNCH("k_karras", s, k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, t->nodes, parent,
+                                                                           right_of, last_of, flags));
+    OWM_LAUNCH("k_refit", s, k_refit<<<(nl + 255) / 256, 256, 0, s>>>(t->nodes, parent, flags, right_of, last_of, nl));
+    count_launch(launches, 2);
   }
   t->max_leaf = fixed ? L : -1;
   OWM_CUDA_TRY(cudaGetLastError());

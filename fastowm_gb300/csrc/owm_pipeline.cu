@@ -115,17 +115,17 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   const int64_t nc = p.ncells, ng = std::max<int64_t>(p.ngrid, 0);
   rc = tree_alloc(&c->tree, &c->tree_mem, n, cfg.tree, c->stream);
   if (rc) return rc;
-  // scratch = [tree build | window classes | stage 2], stage 3 over the
-  // class scratch once stages 1 and 2 are done.  Stage 2 and stage 3's LLP
-  // marks may run beside the hierarchy build, so they stay clear of the
-  // build's scratch; stage 2's bitmaps stay clear of the class scratch too,
-  // so that they can be zeroed while the gather folds into the classes.
+  // scratch = [tree build | window classes | stage 2 | stage 3], disjoint:
+  // the side stream zeroes stage 2's bitmaps and prepares stage 3's edge
+  // tables while the tree is built, and runs stages 1-2 and stage 3's LLP
+  // marks beside the hierarchy build.
   const size_t tbytes = (tree_scratch_bytes(n) + 255) & ~(size_t)255;
   const size_t cbytes = cfg.stage1_walk ? 0 : (classes_scratch_bytes(n, (int32_t)p.ncols, (int32_t)p.nrows) + 255) &
                                                   ~(size_t)255;
   const bool bitmap2 = p.overlap > 0.0;
   const size_t s2bytes = bitmap2 ? stage2_bitmap_scratch_bytes(n) : stage2_scratch_bytes(nc);
-  size_t sbytes = tbytes + std::max(cbytes + s2bytes, stage3_scratch_bytes(ng));
+  const size_t s2al = (s2bytes + 255) & ~(size_t)255;
+  size_t sbytes = tbytes + cbytes + s2al + stage3_scratch_bytes(ng);
   rc = c->scratch.reserve(sbytes, c->stream);
   if (rc) return rc;
   size_t obytes = 2 * al(65536 * sizeof(Edge)) + 2 * al((size_t)nc * 4) + al((size_t)std::max<int64_t>(ng, 1) * 4) +
@@ -166,8 +166,10 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     if (!rc)
       rc = classes_prepare(p, ex, ey, static_cast<char*>(c->scratch.ptr) + tbytes, cbytes, n, &cls, ss, &c->launches);
     if (!rc && bitmap2)
-      rc = stage2_bitmap_clear(static_cast<char*>(c->scratch.ptr) + tbytes + cbytes, c->scratch.cap - tbytes - cbytes,
-                               n, ss);
+      rc = stage2_bitmap_clear(static_cast<char*>(c->scratch.ptr) + tbytes + cbytes, s2al, n, ss);
+    if (!rc)
+      rc = run_stage3_prepare(bb.min_x, bb.min_y, p, static_cast<char*>(c->scratch.ptr) + tbytes + cbytes + s2al,
+                              c->scratch.cap - tbytes - cbytes - s2al, ss, &c->launches);
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   bool fused = false;
@@ -177,9 +179,9 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
                     &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr,
                     forked ? c->ev[6] : nullptr);
   void* s2scratch = static_cast<char*>(c->scratch.ptr) + tbytes + cbytes;
-  const size_t s2cap = c->scratch.cap - tbytes - cbytes;
-  void* s3scratch = static_cast<char*>(c->scratch.ptr) + tbytes;
-  const size_t s3cap = c->scratch.cap - tbytes;
+  const size_t s2cap = s2al;
+  void* s3scratch = static_cast<char*>(c->scratch.ptr) + tbytes + cbytes + s2al;
+  const size_t s3cap = c->scratch.cap - tbytes - cbytes - s2al;
   auto stage2 = [&](cudaStream_t st) {
     return bitmap2 ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, st, &c->launches, forked)
                    : run_stage2(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, st, &c->launches);
@@ -196,7 +198,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[2], ss));
     if (!rc) rc = stage2(ss);
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[3], ss));
-    if (!rc) rc = run_stage3_mark(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
+    if (!rc) rc = run_stage3_mark(d_xyz, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   // join (again, if the gather already did): nothing queued on s after this

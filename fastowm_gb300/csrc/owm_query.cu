@@ -879,16 +879,24 @@ S3Layout stage3_layout(void* scratch, int64_t ng) {
 }
 }  // namespace
 
-int run_stage3_mark(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
-                    const uint32_t* d_nllp, int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s,
-                    int64_t* launches) {
+int run_stage3_prepare(double ox, double oy, const owm_params& p, void* scratch, size_t scratch_bytes,
+                       cudaStream_t s, int64_t* launches) {
   const int64_t ng = p.ngrid;
   if (p.bsize == 0 || ng <= 0) return OWM_OK;
   if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
   const S3Layout L = stage3_layout(scratch, ng);
-  int rc = compute_edges(p, t.ox, t.oy, true, L.ex, L.ey, s, launches);
+  int rc = compute_edges(p, ox, oy, true, L.ex, L.ey, s, launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemsetAsync(L.mark, 0, (size_t)ng, s));
+  return OWM_OK;
+}
+
+int run_stage3_mark(const double* d_xyz, const owm_params& p, const uint32_t* d_llp, const uint32_t* d_nllp,
+                    int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches) {
+  const int64_t ng = p.ngrid;
+  if (p.bsize == 0 || ng <= 0) return OWM_OK;
+  if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
+  const S3Layout L = stage3_layout(scratch, ng);
   if (llp_cap > 0) {
     OWM_LAUNCH("k_s3_mark", s, k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, L.ex, L.ey,
                                                                        (int32_t)p.ncols_grid, (int32_t)p.nrows_grid,
@@ -932,7 +940,8 @@ int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, cons
                const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
                size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches) {
   (void)d_job_slot;
-  int rc = run_stage3_mark(t, d_xyz, p, d_llp, d_nllp, llp_cap, scratch, scratch_bytes, s, launches);
+  int rc = run_stage3_prepare(t.ox, t.oy, p, scratch, scratch_bytes, s, launches);
+  if (!rc) rc = run_stage3_mark(d_xyz, p, d_llp, d_nllp, llp_cap, scratch, scratch_bytes, s, launches);
   if (rc) return rc;
   return run_stage3_query(t, p, d_out, d_count, scratch, scratch_bytes, status, s, launches);
 }

@@ -72,11 +72,14 @@ size_t stage3_scratch_bytes(int64_t ngrid);
 int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
                const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
                size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches);
-// The same in two parts on one scratch layout: the cell edges and LLP marks
-// (needs no tree hierarchy), then the queries and the compaction.
-int run_stage3_mark(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
-                    const uint32_t* d_nllp, int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s,
-                    int64_t* launches);
+// The same in three parts on one scratch layout: the cell edge tables (float
+// offsets from (ox, oy), the tree's origin) and cleared marks (need nothing
+// else), the LLP marks (need stage 2's list), then the queries and the
+// compaction (need the tree hierarchy).
+int run_stage3_prepare(double ox, double oy, const owm_params& p, void* scratch, size_t scratch_bytes,
+                       cudaStream_t s, int64_t* launches);
+int run_stage3_mark(const double* d_xyz, const owm_params& p, const uint32_t* d_llp, const uint32_t* d_nllp,
+                    int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
 int run_stage3_query(const TreeView& t, const owm_params& p, uint32_t* d_out, uint32_t* d_count, void* scratch,
                      size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches);
 
