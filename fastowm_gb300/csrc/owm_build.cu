@@ -253,6 +253,14 @@ __device__ __forceinline__ int delta(const uint32_t* __restrict__ mk, int32_t L,
   return __clzll((long long)(a ^ b));
 }
 
+// Key of every leaf's first point, packed (the hierarchy's binary searches
+// then share cache lines instead of reading one sector per key).
+__global__ void k_leaf_keys(const uint32_t* __restrict__ mk, int32_t L, const int32_t* __restrict__ starts,
+                            int32_t nl, uint32_t* __restrict__ lk) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nl) lk[i] = __ldg(mk + leaf_first(i, L, starts));
+}
+
 // Karras (2012), Sec. 4: internal node i covers leaves [min(i,j), max(i,j)]
 // and splits after gamma.  Internal nodes are 0..nl-2, leaf li is nl-1+li.
 // Also readies k_refit: the root's parent is -1 and every internal node's
@@ -576,10 +584,13 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   }
 
   if (nl > 1) {
-    OWM_LAUNCH("k_karras", s, k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, t->nodes, parent,
+    // the sort's other key buffer is free now: leaf keys there
+    uint32_t* lk = alt ? k0 : k1;
+    OWM_LAUNCH("k_leaf_keys", s, k_leaf_keys<<<(nl + 255) / 256, 256, 0, s>>>(mk, L, lstarts, nl, lk));
+    OWM_LAUNCH("k_karras", s, k_karras<<<(nl - 1 + 255) / 256, 256, 0, s>>>(lk, 1, nullptr, nl, t->nodes, parent,
                                                                            right_of, last_of, flags));
     OWM_LAUNCH("k_refit", s, k_refit<<<(nl + 255) / 256, 256, 0, s>>>(t->nodes, parent, flags, right_of, last_of, nl));
-    count_launch(launches, 2);
+    count_launch(launches, 3);
   }
   t->max_leaf = fixed ? L : -1;
   OWM_CUDA_TRY(cudaGetLastError());
