@@ -810,6 +810,9 @@ int BatchRun::init(int dev, cudaStream_t s) {
     own_stream = true;
   }
   OWM_CUDA_TRY(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+  OWM_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&ev_fork, &ev_cls, &ev_gather, &ev_join})
+    OWM_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   return OWM_OK;
 }
 
@@ -827,6 +830,15 @@ void BatchRun::destroy() {
   stage_cap = 0;
   if (done) cudaEventDestroy(done);
   done = nullptr;
+  if (side) {
+    cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
+  }
+  side = nullptr;
+  for (cudaEvent_t* e : {&ev_fork, &ev_cls, &ev_gather, &ev_join}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
   if (own_stream && stream) cudaStreamDestroy(stream);
   stream = nullptr;
   cudaGetLastError();
@@ -1063,8 +1075,53 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     uint32_t* llp = (uint32_t*)at(P.o_llp);
     uint32_t* s3 = (uint32_t*)at(P.o_s3);
     int rc2 = OWM_OK;
+    // side-stream schedule (stage 1 by classes): ss forks from s, prepares the
+    // tables while s sorts, and finishes stages 1-2 and the LLP marks while s
+    // builds the hierarchies; without classes everything runs on s
+    const bool two = P.classes && side != nullptr;
+    cudaStream_t ss = two ? side : s;
+    bool forked = false;
+    const int64_t NW = P.nwin;
+    const int64_t NC = P.ncell;
     do {
       if (cudaMemsetAsync(words, 0, 256, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      if (two) {
+        if (cudaEventRecord(ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(ss, ev_fork, 0) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
+        }
+        forked = true;
+      }
+      // edge tables (before the gather: the class fold needs the window edges)
+      if (P.ex) OWM_LAUNCH("k_b_edges", ss, k_b_edges<<<(unsigned)((P.ex + 127) / 128), 128, 0, ss>>>(0, 0, d_meta, d_exoff, ntiles, P.ex, E_wx));
+      if (P.ey) OWM_LAUNCH("k_b_edges", ss, k_b_edges<<<(unsigned)((P.ey + 127) / 128), 128, 0, ss>>>(0, 1, d_meta, d_eyoff, ntiles, P.ey, E_wy));
+      if (P.cx) OWM_LAUNCH("k_b_edges", ss, k_b_edges<<<(unsigned)((P.cx + 127) / 128), 128, 0, ss>>>(1, 0, d_meta, d_cxoff, ntiles, P.cx, E_cx));
+      if (P.cy) OWM_LAUNCH("k_b_edges", ss, k_b_edges<<<(unsigned)((P.cy + 127) / 128), 128, 0, ss>>>(1, 1, d_meta, d_cyoff, ntiles, P.cy, E_cy));
+      count_launch(L, (P.ex > 0) + (P.ey > 0) + (P.cx > 0) + (P.cy > 0));
+      if (P.classes) {
+        const dim3 gp((unsigned)P.cls_grid_x, (unsigned)ntiles);
+        OWM_LAUNCH("k_bc_split", ss, k_bc_split<<<gp, 256, 0, ss>>>(d_cls, d_meta, E_wx, E_wy));
+        OWM_LAUNCH("k_bc_prep", ss, k_bc_prep<<<gp, 256, 0, ss>>>(d_cls));
+        count_launch(L, 2);
+        if (cudaMemsetAsync(at(P.o_ccount), 0, (size_t)P.nsub * 4, ss) != cudaSuccess ||
+            cudaMemsetAsync(at(P.o_czid), 0xFF, (size_t)P.nsub * 16, ss) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
+        }
+      }
+      // stage 2/3 buffers cleared ahead of time
+      if (cudaMemsetAsync(cnt2, 0, T1 * 4, ss) != cudaSuccess || cudaMemsetAsync(cnt3, 0, T1 * 4, ss) != cudaSuccess) {
+        rc2 = OWM_ECUDA;
+        break;
+      }
+      if (NW > 0 && P.s2_bitmap &&
+          cudaMemsetAsync(at(P.o_bm1), 0, (size_t)(P.o_bm2 - P.o_bm1) + (size_t)P.bm_words * 4, ss) != cudaSuccess) {
+        rc2 = OWM_ECUDA;
+        break;
+      }
+      if (NC > 0 && cudaMemsetAsync(mark, 0, (size_t)NC, ss) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+      if (two && cudaEventRecord(ev_cls, ss) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+
       const int key_bits = P.tile_bits + 2 * P.mbits;
       const RadixSortPlan sp = radix_sort_plan(N);
       if (sp.parts) {  // the Morton pass also counts the sort's first digit
@@ -1079,23 +1136,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
                      sp.parts > 0) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
       const uint32_t* mk = alt ? k1 : k0;
       const uint32_t* perm = alt ? v1 : v0;
-      // edge tables (before the gather: the class fold needs the window edges)
-      if (P.ex) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ex + 127) / 128), 128, 0, s>>>(0, 0, d_meta, d_exoff, ntiles, P.ex, E_wx));
-      if (P.ey) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.ey + 127) / 128), 128, 0, s>>>(0, 1, d_meta, d_eyoff, ntiles, P.ey, E_wy));
-      if (P.cx) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cx + 127) / 128), 128, 0, s>>>(1, 0, d_meta, d_cxoff, ntiles, P.cx, E_cx));
-      if (P.cy) OWM_LAUNCH("k_b_edges", s, k_b_edges<<<(unsigned)((P.cy + 127) / 128), 128, 0, s>>>(1, 1, d_meta, d_cyoff, ntiles, P.cy, E_cy));
-      count_launch(L, (P.ex > 0) + (P.ey > 0) + (P.cx > 0) + (P.cy > 0));
-      if (P.classes) {
-        const dim3 gp((unsigned)P.cls_grid_x, (unsigned)ntiles);
-        OWM_LAUNCH("k_bc_split", s, k_bc_split<<<gp, 256, 0, s>>>(d_cls, d_meta, E_wx, E_wy));
-        OWM_LAUNCH("k_bc_prep", s, k_bc_prep<<<gp, 256, 0, s>>>(d_cls));
-        count_launch(L, 2);
-        if (cudaMemsetAsync(at(P.o_ccount), 0, (size_t)P.nsub * 4, s) != cudaSuccess ||
-            cudaMemsetAsync(at(P.o_czid), 0xFF, (size_t)P.nsub * 16, s) != cudaSuccess) {
-          rc2 = OWM_ECUDA;
-          break;
-        }
-      }
+      if (two && cudaStreamWaitEvent(s, ev_cls, 0) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
       {
         // one warp per leaf: resident warps then work on neighbouring leaves
         int64_t blocks = std::min<int64_t>((P.nleaves * 32 + 255) / 256, (int64_t)152 * 1024);
@@ -1103,6 +1144,23 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
             xyz, perm, d_meta, d_leafoff, ntiles, P.nleaves, xk, yk, zk, pid, nodes, words, d_cls));
         count_launch(L);
       }
+      if (two && (cudaEventRecord(ev_gather, s) != cudaSuccess || cudaStreamWaitEvent(ss, ev_gather, 0) != cudaSuccess)) {
+        rc2 = OWM_ECUDA;
+        break;
+      }
+      // stage 1: window classes (rows, windows) on ss, or the persistent walk
+      // (on s, after the hierarchies, below)
+      if (P.classes) {
+        if (P.rows_total > 0) {
+          OWM_LAUNCH("k_bc_rows", ss, k_bc_rows<<<gsz(P.rows_total), 256, 0, ss>>>(d_cls, d_rowsoff, ntiles, P.rows_total));
+          count_launch(L);
+        }
+        if (NW > 0) {
+          OWM_LAUNCH("k_bc_windows", ss, k_bc_windows<<<gsz(NW), 256, 0, ss>>>(d_cls, d_meta, d_winoff, ntiles, NW, win));
+          count_launch(L);
+        }
+      }
+      // hierarchies on s
       if (cudaMemsetAsync(parent, 0xFF, (size_t)P.nnodes * 4, s) != cudaSuccess ||
           cudaMemsetAsync(flags, 0, (size_t)std::max<int64_t>(P.ninternal, 1) * 4, s) != cudaSuccess) {
         rc2 = OWM_ECUDA;
@@ -1118,78 +1176,64 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       OWM_LAUNCH("k_b_refit", s, k_b_refit<<<(unsigned)((P.nleaves + 255) / 256), 256, 0, s>>>(
           nodes, parent, flags, d_meta, d_leafoff, ntiles, P.nleaves));
       count_launch(L, 2);
-      // stage 1: window classes (tie ids, rows, windows), or the persistent walk
-      if (P.classes) {
-        if (P.rows_total > 0) {
-          OWM_LAUNCH("k_bc_rows", s, k_bc_rows<<<gsz(P.rows_total), 256, 0, s>>>(d_cls, d_rowsoff, ntiles, P.rows_total));
-          count_launch(L);
-        }
-        if (P.nwin > 0) {
-          OWM_LAUNCH("k_bc_windows", s, k_bc_windows<<<gsz(P.nwin), 256, 0, s>>>(d_cls, d_meta, d_winoff, ntiles, P.nwin, win));
-          count_launch(L);
-        }
-      } else if (launch_query_persistent(d_j1, ntiles, w1, qnext, 152 * 16, s, L, "k_query_s1_batch")) {
+      if (!P.classes && launch_query_persistent(d_j1, ntiles, w1, qnext, 152 * 16, s, L, "k_query_s1_batch")) {
         rc2 = OWM_ECUDA;
         break;
       }
-      // stage 2 on (tile, id) keys
-      const int64_t NW = P.nwin;
+      // stage 2 on (tile, id) keys, on ss
       const uint32_t none = (P.idbits >= 32) ? 0xFFFFFFFFu : ((1u << P.idbits) - 1u);
       uint32_t* s2k0 = (uint32_t*)at(P.o_s2k0);
       uint32_t* s2k1 = (uint32_t*)at(P.o_s2k1);
       uint32_t* s2f = (uint32_t*)at(P.o_s2f);
       uint32_t* s2p = (uint32_t*)at(P.o_s2p);
       char* s2t = at(P.o_s2t);
-      if (cudaMemsetAsync(cnt2, 0, T1 * 4, s) != cudaSuccess || cudaMemsetAsync(cnt3, 0, T1 * 4, s) != cudaSuccess) {
-        rc2 = OWM_ECUDA;
-        break;
-      }
       if (NW > 0 && P.s2_bitmap) {
         const int64_t BW = P.bm_words;
         uint32_t* bm1 = (uint32_t*)at(P.o_bm1);
         uint32_t* bm2 = (uint32_t*)at(P.o_bm2);
         uint32_t* bmc = (uint32_t*)at(P.o_bmc);
         uint32_t* bmp = (uint32_t*)at(P.o_bmp);
-        if (cudaMemsetAsync(bm1, 0, (size_t)(P.o_bm2 - P.o_bm1) + (size_t)BW * 4, s) != cudaSuccess) {
-          rc2 = OWM_ECUDA;
-          break;
-        }
-        OWM_LAUNCH("k_b_s2_mark", s, k_b_s2_mark<<<gsz(NW), 256, 0, s>>>(win, NW, d_winoff, ntiles, d_meta, bm1, bm2));
-        OWM_LAUNCH("k_b_s2_popc", s, k_b_s2_popc<<<gsz(BW), 256, 0, s>>>(bm2, BW, bmc));
+        OWM_LAUNCH("k_b_s2_mark", ss, k_b_s2_mark<<<gsz(NW), 256, 0, ss>>>(win, NW, d_winoff, ntiles, d_meta, bm1, bm2));
+        OWM_LAUNCH("k_b_s2_popc", ss, k_b_s2_popc<<<gsz(BW), 256, 0, ss>>>(bm2, BW, bmc));
         count_launch(L, 2);
-        if (exclusive_scan_u32(bmc, bmp, BW, words + 1, at(P.o_bmt), scan_temp_bytes(BW) + 256, s, L) != cudaSuccess) {
+        if (exclusive_scan_u32(bmc, bmp, BW, words + 1, at(P.o_bmt), scan_temp_bytes(BW) + 256, ss, L) != cudaSuccess) {
           rc2 = OWM_ECUDA;
           break;
         }
-        OWM_LAUNCH("k_b_s2_emit", s, k_b_s2_emit<<<gsz(BW), 256, 0, s>>>(bm2, bmp, BW, d_bmoff, ntiles, P.idbits, llp));
-        OWM_LAUNCH("k_b_s2_tilecount", s, k_b_s2_tilecount<<<(ntiles + 255) / 256, 256, 0, s>>>(bmp, d_bmoff, ntiles, BW,
-                                                                                             words + 1, cnt2));
+        OWM_LAUNCH("k_b_s2_emit", ss, k_b_s2_emit<<<gsz(BW), 256, 0, ss>>>(bm2, bmp, BW, d_bmoff, ntiles, P.idbits, llp));
+        OWM_LAUNCH("k_b_s2_tilecount", ss, k_b_s2_tilecount<<<(ntiles + 255) / 256, 256, 0, ss>>>(bmp, d_bmoff, ntiles, BW,
+                                                                                               words + 1, cnt2));
         count_launch(L, 2);
       } else if (NW > 0) {
-        OWM_LAUNCH("k_b_s2_keys", s, k_b_s2_keys<<<gsz(NW), 256, 0, s>>>(win, NW, d_winoff, ntiles, P.idbits, none, s2k0));
+        OWM_LAUNCH("k_b_s2_keys", ss, k_b_s2_keys<<<gsz(NW), 256, 0, ss>>>(win, NW, d_winoff, ntiles, P.idbits, none, s2k0));
         count_launch(L);
         bool a2 = false;
         size_t sb = radix_sort_temp_bytes(NW);
-        if (radix_sort(s2k0, nullptr, s2k1, nullptr, NW, P.tile_bits + P.idbits, false, s2t, sb, s, &a2, L) !=
+        if (radix_sort(s2k0, nullptr, s2k1, nullptr, NW, P.tile_bits + P.idbits, false, s2t, sb, ss, &a2, L) !=
             cudaSuccess) { rc2 = OWM_ECUDA; break; }
         const uint32_t* sk = a2 ? s2k1 : s2k0;
-        OWM_LAUNCH("k_b_s2_flags", s, k_b_s2_flags<<<gsz(NW), 256, 0, s>>>(sk, NW, P.idbits, none, d_meta, s2f, cnt2));
+        OWM_LAUNCH("k_b_s2_flags", ss, k_b_s2_flags<<<gsz(NW), 256, 0, ss>>>(sk, NW, P.idbits, none, d_meta, s2f, cnt2));
         count_launch(L);
         if (exclusive_scan_u32(s2f, s2p, NW, words + 1, s2t + a256(sb), scan_temp_bytes(std::max<int64_t>(NW, P.ncell)) + 256,
-                               s, L) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
-        OWM_LAUNCH("k_b_compact", s, k_b_compact<<<gsz(NW), 256, 0, s>>>(sk, s2f, s2p, NW, llp));
+                               ss, L) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
+        OWM_LAUNCH("k_b_compact", ss, k_b_compact<<<gsz(NW), 256, 0, ss>>>(sk, s2f, s2p, NW, llp));
         count_launch(L);
       }
-      if (exclusive_scan_u32(cnt2, llp_off, ntiles + 1, nullptr, s2t, scan_temp_bytes(ntiles + 1) + 256, s, L) !=
+      if (exclusive_scan_u32(cnt2, llp_off, ntiles + 1, nullptr, s2t, scan_temp_bytes(ntiles + 1) + 256, ss, L) !=
           cudaSuccess) { rc2 = OWM_ECUDA; break; }
-      // stage 3
-      const int64_t NC = P.ncell;
-      if (NC > 0) {
-        if (cudaMemsetAsync(mark, 0, (size_t)NC, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
-        if (NW > 0) {
-          OWM_LAUNCH("k_b_s3_mark", s, k_b_s3_mark<<<gsz(NW), 256, 0, s>>>(xyz, llp, words + 1, NW, P.idbits, d_meta, E_cx, E_cy, mark));
-          count_launch(L);
+      // stage 3: LLP marks on ss; queries on s once both streams are done
+      if (NC > 0 && NW > 0) {
+        OWM_LAUNCH("k_b_s3_mark", ss, k_b_s3_mark<<<gsz(NW), 256, 0, ss>>>(xyz, llp, words + 1, NW, P.idbits, d_meta, E_cx, E_cy, mark));
+        count_launch(L);
+      }
+      if (two) {
+        if (cudaEventRecord(ev_join, ss) != cudaSuccess || cudaStreamWaitEvent(s, ev_join, 0) != cudaSuccess) {
+          rc2 = OWM_ECUDA;
+          break;
         }
+        forked = false;
+      }
+      if (NC > 0) {
         if (launch_query_persistent(d_j3, ntiles, w3, qnext, 152 * 16, s, L, "k_query_s3_batch")) { rc2 = OWM_ECUDA; break; }
         uint32_t* cf = (uint32_t*)at(P.o_cf);
         uint32_t* cp = (uint32_t*)at(P.o_cp);
@@ -1209,6 +1253,10 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       if (cudaMemcpyAsync(h_off, d_outoff, T1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
       if (cudaMemcpyAsync(h_off + T1, words, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
     } while (false);
+    if (forked) {  // an error left the side stream forked: join it (a capture must end joined)
+      cudaEventRecord(ev_join, ss);
+      cudaStreamWaitEvent(s, ev_join, 0);
+    }
     if (capture) {
       cudaGraph_t g = nullptr;
       cudaError_t e = cudaStreamEndCapture(stream, &g);

@@ -66,6 +66,12 @@ struct BatchRun {
   uint32_t* d_status = nullptr;
   size_t bytes_needed = 0;
   cudaEvent_t done = nullptr;
+  // With stage 1 by window classes, a side stream prepares the edge and class
+  // tables and clears the stage-2/3 buffers while the keys are sorted, then
+  // runs stages 1-2 and stage 3's LLP marks while `stream` builds the
+  // hierarchies (fork, tables ready, gather done, join).
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_cls = nullptr, ev_gather = nullptr, ev_join = nullptr;
 
   int init(int device, cudaStream_t s);
   void destroy();
