@@ -26,6 +26,7 @@
 #include <cstring>
 
 #include "owm_batch.cuh"
+#include "owm_cellq.cuh"
 #include "owm_classes.cuh"
 #include "owm_devutil.cuh"
 
@@ -260,16 +261,20 @@ __device__ __forceinline__ int bdelta(const uint32_t* __restrict__ mk, const Til
 }
 
 // Karras (2012) per tile; indices stored local to the tile.
+// Also readies k_b_refit: each tile's root has parent -1 and every internal
+// node's arrival counter starts at 0.
 __global__ void k_b_karras(const uint32_t* __restrict__ mk, const TileMeta* __restrict__ meta,
                            const int32_t* __restrict__ int_off, int ntiles, int64_t total_internal,
                            Node* __restrict__ nodes, int32_t* __restrict__ parent, int32_t* __restrict__ right_of,
-                           int32_t* __restrict__ last_of) {
+                           int32_t* __restrict__ last_of, int32_t* __restrict__ flags) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= total_internal) return;
   const int t = tile_of(int_off, ntiles, q);
   const TileMeta& m = meta[t];
   const int32_t i = (int32_t)(q - m.int_off);
   const int32_t nl = m.nleaves;
+  flags[q] = 0;
+  if (i == 0) parent[m.node_off] = -1;  // no node of the tile has its root as a child
   int d = bdelta(mk, m, i, i + 1) - bdelta(mk, m, i, i - 1) > 0 ? 1 : -1;
   int dmin = bdelta(mk, m, i, i - d);
   int32_t lmax = 2;
@@ -298,19 +303,11 @@ __global__ void k_b_karras(const uint32_t* __restrict__ mk, const TileMeta* __re
   last_of[m.int_off + i] = hi;
 }
 
-__global__ void k_b_escapes(Node* __restrict__ nodes, const int32_t* __restrict__ right_of,
-                            const int32_t* __restrict__ last_of, const TileMeta* __restrict__ meta,
-                            const int32_t* __restrict__ node_off, int ntiles, int64_t total_nodes) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= total_nodes) return;
-  const int t = tile_of(node_off, ntiles, k);
-  const TileMeta& m = meta[t];
-  const int32_t kl = (int32_t)(k - m.node_off), nl = m.nleaves;
-  const int32_t last = kl < nl - 1 ? last_of[m.int_off + kl] : kl - (nl - 1);
-  nodes[k].escape = last >= nl - 1 ? kEnd : right_of[m.leaf_off + last];
-}
-
+// Bottom-up refit of every tile's hierarchy; every node also gets its escape
+// link (the right child of the split after its last leaf, or end) from the
+// thread that starts at a leaf or arrives second at an internal node.
 __global__ void k_b_refit(Node* __restrict__ nodes, const int32_t* __restrict__ parent, int32_t* __restrict__ flags,
+                          const int32_t* __restrict__ right_of, const int32_t* __restrict__ last_of,
                           const TileMeta* __restrict__ meta, const int32_t* __restrict__ leaf_off, int ntiles,
                           int64_t total_leaves) {
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -319,7 +316,10 @@ __global__ void k_b_refit(Node* __restrict__ nodes, const int32_t* __restrict__ 
   const TileMeta& m = meta[t];
   Node* base = nodes + m.node_off;
   const int32_t li = (int32_t)(g - m.leaf_off);
-  int32_t n = parent[m.node_off + m.nleaves - 1 + li];
+  const int32_t nl = m.nleaves;
+  base[nl - 1 + li].escape = li >= nl - 1 ? kEnd : __ldg(right_of + m.leaf_off + li);
+  if (nl <= 1) return;  // a one-leaf tile: the leaf is the root
+  int32_t n = parent[m.node_off + nl - 1 + li];
   for (int32_t guard = 0; n >= 0 && guard < m.nleaves; ++guard) {
     __threadfence();
     if (atomicAdd(&flags[m.int_off + n], 1) == 0) return;
@@ -339,8 +339,31 @@ __global__ void k_b_refit(Node* __restrict__ nodes, const int32_t* __restrict__ 
     __stcg(&o->min_id, bl ? ib : ia);
     __stcg(&o->min_pos, bl ? pb : pa);
     __stcg(&o->count, ca + cb);
+    const int32_t last = __ldg(last_of + m.int_off + n);
+    o->escape = last >= nl - 1 ? kEnd : __ldg(right_of + m.leaf_off + last);
     n = parent[m.node_off + n];
   }
+}
+
+// Stage 3 of all tiles: one warp per grid cell of any tile (cell_off gives
+// each tile's first cell), answered by the tile's stage-3 job; marked cells
+// are skipped at once.
+__global__ void __launch_bounds__(kS3Warps * 32) k_b_query_cells(const QueryJob* __restrict__ jobs,
+                                                                   const int64_t* __restrict__ cell_off, int ntiles,
+                                                                   int64_t total_cells) {
+  __shared__ int32_t stack_all[kS3Warps][kS3Stack];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * kS3Warps + wib;
+  if (c >= total_cells) return;  // warp-uniform
+  const int t = tile_of(cell_off, ntiles, c);
+  const QueryJob& J = jobs[t];
+  const int64_t k = c - __ldg(cell_off + t);
+  if (J.skip && J.skip[k]) {
+    if (lane == 0) J.out[k] = kNone;
+    return;
+  }
+  const uint32_t r = cell_min_warp(J.tree, J.ex[k % J.ncols], J.ey[k / J.ncols], stack_all[wib], J.status, lane);
+  if (lane == 0) J.out[k] = r;
 }
 
 __device__ __forceinline__ Edge bedge(double lo, double hi, double o) {
@@ -1161,21 +1184,14 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
         }
       }
       // hierarchies on s
-      if (cudaMemsetAsync(parent, 0xFF, (size_t)P.nnodes * 4, s) != cudaSuccess ||
-          cudaMemsetAsync(flags, 0, (size_t)std::max<int64_t>(P.ninternal, 1) * 4, s) != cudaSuccess) {
-        rc2 = OWM_ECUDA;
-        break;
-      }
       if (P.ninternal > 0) {
         OWM_LAUNCH("k_b_karras", s, k_b_karras<<<(unsigned)((P.ninternal + 255) / 256), 256, 0, s>>>(
-            mk, d_meta, d_intoff, ntiles, P.ninternal, nodes, parent, right_of, last_of));
+            mk, d_meta, d_intoff, ntiles, P.ninternal, nodes, parent, right_of, last_of, flags));
         count_launch(L);
       }
-      OWM_LAUNCH("k_b_escapes", s, k_b_escapes<<<(unsigned)((P.nnodes + 255) / 256), 256, 0, s>>>(
-          nodes, right_of, last_of, d_meta, d_nodeoff, ntiles, P.nnodes));
       OWM_LAUNCH("k_b_refit", s, k_b_refit<<<(unsigned)((P.nleaves + 255) / 256), 256, 0, s>>>(
-          nodes, parent, flags, d_meta, d_leafoff, ntiles, P.nleaves));
-      count_launch(L, 2);
+          nodes, parent, flags, right_of, last_of, d_meta, d_leafoff, ntiles, P.nleaves));
+      count_launch(L);
       if (!P.classes && launch_query_persistent(d_j1, ntiles, w1, qnext, 152 * 16, s, L, "k_query_s1_batch")) {
         rc2 = OWM_ECUDA;
         break;
@@ -1234,7 +1250,10 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
         forked = false;
       }
       if (NC > 0) {
-        if (launch_query_persistent(d_j3, ntiles, w3, qnext, 152 * 16, s, L, "k_query_s3_batch")) { rc2 = OWM_ECUDA; break; }
+        if ((NC + kS3Warps - 1) / kS3Warps >= 0x7FFFFFFFll) { rc2 = OWM_ERANGE; break; }
+        OWM_LAUNCH("k_query_s3_batch", s, k_b_query_cells<<<(unsigned)((NC + kS3Warps - 1) / kS3Warps), kS3Warps * 32, 0, s>>>(
+            d_j3, d_celloff, ntiles, NC));
+        count_launch(L);
         uint32_t* cf = (uint32_t*)at(P.o_cf);
         uint32_t* cp = (uint32_t*)at(P.o_cp);
         OWM_LAUNCH("k_b_flag_cells", s, k_b_flag_cells<<<gsz(NC), 256, 0, s>>>(cmin, NC, d_celloff, ntiles, cf, cnt3));
