@@ -3,7 +3,7 @@
 One step = the whole path (tree build + stage 1 + stage 2 + stage 3 + seed
 copy-out) over one cloud.  Default workload: the single large cloud
 (100,000,000 FP64 points, 2 km x 2 km, Wsize 12, overlap 0.8, Bsize 20,
-leaf 32), inputs resident in HBM for `value`; `e2e` runs the same step
+leaf size picked by fastowm_gb300.autotune: 256), inputs resident in HBM for `value`; `e2e` runs the same step
 through owm_run_host from pinned host memory (host->device copy of the
 points and device->host copy of the seeds inside the timed region).
 
@@ -483,7 +483,8 @@ def run_batched(F, torch, ctx, args, local, ws):
         cap += p.ncells + p.ngrid + 1
     out = np.empty(cap, dtype=np.int64)
     offs = np.empty(len(info) + 1, dtype=np.int64)
-    tuned = autotune.tune_leaf_classes(ctx, tiles_per_class=4, reps=2)
+    # samples large enough that launch overhead does not decide the pick
+    tuned = autotune.tune_leaf_classes(ctx, tiles_per_class=16, reps=5)
     batch = F.Batch(ctx)
     autotune.apply(batch, tuned)
     batch.set_graphs(True)

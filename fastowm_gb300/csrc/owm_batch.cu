@@ -125,15 +125,28 @@ __global__ void __launch_bounds__(256) k_b_morton_counts(const double* __restric
     int64_t tend = __ldg(pt_off + t + 1);
     TileKey key;
     key.load(meta[t], t, mbits);
-    for (; i < e; i += 256) {
+    for (; i < e;) {
       while (i >= tend) {  // next tile (tiles are contiguous; empty ones skipped)
         ++t;
         tend = __ldg(pt_off + t + 1);
         key.load(meta[t], t, mbits);
       }
-      const uint32_t k = key(xyz + 3 * i);
-      keys[i] = k;
-      atomicAdd(hw + (k & 255u), 1u);
+      if (i + 3 * 256 < e && i + 3 * 256 < tend) {  // four points of this tile in flight
+        uint32_t k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) k[u] = key(xyz + 3 * (i + u * 256));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          keys[i + u * 256] = k[u];
+          atomicAdd(hw + (k[u] & 255u), 1u);
+        }
+        i += 4 * 256;
+      } else {
+        const uint32_t k = key(xyz + 3 * i);
+        keys[i] = k;
+        atomicAdd(hw + (k & 255u), 1u);
+        i += 256;
+      }
     }
   }
   __syncthreads();
@@ -253,17 +266,29 @@ __global__ void k_bc_windows(const ClassArgs* __restrict__ cls, const TileMeta* 
   }
 }
 
-__device__ __forceinline__ int bdelta(const uint32_t* __restrict__ mk, const TileMeta& m, int32_t i, int32_t j) {
+// lk: packed leaf keys (k_b_leaf_keys), lk[m.leaf_off + i] for leaf i of tile m.
+__device__ __forceinline__ int bdelta(const uint32_t* __restrict__ lk, const TileMeta& m, int32_t i, int32_t j) {
   if (j < 0 || j >= m.nleaves) return -1;
-  uint64_t a = ((uint64_t)__ldg(mk + m.pt_off + (int64_t)i * m.leaf) << 32) | (uint32_t)i;
-  uint64_t b = ((uint64_t)__ldg(mk + m.pt_off + (int64_t)j * m.leaf) << 32) | (uint32_t)j;
+  uint64_t a = ((uint64_t)__ldg(lk + m.leaf_off + i) << 32) | (uint32_t)i;
+  uint64_t b = ((uint64_t)__ldg(lk + m.leaf_off + j) << 32) | (uint32_t)j;
   return __clzll((long long)(a ^ b));
+}
+
+// Key of every leaf's first point, packed over all tiles.
+__global__ void k_b_leaf_keys(const uint32_t* __restrict__ mk, const TileMeta* __restrict__ meta,
+                              const int32_t* __restrict__ leaf_off, int ntiles, int64_t total_leaves,
+                              uint32_t* __restrict__ lk) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_leaves) return;
+  const int t = tile_of(leaf_off, ntiles, g);
+  const TileMeta& m = meta[t];
+  lk[g] = __ldg(mk + m.pt_off + (g - m.leaf_off) * m.leaf);
 }
 
 // Karras (2012) per tile; indices stored local to the tile.
 // Also readies k_b_refit: each tile's root has parent -1 and every internal
 // node's arrival counter starts at 0.
-__global__ void k_b_karras(const uint32_t* __restrict__ mk, const TileMeta* __restrict__ meta,
+__global__ void k_b_karras(const uint32_t* __restrict__ lk, const TileMeta* __restrict__ meta,
                            const int32_t* __restrict__ int_off, int ntiles, int64_t total_internal,
                            Node* __restrict__ nodes, int32_t* __restrict__ parent, int32_t* __restrict__ right_of,
                            int32_t* __restrict__ last_of, int32_t* __restrict__ flags) {
@@ -275,19 +300,19 @@ __global__ void k_b_karras(const uint32_t* __restrict__ mk, const TileMeta* __re
   const int32_t nl = m.nleaves;
   flags[q] = 0;
   if (i == 0) parent[m.node_off] = -1;  // no node of the tile has its root as a child
-  int d = bdelta(mk, m, i, i + 1) - bdelta(mk, m, i, i - 1) > 0 ? 1 : -1;
-  int dmin = bdelta(mk, m, i, i - d);
+  int d = bdelta(lk, m, i, i + 1) - bdelta(lk, m, i, i - 1) > 0 ? 1 : -1;
+  int dmin = bdelta(lk, m, i, i - d);
   int32_t lmax = 2;
-  while (bdelta(mk, m, i, i + lmax * d) > dmin) lmax <<= 1;
+  while (bdelta(lk, m, i, i + lmax * d) > dmin) lmax <<= 1;
   int32_t l = 0;
   for (int32_t s = lmax >> 1; s >= 1; s >>= 1)
-    if (bdelta(mk, m, i, i + (l + s) * d) > dmin) l += s;
+    if (bdelta(lk, m, i, i + (l + s) * d) > dmin) l += s;
   int32_t j = i + l * d;
-  int dnode = bdelta(mk, m, i, j);
+  int dnode = bdelta(lk, m, i, j);
   int32_t s = 0;
   for (int32_t div = 2;; div <<= 1) {
     int32_t st = (l + div - 1) / div;
-    if (bdelta(mk, m, i, i + (s + st) * d) > dnode) s += st;
+    if (bdelta(lk, m, i, i + (s + st) * d) > dnode) s += st;
     if (st <= 1) break;
   }
   int32_t gamma = i + s * d + (d < 0 ? -1 : 0);
@@ -1185,9 +1210,12 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       }
       // hierarchies on s
       if (P.ninternal > 0) {
+        uint32_t* lk = alt ? k0 : k1;  // the sort's other key buffer is free now
+        OWM_LAUNCH("k_b_leaf_keys", s, k_b_leaf_keys<<<(unsigned)((P.nleaves + 255) / 256), 256, 0, s>>>(
+            mk, d_meta, d_leafoff, ntiles, P.nleaves, lk));
         OWM_LAUNCH("k_b_karras", s, k_b_karras<<<(unsigned)((P.ninternal + 255) / 256), 256, 0, s>>>(
-            mk, d_meta, d_intoff, ntiles, P.ninternal, nodes, parent, right_of, last_of, flags));
-        count_launch(L);
+            lk, d_meta, d_intoff, ntiles, P.ninternal, nodes, parent, right_of, last_of, flags));
+        count_launch(L, 2);
       }
       OWM_LAUNCH("k_b_refit", s, k_b_refit<<<(unsigned)((P.nleaves + 255) / 256), 256, 0, s>>>(
           nodes, parent, flags, right_of, last_of, d_meta, d_leafoff, ntiles, P.nleaves));
