@@ -99,6 +99,16 @@ def test_window_geometry_variants(owm, oracle, ctx, W, Ov, B):
     np.testing.assert_array_equal(got, want)
 
 
+def test_large_stage3_grid(owm, oracle, ctx):
+    """2 m cells over 1100 m x 1100 m (303,601 > 2^18 cells: the multi-launch
+    ordered compaction of stage 3); sparse points, so most cells hold no LLP
+    and stage 3 answers about 227,000 of them."""
+    xyz, bb, _, _, _, _ = _cloud(owm, 1, n=600_000, w=1100, h=1100)
+    got, want, nllp = _run_both(owm, oracle, ctx, xyz, bb, 6, 0.5, 2)
+    assert len(want) - nllp > 200_000
+    np.testing.assert_array_equal(got, want)
+
+
 def test_tiny_and_degenerate_clouds(owm, oracle, ctx):
     rng = np.random.default_rng(5)
     cases = []
