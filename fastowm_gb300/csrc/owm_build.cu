@@ -3,7 +3,8 @@
 // 220-307).
 //
 //   k_morton          quantise (x, y) on the square root domain, interleave
-//                     (2D Morton / quadtree order), one 32-bit key per point
+//                     (2D Morton / quadtree order), one key of 16-24 bits per
+//                     point (choose_key_bits)
 //   radix_sort        stable LSD sort of (key, input position)
 //   k_gather_leaves   permute the points into sorted order as exact
 //                     order-preserving int64 keys + 1-based id, and reduce each
@@ -11,6 +12,7 @@
 //                     with warp shuffles -- one pass over the points
 //   k_leaf_starts /   leaves = quadtree cells of half-side <= min_radius
 //   k_leaf_reduce     (min-radius policy) or any other leaf partition
+//   k_leaf_keys       the key of every leaf's first point, packed
 //   k_karras          binary radix hierarchy over the leaves (Karras 2012) on
 //                     64-bit (leaf Morton key, leaf index) codes
 //   k_refit           bottom-up atomic refit: internal count, box and

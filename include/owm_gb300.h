@@ -250,8 +250,13 @@ typedef struct {
   int32_t _pad;
 } owm_run_cfg;
 
+/* Device time of the run (ms_total) and of its phases.  owm_run overlaps
+ * them: with stage 1 by window classes, stages 1-2 run on a second stream
+ * while the tree's hierarchy is built, so ms_stage1 counts from the end of
+ * the build's gather, ms_stage3 from the end of both streams' work, and the
+ * phases may add up to more than ms_total. */
 typedef struct {
-  double ms_tree, ms_stage1, ms_stage2, ms_stage3, ms_total; /* device time */
+  double ms_tree, ms_stage1, ms_stage2, ms_stage3, ms_total;
   int64_t n_llp, n_stage3, n_seeds;
   owm_params params;
 } owm_run_info;
