@@ -111,7 +111,7 @@ struct TileKey {
 __global__ void __launch_bounds__(256) k_b_morton_counts(const double* __restrict__ xyz, int64_t n,
                                                          const int64_t* __restrict__ pt_off,
                                                          const TileMeta* __restrict__ meta, int ntiles, int mbits,
-                                                         int64_t ntiles_sort, uint32_t* __restrict__ keys,
+                                                         int64_t ntiles_sort, uint32_t dmask0, uint32_t* __restrict__ keys,
                                                          uint32_t* __restrict__ counts) {
   __shared__ uint32_t h[8][256];
   for (int i = threadIdx.x; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
@@ -138,13 +138,13 @@ __global__ void __launch_bounds__(256) k_b_morton_counts(const double* __restric
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           keys[i + u * 256] = k[u];
-          atomicAdd(hw + (k[u] & 255u), 1u);
+          atomicAdd(hw + (k[u] & dmask0), 1u);
         }
         i += 4 * 256;
       } else {
         const uint32_t k = key(xyz + 3 * i);
         keys[i] = k;
-        atomicAdd(hw + (k & 255u), 1u);
+        atomicAdd(hw + (k & dmask0), 1u);
         i += 256;
       }
     }
@@ -1174,7 +1174,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       const RadixSortPlan sp = radix_sort_plan(N);
       if (sp.parts) {  // the Morton pass also counts the sort's first digit
         OWM_LAUNCH("k_b_morton", s, k_b_morton_counts<<<(unsigned)sp.parts, 256, 0, s>>>(
-            xyz, N, d_ptoff, d_meta, ntiles, P.mbits, sp.ntiles, k0, (uint32_t*)at(P.o_sort)));
+            xyz, N, d_ptoff, d_meta, ntiles, P.mbits, sp.ntiles, (1u << radix_digit_bits(key_bits, 0)) - 1u, k0,
+            (uint32_t*)at(P.o_sort)));
       } else {
         OWM_LAUNCH("k_b_morton", s, k_b_morton<<<gsz(N), 256, 0, s>>>(xyz, N, d_ptoff, d_meta, ntiles, P.mbits, k0));
       }

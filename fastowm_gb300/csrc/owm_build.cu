@@ -90,12 +90,12 @@ struct MortonFpKey {
 };
 
 // Morton keys of part blockIdx.x of a large sort (sort_part_range), with the
-// part's counts of the sort's first digit (bits 0..7) into
+// part's counts of the sort's first digit (key & dmask0) into
 // counts[d * gridDim.x + blockIdx.x]: the first radix pass then needs no
 // separate read of the keys.
 template <class KeyOf>
 __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict__ xyz, int64_t n, KeyOf key_of,
-                                                       int64_t ntiles, uint32_t* __restrict__ keys,
+                                                       int64_t ntiles, uint32_t dmask0, uint32_t* __restrict__ keys,
                                                        uint32_t* __restrict__ counts) {
   __shared__ uint32_t h[8][256];
   for (int i = threadIdx.x; i < 8 * 256; i += 256) (&h[0][0])[i] = 0;
@@ -111,13 +111,13 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       keys[i + u * 256] = k[u];
-      atomicAdd(hw + (k[u] & 255u), 1u);
+      atomicAdd(hw + (k[u] & dmask0), 1u);
     }
   }
   for (; i < e; i += 256) {
     const uint32_t k = key_of(xyz + 3 * i);
     keys[i] = k;
-    atomicAdd(hw + (k & 255u), 1u);
+    atomicAdd(hw + (k & dmask0), 1u);
   }
   __syncthreads();
   {
@@ -502,7 +502,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     if (plan.parts) {
       const MortonIntKey kf{kx0, ky0, (1ll << bits_axis) - 1, shx, shy};
       OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey><<<(unsigned)plan.parts, 256, 0, s>>>(
-          d_xyz, n, kf, plan.ntiles, k0, first_counts));
+          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0)) - 1u, k0, first_counts));
     } else {
       OWM_LAUNCH("k_morton", s, k_morton_int<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
     }
@@ -510,7 +510,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     if (plan.parts) {
       const MortonFpKey kf{ox, oy, scale, (float)((1u << bits_axis) - 1u)};
       OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey><<<(unsigned)plan.parts, 256, 0, s>>>(
-          d_xyz, n, kf, plan.ntiles, k0, first_counts));
+          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0)) - 1u, k0, first_counts));
     } else {
       OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
     }

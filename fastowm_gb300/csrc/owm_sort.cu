@@ -1,6 +1,6 @@
 // Device-wide primitives: exclusive scan and an on-chip-staged LSD radix sort
-// (8-bit digits, the last one narrower when the key width is not a multiple
-// of 8; reduce-then-scan).
+// (the fewest passes of digits of at most 8 bits, their widths balanced:
+// radix_digit_bits; reduce-then-scan).
 //
 // Radix pass over tiles of 4096 keys.  Large sorts split the tiles into one
 // contiguous chunk per persistent block:
@@ -584,11 +584,11 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   bool first = true;
   // large sorts: one contiguous chunk of tiles per persistent block (two per SM)
   const int64_t chunks = sort_chunks(ntiles);
-  // given first-pass counts are of the full low byte
-  if (first_counts_given && (!chunks || end_bit < 8)) return cudaErrorInvalidValue;
-  for (int shift = 0; shift < end_bit; shift += 8) {
+  if (first_counts_given && !chunks) return cudaErrorInvalidValue;
+  int pass = 0;
+  for (int shift = 0; shift < end_bit; shift += radix_digit_bits(end_bit, pass++)) {
     // a pass sorts on bits [shift, shift + dbits); higher key bits are ignored
-    const int dbits = std::min(8, end_bit - shift);
+    const int dbits = radix_digit_bits(end_bit, pass);
     const uint32_t dmask = (1u << dbits) - 1u;
     if (chunks) {
       if (!(first && first_counts_given))
