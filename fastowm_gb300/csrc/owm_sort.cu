@@ -574,7 +574,6 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   if (temp_bytes < radix_sort_temp_bytes(n) || end_bit <= 0 || end_bit > 32) return cudaErrorInvalidValue;
   const bool has_vals = v0 != nullptr;
   int64_t ntiles = (n + kTile - 1) / kTile;
-  int64_t hn = ntiles * kRadix;  // per-tile table of small sorts
   uint32_t* hist = static_cast<uint32_t*>(temp);
   size_t hbytes = ((size_t)hist_entries(ntiles) * sizeof(uint32_t) + 255) & ~(size_t)255;
   void* stemp = static_cast<char*>(temp) + hbytes;
@@ -594,7 +593,9 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
       if (!(first && first_counts_given))
         OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep_chunk<<<(unsigned)(chunks * kSubChunks), kBlock, 0, s>>>(
             ka, n, shift, dmask, hist, ntiles));
-      cudaError_t e = exclusive_scan_u32(hist, hist, chunks * kSubChunks * kRadix, nullptr, stemp, sbytes, s, launches);
+      // digit-major table: the live digits' counts come first, and only they
+      // need offsets (no key has a digit >= 2^dbits)
+      cudaError_t e = exclusive_scan_u32(hist, hist, (chunks * kSubChunks) << dbits, nullptr, stemp, sbytes, s, launches);
       if (e != cudaSuccess) return e;
       cudaError_t e2;
       if (has_vals)
@@ -605,7 +606,7 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
       if (e2 != cudaSuccess) return e2;
     } else {  // small sorts: one block per tile, per-tile counts
       OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, dmask, hist, ntiles));
-      cudaError_t e = exclusive_scan_u32(hist, hist, hn, nullptr, stemp, sbytes, s, launches);
+      cudaError_t e = exclusive_scan_u32(hist, hist, ntiles << dbits, nullptr, stemp, sbytes, s, launches);
       if (e != cudaSuccess) return e;
       if (has_vals && first && iota_vals)
         OWM_LAUNCH("k_rs_downsweep", s, k_rs_downsweep<true, true><<<(unsigned)ntiles, kBlock, 0, s>>>(ka, va, kb, vb, n, shift, dmask, hist, ntiles));
