@@ -169,3 +169,17 @@ def test_large_cloud_policies(owm, oracle, ctx, policy, mn, mr):
     xyz, bb, W, Ov, B, _ = _cloud(owm, 1, n=1_500_000, w=240, h=310)
     got, want, _ = _run_both(owm, oracle, ctx, xyz, bb, W, Ov, B, mn, policy, mr)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("n,mn,bits", [(200_000, 32, 16), (1_500_000, 32, 18), (1_500_000, 128, 16),
+                                       (5_000_000, 256, 16), (5_000_000, 4, 22)])
+def test_key_width_rule(owm, ctx, n, mn, bits):
+    """Morton key width: the fewest bits per axis (8..12) with at most half a
+    leaf of points per finest cell; the tree stays well-formed at every width."""
+    xyz, bb, _, _, _, _ = _cloud(owm, 1, n=n, w=300, h=300)
+    cloud = ctx.cloud(xyz, bb)
+    tree = ctx.tree(cloud, max_number=mn)
+    info = tree.info()
+    assert info.key_bits == bits
+    assert info.root_count == n and tree.check()
+    cloud.close()
