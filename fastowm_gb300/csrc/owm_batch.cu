@@ -328,6 +328,15 @@ __global__ void k_b_karras(const uint32_t* __restrict__ lk, const TileMeta* __re
   last_of[m.int_off + i] = hi;
 }
 
+// Arrival at a node of the bottom-up refit: the first arriver's summary
+// stores are released by its increment and acquired by the second arriver's,
+// which then reads both children from L2.
+__device__ __forceinline__ int32_t arrive_acq_rel(int32_t* f) {
+  int32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(f) : "memory");
+  return old;
+}
+
 // Bottom-up refit of every tile's hierarchy; every node also gets its escape
 // link (the right child of the split after its last leaf, or end) from the
 // thread that starts at a leaf or arrives second at an internal node.
@@ -346,9 +355,8 @@ __global__ void k_b_refit(Node* __restrict__ nodes, const int32_t* __restrict__ 
   if (nl <= 1) return;  // a one-leaf tile: the leaf is the root
   int32_t n = parent[m.node_off + nl - 1 + li];
   for (int32_t guard = 0; n >= 0 && guard < m.nleaves; ++guard) {
-    __threadfence();
-    if (atomicAdd(&flags[m.int_off + n], 1) == 0) return;
-    __threadfence();
+    // acquire-release arrival (see arrive_acq_rel)
+    if (arrive_acq_rel(flags + m.int_off + n) == 0) return;
     const Node* a = base + __ldcg(&base[n].left);
     const Node* b = base + __ldcg(&base[n].right);
     float4 ba = __ldcg(reinterpret_cast<const float4*>(a)), bb = __ldcg(reinterpret_cast<const float4*>(b));

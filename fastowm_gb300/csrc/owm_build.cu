@@ -319,6 +319,12 @@ __device__ __forceinline__ void load_summary(const Node* p, float4& box, int64_t
 
 // Bottom-up refit; every node also gets its escape link here (the thread
 // that starts at a leaf, and the second arrival at an internal node).
+__device__ __forceinline__ int32_t arrive_acq_rel(int32_t* f) {
+  int32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(f) : "memory");
+  return old;
+}
+
 __global__ void k_refit(Node* __restrict__ nodes, const int32_t* __restrict__ parent, int32_t* __restrict__ flags,
                         const int32_t* __restrict__ right_of, const int32_t* __restrict__ last_of, int32_t nl) {
   int32_t li = blockIdx.x * blockDim.x + threadIdx.x;
@@ -327,9 +333,10 @@ __global__ void k_refit(Node* __restrict__ nodes, const int32_t* __restrict__ pa
   int32_t n = parent[nl - 1 + li];
   // a root path has at most nl-1 internal nodes; the bound guards corruption
   for (int32_t guard = 0; n >= 0 && guard < nl; ++guard) {
-    __threadfence();
-    if (atomicAdd(&flags[n], 1) == 0) return;  // sibling not done yet
-    __threadfence();
+    // acquire-release arrival: the first arriver's summary stores are
+    // released by its increment and acquired by the second arriver's, which
+    // then reads both children from L2
+    if (arrive_acq_rel(flags + n) == 0) return;  // sibling not done yet
     const Node* a = nodes + __ldcg(&nodes[n].left);
     const Node* b = nodes + __ldcg(&nodes[n].right);
     float4 ba, bb;
