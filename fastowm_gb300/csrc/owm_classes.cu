@@ -79,6 +79,17 @@ __global__ void k_cls_windows(ClassArgs A, uint32_t thr, uint32_t* __restrict__ 
     out[cls_window_slot(A, w)] = cls_window_one(A, w, thr);
 }
 
+// The same, and each result also marks stage 2's occupancy bitmaps.
+__global__ void k_cls_windows_marked(ClassArgs A, uint32_t thr, uint32_t* __restrict__ out, uint32_t* __restrict__ once,
+                                     uint32_t* __restrict__ twice, uint32_t max_id) {
+  const int64_t total = (int64_t)A.nx * A.ny;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = cls_window_one(A, w, thr);
+    out[cls_window_slot(A, w)] = v;
+    s2_mark_id(once, twice, max_id, v);
+  }
+}
+
 int grid(int64_t n, int block = 256) {
   int64_t g = (n + block - 1) / block;
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
@@ -186,6 +197,16 @@ int classes_finish(const ClassArgs& A, const TreeView& t, int64_t n, const owm_p
   (void)n;
   OWM_LAUNCH("k_cls_rows", s, k_cls_rows<<<grid((int64_t)A.nx * A.ty), 256, 0, s>>>(A));
   OWM_LAUNCH("k_cls_windows", s, k_cls_windows<<<grid((int64_t)A.nx * A.ny), 256, 0, s>>>(A, p.min_num_points, d_win));
+  count_launch(launches, 2);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int classes_finish_marked(const ClassArgs& A, const owm_params& p, uint32_t* d_win, uint32_t* once, uint32_t* twice,
+                          uint32_t max_id, cudaStream_t s, int64_t* launches) {
+  OWM_LAUNCH("k_cls_rows", s, k_cls_rows<<<grid((int64_t)A.nx * A.ty), 256, 0, s>>>(A));
+  OWM_LAUNCH("k_cls_windows", s, k_cls_windows_marked<<<grid((int64_t)A.nx * A.ny), 256, 0, s>>>(
+      A, p.min_num_points, d_win, once, twice, max_id));
   count_launch(launches, 2);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;

@@ -226,6 +226,10 @@ int classes_aggregate(const ClassArgs& A, const TreeView& t, int64_t n, cudaStre
 // Tie ids, row and window reductions: stage-1 results into d_win.
 int classes_finish(const ClassArgs& A, const TreeView& t, int64_t n, const owm_params& p, uint32_t* d_win,
                    cudaStream_t s, int64_t* launches);
+// The same, marking stage 2's occupancy bitmaps (zeroed) as each window
+// result is produced (s2_mark_id); stage 2 then only emits the LLPs.
+int classes_finish_marked(const ClassArgs& A, const owm_params& p, uint32_t* d_win, uint32_t* once, uint32_t* twice,
+                          uint32_t max_id, cudaStream_t s, int64_t* launches);
 // prepare + aggregate + finish.
 int run_stage1_classes(const TreeView& t, int64_t n, const owm_params& p, const Edge* ex, const Edge* ey,
                        uint32_t* d_win, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);

@@ -194,9 +194,17 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     cudaStream_t ss = c->side_stream;
     c->stage12_side = true;
     OWM_CUDA_TRY(cudaStreamWaitEvent(ss, c->ev[6], 0));
-    rc = classes_finish(cls, c->tree.view(), n, p, win, ss, &c->launches);
+    if (bitmap2) {  // the window kernel marks stage 2's bitmaps (zeroed early, above)
+      uint32_t *once = nullptr, *twice = nullptr;
+      stage2_bitmap_ptrs(s2scratch, n, &once, &twice);
+      rc = classes_finish_marked(cls, p, win, once, twice, (uint32_t)n, ss, &c->launches);
+    } else {
+      rc = classes_finish(cls, c->tree.view(), n, p, win, ss, &c->launches);
+    }
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[2], ss));
-    if (!rc) rc = stage2(ss);
+    if (!rc)
+      rc = bitmap2 ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, ss, &c->launches, true, true)
+                   : stage2(ss);
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[3], ss));
     if (!rc) rc = run_stage3_mark(d_xyz, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));

@@ -326,11 +326,7 @@ __global__ void k_s2_flags(const uint32_t* __restrict__ keys, int64_t n, uint32_
 __global__ void k_s2_mark(const uint32_t* __restrict__ win, int64_t n, uint32_t max_id,
                           uint32_t* __restrict__ once, uint32_t* __restrict__ twice) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t v = win[i];
-    if (v > max_id) continue;  // kNone (and nothing else: ids are <= max_id)
-    const uint32_t bit = 1u << (v & 31u);
-    const uint32_t old = atomicOr(once + (v >> 5), bit);
-    if (old & bit) atomicOr(twice + (v >> 5), bit);
+    s2_mark_id(once, twice, max_id, win[i]);  // kNone (and nothing else: ids are <= max_id) is skipped
   }
 }
 
@@ -631,9 +627,15 @@ int stage2_bitmap_clear(void* scratch, size_t scratch_bytes, int64_t npoints, cu
   return OWM_OK;
 }
 
+void stage2_bitmap_ptrs(void* scratch, int64_t npoints, uint32_t** once, uint32_t** twice) {
+  const S2Bitmaps B = stage2_bitmap_layout(scratch, npoints);
+  *once = B.once;
+  *twice = B.twice;
+}
+
 int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
                       uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches,
-                      bool cleared) {
+                      bool cleared, bool marked) {
   if (n <= 0) {
     OWM_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
     return OWM_OK;
@@ -641,10 +643,13 @@ int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double 
   if (npoints < 0 || npoints >= (int64_t)kNone || !(overlap > 0.0)) return OWM_EINVAL;
   if (scratch_bytes < stage2_bitmap_scratch_bytes(npoints)) return OWM_ENOMEM;
   const S2Bitmaps B = stage2_bitmap_layout(scratch, npoints);
-  if (!cleared) OWM_CUDA_TRY(cudaMemsetAsync(B.once, 0, 2 * align256((size_t)B.nw * 4), s));
-  OWM_LAUNCH("k_s2_mark", s, k_s2_mark<<<grid1d(n), 256, 0, s>>>(d_win, n, (uint32_t)npoints, B.once, B.twice));
+  if (!marked) {
+    if (!cleared) OWM_CUDA_TRY(cudaMemsetAsync(B.once, 0, 2 * align256((size_t)B.nw * 4), s));
+    OWM_LAUNCH("k_s2_mark", s, k_s2_mark<<<grid1d(n), 256, 0, s>>>(d_win, n, (uint32_t)npoints, B.once, B.twice));
+    count_launch(launches);
+  }
   OWM_LAUNCH("k_s2_count", s, k_s2_count<<<(unsigned)B.nblocks, kS2Block, 0, s>>>(B.twice, B.part));
-  count_launch(launches, 2);
+  count_launch(launches);
   OWM_CUDA_TRY(exclusive_scan_u32(B.part, B.part, B.nblocks, d_count, B.ct, B.cb, s, launches));
   OWM_LAUNCH("k_s2_emit", s, k_s2_emit_chunk<<<(unsigned)B.nblocks, kS2Block, 0, s>>>(B.twice, B.part, d_llp));
   count_launch(launches);

@@ -56,9 +56,21 @@ int run_stage2(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap
 // stage2_bitmap_clear (which may run early, on another stream).
 size_t stage2_bitmap_scratch_bytes(int64_t npoints);
 int stage2_bitmap_clear(void* scratch, size_t scratch_bytes, int64_t npoints, cudaStream_t s);
+// With marked, the bitmaps were also marked already (by the stage-1 window
+// kernel, s2_mark_id) and only the ascending emit remains.
 int run_stage2_bitmap(const uint32_t* d_win, int64_t n, int64_t npoints, double overlap, uint32_t* d_llp,
                       uint32_t* d_count, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches,
-                      bool cleared = false);
+                      bool cleared = false, bool marked = false);
+void stage2_bitmap_ptrs(void* scratch, int64_t npoints, uint32_t** once, uint32_t** twice);
+
+// Stage 2's occupancy marks of one window result v (ids 0..max_id; kNone is
+// skipped): the first occurrence sets `once`, a later one `twice`.
+__device__ __forceinline__ void s2_mark_id(uint32_t* __restrict__ once, uint32_t* __restrict__ twice, uint32_t max_id,
+                                           uint32_t v) {
+  if (v > max_id) return;
+  const uint32_t bit = 1u << (v & 31u);
+  if (atomicOr(once + (v >> 5), bit) & bit) atomicOr(twice + (v >> 5), bit);
+}
 // Same with explicit working arrays (n uint32 each; d_llp must not alias
 // them) and a temp block of radix_sort_temp_bytes(n) (256-aligned) +
 // scan_temp_bytes(n).  d_win may equal k0.
