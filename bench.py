@@ -11,9 +11,10 @@ points and device->host copy of the seeds inside the timed region).
 
 Multi-GPU (torchrun): every rank runs an independent replica of the
 workload (the path has no exchange step); value = all ranks' points / max
-rank time.  --impl reference times the reference's own CPU path (compiled
-from its sources when present, else the C port of the same quadtree
-algorithm, oracle/owm_refport.c) on rank 0.
+rank time.  --impl reference times the reference's own CPU path (its
+CPP-TBB-CPU/src/optim3_func.cpp compiled from its sources, else the C port
+of the same quadtree algorithm, oracle/owm_refport.c) on rank 0 with every
+host core, on the same cloud as our arm, and loads no GPU code.
 """
 from __future__ import annotations
 
@@ -141,10 +142,16 @@ def job_value(ws: int, points_per_rank: int, steps: int, ms_max: float) -> float
     return ws * points_per_rank * steps / (ms_max / 1e3) / 1e6
 
 
-def workload(config: int, n_override: int | None):
-    import fastowm_gb300 as F
+def workload(config: int, n_override: int | None, synth_config=None):
+    """(spec, wsize, overlap, bsize, max_number, seed) of a workload config;
+    n_override keeps the density and terrain on a smaller square.
+    synth_config defaults to the GPU library's; the reference arm passes the
+    oracle's (the same generator source) so it never loads the GPU library."""
+    if synth_config is None:
+        import fastowm_gb300 as F
 
-    spec, W, Ov, B, mn, seed = F.synth_config(config)
+        synth_config = F.synth_config
+    spec, W, Ov, B, mn, seed = synth_config(config)
     if n_override:
         # same density and terrain, smaller square area
         dens = spec.n / ((spec.x1 - spec.x0) * (spec.y1 - spec.y0))
@@ -153,6 +160,15 @@ def workload(config: int, n_override: int | None):
         spec.x1 = spec.x0 + side
         spec.y1 = spec.y0 + side
     return spec, W, Ov, B, mn, seed
+
+
+def workload_config(config: int, spec, W: int, Ov: float, B: int, ncells: int, ngrid: int) -> dict:
+    """The `config` object of both arms' lines: the workload only (every arm
+    picks its own leaf size, reported beside it)."""
+    return {"workload": f"config {config}: {spec.n} FP64 points {spec.x1 - spec.x0:.0f} x {spec.y1 - spec.y0:.0f} m, "
+                        f"Wsize {W}, overlap {Ov}, Bsize {B}, build + stages 1-3",
+            "points": int(spec.n), "wsize": int(W), "overlap": float(Ov), "bsize": int(B), "windows": int(ncells),
+            "cells": int(ngrid)}
 
 
 def kernel_bytes(name: str, n: int, p, nleaves: int) -> float | None:
@@ -189,52 +205,87 @@ def measured_traffic(name: str, n: int) -> float | None:
     return None
 
 
-def cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads: int):
-    """The reference's CPU path on the given sample: (Mpts/s, kind, seconds)."""
+def cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads: int, memo_a: bool = False):
+    """The reference's CPU path on the given cloud, timed as its driver times
+    it (tree build + stages 1-3, cloud already in memory): (Mpts/s, kind,
+    seconds, seed count)."""
     from oracle import oracle as O
 
     n = xyz.shape[0]
     if O.ref_available():
-        _, _, _, res = O.ref_run(xyz, bb, W, Ov, B, policy=1, max_number=mn, level=5, nthreads=threads,
-                                 want_win=False)
+        seeds, _, _, res = O.ref_run(xyz, bb, W, Ov, B, policy=1, max_number=mn, level=5, nthreads=threads,
+                                     memo_a=memo_a, want_win=False)
         t = res.t_tree + res.t_owm
-        return n / t / 1e6, "reference", t
+        return n / t / 1e6, "reference", t, len(seeds)
     # C port of the same quadtree algorithm (oracle/owm_refport.c), timed the
-    # same way: tree build + stages 1-3, cloud already in memory
+    # same way; it has the exact stage 1 only
     O.build(ref=False)
-    _, _, tt, to = O.port_run(xyz, bb, W, Ov, B, max_number=mn, level=5, nthreads=threads)
+    seeds, _, tt, to = O.port_run(xyz, bb, W, Ov, B, max_number=mn, level=5, nthreads=threads)
     t = tt + to
-    return n / t / 1e6, "port", t
+    return n / t / 1e6, "port", t, len(seeds)
+
+
+def repo_libraries() -> list[str]:
+    """This repository's shared libraries mapped into this process."""
+    libs = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for ln in f:
+                path = ln.split()[-1] if ln.split() else ""
+                if path.endswith(".so") and path.startswith(str(ROOT)):
+                    libs.add(os.path.relpath(path, ROOT))
+    except OSError:
+        return []
+    return sorted(libs)
 
 
 def run_reference(args, ws, rank):
+    """The reference arm: the reference's own CPU path (CPP-TBB-CPU/src/
+    optim3_func.cpp compiled from its sources, exact stage 1 as o3memoB) on
+    the same cloud and knobs as our arm, with every host core; each step
+    builds the tree and runs stages 1-3 once (owm_optim3.cpp:77-89,143-230).
+    The cloud comes from the oracle's copy of the generator, so this process
+    loads no GPU code at all."""
     if rank != 0:
         return
-    import fastowm_gb300 as F
+    from oracle import oracle as O
 
-    n_sample = args.cpu_sample
-    spec, W, Ov, B, mn, seed = workload(args.config, n_sample)
-    xyz, bb = F.synth_cloud(spec, seed)
+    spec, W, Ov, B, mn, seed = workload(args.config, args.n, O.synth_config)
+    t0 = time.perf_counter()
+    xyz, bb = O.synth_cloud(spec, seed)
+    gen_s = time.perf_counter() - t0
+    p = O.params(bb, spec.n, W, Ov, B)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads)
-    vals, secs, kind = [], [], "port"
+    secs, kind, nseeds = [], "port", 0
     for _ in range(args.steps):
-        v, kind, t = cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads)
-        vals.append(v)
+        _, kind, t, nseeds = cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads)
         secs.append(t)
     tot = sum(secs)
     value = spec.n * len(secs) / tot / 1e6
-    sample = (f"{spec.n} pts of the {args.config == 2 and '2 km x 2 km' or 'config'} workload generator at the same "
-              f"density ({spec.x1 - spec.x0:.0f} m square), W={W} O={Ov} B={B}")
+    memo = None
+    if kind == "reference":
+        # the reference's default build (o3memo: stage1memoA, approximate
+        # window counts), one run, reported beside the exact path
+        mv, _, mt, mseeds = cpu_baseline_run(xyz, bb, W, Ov, B, mn, threads, memo_a=True)
+        memo = {"value": round(mv, 3), "unit": UNIT, "seconds": round(mt, 3), "seeds": int(mseeds),
+                "what": "stage1memoA (o3memo, the reference's default; approximate, not parity-bearing), one run"}
+    sample = (f"the whole workload: {spec.n} points, W={W} O={Ov} B={B}, maxNumber {mn}, level 5; each step "
+              f"builds the quadtree and runs stages 1-3 once")
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * tot / len(secs), 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"config {args.config} sample", "points": spec.n, "wsize": W, "overlap": Ov,
-                       "bsize": B, "leaf_max_number": mn},
+            "config": workload_config(args.config, spec, W, Ov, B, p.ncells, p.ngrid),
+            "leaf_max_number": mn, "seeds": int(nseeds),
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": kind,
                              "sample": sample},
-            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "step_seconds": [round(t, 3) for t in secs], "memo_a": memo, "cloud_generation_s": round(gen_s, 2),
+            "code": "oracle/_ref/libowmref.so: CPP-TBB-CPU/src/optim3_func.cpp unmodified, TBB/oneDPL scheduling "
+                    "names on std::thread (oracle/shim)" if kind == "reference" else
+                    "oracle/librefport.so: C port of the reference's quadtree algorithm",
+            "libraries_loaded": repo_libraries()}
     print(json.dumps(line), flush=True)
 
 
@@ -245,7 +296,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", type=int, default=2)
-    ap.add_argument("--n", type=int, default=None, help="override point count (same density)")
+    ap.add_argument("--points", "--n", dest="n", type=int, default=None, help="override point count (same density)")
     ap.add_argument("--cpu-sample", type=int, default=16_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -410,10 +461,11 @@ def main():
         sspec, sW, sO, sB, smn, sseed = workload(args.config, args.cpu_sample)
         sxyz, sbb = F.synth_cloud(sspec, sseed)
         threads = os.cpu_count() or 1
-        v, kind, t = cpu_baseline_run(sxyz, sbb, sW, sO, sB, smn, threads)
+        v, kind, t, _ = cpu_baseline_run(sxyz, sbb, sW, sO, sB, smn, threads)
         cpu = {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{sspec.n} pts, same generator and density ({sspec.x1 - sspec.x0:.0f} m square), "
-                         f"W={sW} O={sO} B={sB}, build+OWM once ({t:.2f} s)"}
+                         f"W={sW} O={sO} B={sB}, build+OWM once ({t:.2f} s); the reference arm "
+                         f"(--impl reference) times the whole workload"}
     pb = path_bytes(spec.n, p)
     path_gbs = pb / (ms_max / args.steps / 1e3) / 1e9
     path_roof = {"model": "compulsory bytes of the whole step: 154 B/pt + 40 B/window + 8 B/cell",
@@ -424,14 +476,11 @@ def main():
         line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"config {args.config}: {spec.n} FP64 points "
-                                       f"{spec.x1 - spec.x0:.0f} x {spec.y1 - spec.y0:.0f} m, plain GPU path "
-                                       f"(one cloud per launch sequence)",
-                           "wsize": W, "overlap": Ov, "bsize": B, "leaf_max_number": mn,
-                           "leaf_tuning_ms": leaf_tuning["ms"] if leaf_tuning else None,
-                           "windows": int(p.ncells), "cells": int(p.ngrid), "seeds": int(len(seeds)),
-                           "l2": "inputs (2.4 GB at 100M points) larger than L2; no flush",
-                           "parallelism": f"replicas x{ws}"},
+                "config": workload_config(args.config, spec, W, Ov, B, p.ncells, p.ngrid),
+                "path": "plain GPU path, one cloud per owm_run (device-resident input)",
+                "leaf_max_number": mn, "leaf_tuning_ms": leaf_tuning["ms"] if leaf_tuning else None,
+                "seeds": int(len(seeds)), "l2": "inputs (2.4 GB at 100M points) larger than L2; no flush",
+                "parallelism": f"replicas x{ws}",
                 "phases_ms": {"tree": round(phase[0] / args.steps, 4), "stage1": round(phase[1] / args.steps, 4),
                               "stage2": round(phase[2] / args.steps, 4), "stage3": round(phase[3] / args.steps, 4)},
                 "kernel_timing": "second pass over the same K steps with CUDA events around every launch "
@@ -441,13 +490,32 @@ def main():
                 "kernels": {k: {"ms": round(v[0] / args.steps, 4), "share": round(v[0] / tot_k, 4),
                                 "launches_per_step": v[1] / args.steps} for k, v in
                             sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
-                "roofline": roof, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "batched": batched, "served": served, "ingest": ingest,
+                "roofline": roof, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": int(launches)}
+        line["summary"] = summary(line)
         print(json.dumps(line), flush=True)
     cloud.close()
     ctx.close()
     barrier(ws)
+
+
+def summary(line: dict) -> dict:
+    """The line's headline figures, repeated compactly as its last key so that
+    a reader of only the line's tail has them all."""
+    b, sv, e, pr, rf = (line.get(k) or {} for k in ("batched", "served", "e2e", "path_roofline", "roofline"))
+    out = {"value": line["value"], "ms_per_step": line["ms_per_step"], "e2e": e.get("value"),
+           "path_roofline_frac": pr.get("frac"), "dominant_kernel": rf.get("kernel"), "kernel_frac": rf.get("frac"),
+           "cpu_baseline": (line.get("cpu_baseline") or {}).get("value")}
+    if b:
+        out["batched"] = {k: b.get(k) for k in ("batched_mpts", "per_tile_mpts", "speedup", "per_tile_p50_ms",
+                                                "per_tile_p99_ms", "seeds_equal")}
+    if sv:
+        out["served"] = {"saturation_mpts": sv.get("saturation_mpts"), "plain_per_tile_mpts": sv.get("plain_per_tile_mpts"),
+                         "saturation_vs_plain": sv.get("saturation_vs_plain"),
+                         "p50_p99_ms_by_lambda": {str(r["lambda_tiles_s"]): [r["p50_ms"], r["p99_ms"]]
+                                                  for r in sv.get("sweep", [])}}
+    return out
 
 
 def _device_tiles(F, torch, config, ntiles, local, first=0):

@@ -1,8 +1,8 @@
 """Build recipe of the native library ``fastowm_gb300/libowm_gb300.so``.
 
 Compiles every ``csrc/*.cu`` for sm_103a only (``-gencode
-arch=compute_103a,code=sm_103a``) and every ``csrc/*.cpp`` with g++, in
-parallel, into ``fastowm_gb300/_build/`` and links one shared library in the
+arch=compute_103a,code=sm_103a``), every ``csrc/*.cpp`` with g++ and every
+``csrc/*.c`` with gcc, in parallel, into ``fastowm_gb300/_build/`` and links one shared library in the
 package directory.  Host code is compiled with ``-ffp-contract=off`` so the
 parameter arithmetic and the synthetic generator give the same bits on
 x86-64 and aarch64.  Rebuilds only what changed (sources or headers newer
@@ -69,6 +69,12 @@ def build(verbose: bool = False, jobs: int | None = None, force: bool = False) -
             cmds.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread",
                          "-I", str(INCLUDE), "-I", str(Path(nvcc).resolve().parent.parent / "include"),
                          "-c", str(src), "-o", str(obj)])
+    for src in sorted(CSRC.glob("*.c")):
+        obj = OUT / (src.stem + ".c.o")
+        objs.append(obj)
+        if force or _stale(obj, src, deps):
+            cmds.append(["gcc", "-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-pthread", "-D_GNU_SOURCE",
+                         "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)])
     workers = jobs or min(8, os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
         for cmd, rc, out in ex.map(_compile, cmds):
@@ -77,7 +83,7 @@ def build(verbose: bool = False, jobs: int | None = None, force: bool = False) -
             if rc:
                 raise RuntimeError(f"compile failed: {cmd[-3]}")
     if force or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
-        cmd = [nvcc, "-shared", *ARCH, "-o", str(LIB), *map(str, objs), "-lpthread"]
+        cmd = [nvcc, "-shared", *ARCH, "-o", str(LIB), *map(str, objs), "-lpthread", "-lm"]
         _, rc, out = _compile(cmd)
         if verbose or rc:
             sys.stderr.write(" ".join(cmd) + "\n" + out)

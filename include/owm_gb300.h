@@ -89,8 +89,10 @@ int owm_xyz_write_ids(const char* path, const double* xyz, int64_t n, const int6
 void owm_host_free(void* p);
 
 /* Tolerant correctness score of check_results (optim3_func.cpp:725-794):
- * percentage of `gold` points matched by an output point within a
- * displace/2 box and |dz| < 0.01.  Host-only helper for real-cloud runs. */
+ * the number of output points (ids into xyz) that find a gold point strictly
+ * inside their displace/2 box with |dz| < 0.01, as a percentage of n_gold.
+ * Id 0 is the reference's sentinel point {0, 0, DBL_MAX}, as in the
+ * reference; ids above n are skipped.  Host-only helper for real-cloud runs. */
 double owm_check_results(const double* gold_xyz, int64_t n_gold, const double* xyz, int64_t n,
                          const int64_t* ids, int64_t n_ids, float displace);
 

@@ -1,11 +1,14 @@
 """ORACLE / TEST INFRASTRUCTURE -- Python binding of the CPU oracles.
 
-* ``liboracle.so``      my C restatement of the OWM path (owm_oracle.c)
+* ``liboracle.so``      my C restatement of the OWM path (owm_oracle.c) and
+                        the project's seeded cloud generator (oracle_synth_*)
 * ``_ref/libowmref.so`` the reference's own CPP-TBB-CPU/src/optim3_func.cpp
-                        compiled in place (ref_runner.cpp + shim/)
+                        compiled unmodified (ref_runner.cpp + shim/), from the
+                        checkout named by $OWM_REFERENCE or from the copies
+                        staged under _ref/src by ``make -C oracle REF=...``
 * ``librefport.so``     C port of that reference algorithm (owm_refport.c):
-                        the timed CPU baseline where the reference sources
-                        are not there to compile
+                        the timed CPU baseline where the reference cannot be
+                        compiled
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 this module, as the checker; the product never imports it.
@@ -23,7 +26,9 @@ HERE = Path(__file__).resolve().parent
 LIB_ORACLE = HERE / "liboracle.so"
 LIB_REF = HERE / "_ref" / "libowmref.so"
 LIB_PORT = HERE / "librefport.so"
-REF_SRC = Path(os.environ.get("OWM_REFERENCE", "/root/reference"))
+# the reference checkout, when one is at hand (no default location)
+REF_SRC = Path(os.environ["OWM_REFERENCE"]) if os.environ.get("OWM_REFERENCE") else None
+STAGED_SRC = HERE / "_ref" / "src" / "CPP-TBB-CPU"
 
 
 class OracleParams(C.Structure):
@@ -33,6 +38,15 @@ class OracleParams(C.Structure):
                 ("min_num_points", C.c_uint32), ("ncols", C.c_uint32), ("nrows", C.c_uint32),
                 ("ncols_grid", C.c_uint32), ("nrows_grid", C.c_uint32), ("ncells", C.c_int64),
                 ("ngrid", C.c_int64)]
+
+
+class SynthSpec(C.Structure):
+    """owm_synth_spec of include/owm_gb300.h."""
+    _fields_ = [("n", C.c_int64), ("x0", C.c_double), ("y0", C.c_double), ("x1", C.c_double), ("y1", C.c_double),
+                ("amplitude", C.c_double), ("wavelength", C.c_double), ("noise_sigma", C.c_double),
+                ("lifted_frac", C.c_double), ("lift_lo", C.c_double), ("lift_hi", C.c_double),
+                ("z_quantum", C.c_double), ("tie_free", C.c_int32), ("strips", C.c_int32), ("holes", C.c_int32),
+                ("_pad", C.c_int32)]
 
 
 class RefResult(C.Structure):
@@ -48,7 +62,10 @@ def build(ref: bool | None = None) -> None:
     target = "all"
     if ref is False:
         target = "restatement"
-    subprocess.run(["make", "-s", "-C", str(HERE), target, f"REF={REF_SRC}"], check=True)
+    cmd = ["make", "-s", "-C", str(HERE), target]
+    if REF_SRC is not None:
+        cmd.append(f"REF={REF_SRC}")
+    subprocess.run(cmd, check=True)
 
 
 _o = None
@@ -78,6 +95,9 @@ def _oracle():
         _o.oracle_xyz_parse.argtypes = [C.c_char_p, C.c_int64, P(C.c_double), C.c_int64, P(C.c_int64),
                                         P(C.c_double), P(C.c_int)]
         _o.oracle_cell_box.argtypes = [P(OracleParams), C.c_int64, C.c_int64, P(C.c_double)]
+        _o.oracle_synth_config.argtypes = [C.c_int, C.c_int64, P(SynthSpec), P(C.c_uint32), P(C.c_double),
+                                           P(C.c_uint32), P(C.c_int32), P(C.c_uint64)]
+        _o.oracle_synth_cloud.argtypes = [P(SynthSpec), C.c_uint64, P(C.c_double), P(C.c_double), C.c_int]
     return _o
 
 
@@ -98,7 +118,9 @@ def _port():
 def ref_available() -> bool:
     if LIB_REF.exists():
         return True
-    if (REF_SRC / "CPP-TBB-CPU" / "src" / "optim3_func.cpp").exists():
+    have_src = (STAGED_SRC / "src" / "optim3_func.cpp").exists() or (
+        REF_SRC is not None and (REF_SRC / "CPP-TBB-CPU" / "src" / "optim3_func.cpp").exists())
+    if have_src:
         try:
             build(ref=True)
         except subprocess.CalledProcessError:
@@ -119,6 +141,8 @@ def _ref():
         _r.owmref_run.argtypes = [P(C.c_double), C.c_int64, P(C.c_double), C.c_uint32, C.c_uint32, C.c_double,
                                   C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int),
                                   C.c_int64, P(C.c_int), C.c_int64, P(RefResult)]
+        _r.owmref_check_results.argtypes = [C.c_char_p, P(C.c_double), C.c_int64, P(C.c_int), C.c_int64, C.c_float]
+        _r.owmref_check_results.restype = C.c_double
     return _r
 
 
@@ -128,6 +152,28 @@ def _d(a):
 
 def _q(a):
     return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def synth_config(config: int, tile: int = 0):
+    """The project's workload config (the same source as the GPU library's
+    owm_synth_config): (spec, wsize, overlap, bsize, max_number, seed)."""
+    spec = SynthSpec()
+    w, b, m = C.c_uint32(), C.c_uint32(), C.c_int32()
+    o, seed = C.c_double(), C.c_uint64()
+    if _oracle().oracle_synth_config(config, tile, C.byref(spec), C.byref(w), C.byref(o), C.byref(b), C.byref(m),
+                                     C.byref(seed)) != 0:
+        raise ValueError(f"no workload config {config}")
+    return spec, w.value, o.value, b.value, m.value, seed.value
+
+
+def synth_cloud(spec: SynthSpec, seed: int, nthreads: int = 0, out: np.ndarray | None = None):
+    """The seeded cloud, bit-identical to the GPU library's owm_synth_cloud:
+    (xyz (n, 3) float64, bbox array [min_x, min_y, max_x, max_y])."""
+    xyz = out if out is not None else np.empty((spec.n, 3), dtype=np.float64)
+    bb = np.zeros(4, dtype=np.float64)  # owm_bbox: min_x, min_y, max_x, max_y
+    if _oracle().oracle_synth_cloud(C.byref(spec), seed, _d(xyz), _d(bb), nthreads) != 0:
+        raise ValueError("bad synthetic cloud spec")
+    return xyz, bb
 
 
 def _bbox_arr(bbox) -> np.ndarray:
@@ -232,6 +278,14 @@ def xyz_parse(text: bytes):
     if rc != 0:
         return None
     return out[: n.value].copy(), tuple(bb.tolist()), bool(hh.value)
+
+
+def ref_check_results(gold_path: str, xyz, ids, displace: float) -> float:
+    """The reference's own check_results on a gold file (percentage)."""
+    a = np.ascontiguousarray(xyz, dtype=np.float64)
+    i = np.ascontiguousarray(ids, dtype=np.int32)
+    return _ref().owmref_check_results(str(gold_path).encode(), _d(a), a.shape[0],
+                                        i.ctypes.data_as(C.POINTER(C.c_int)), i.size, displace)
 
 
 def ref_read_xyz(path: str, cap: int):

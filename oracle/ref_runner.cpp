@@ -187,4 +187,20 @@ int owmref_read_xyz(const char* path, double* out, int64_t cap, int64_t* n, doub
   return rc;
 }
 
+// The reference's own GOLD score, check_results (optim3_func.cpp:725-794), on
+// a gold file of "x y z" lines and 1-based ids into the n AoS points xyz
+// (cloud[0] is the sentinel {0, 0, DBL_MAX}, as readXYZfile makes it).
+// Returns the reference's percentage (-1 when it cannot read the file).
+double owmref_check_results(const char* gold_path, const double* xyz, int64_t n, const int* ids, int64_t n_ids,
+                            float displace) {
+  if (n <= 0 || n >= 0xFFFFFFFFLL) return -2.0;
+  Lpoint* cloud = static_cast<Lpoint*>(mallocWrap((size_t)(n + 1) * sizeof(Lpoint)));
+  cloud[0] = {0.0, 0.0, std::numeric_limits<double>::max()};
+  std::memcpy(&cloud[1], xyz, (size_t)n * sizeof(Lpoint));
+  std::vector<int> v(ids, ids + n_ids);
+  const double r = check_results(std::string(gold_path), v, cloud, displace);
+  free(cloud);
+  return r;
+}
+
 }  // extern "C"

@@ -89,6 +89,23 @@ def test_synth_deterministic_and_thread_independent(owm):
     assert a[:, 0].min() == ba.min_x and a[:, 1].max() == ba.max_y
 
 
+def test_oracle_generator_equals_library_generator(owm, oracle):
+    """The CPU baseline makes its clouds with the oracle library's copy of the
+    generator (oracle_synth_*, the same source compiled separately), so that
+    it never loads the GPU library: both give the same bits."""
+    for c, t, n in ((1, 0, 120_000), (2, 0, 150_000), (3, 0, 90_000), (4, 11, None), (5, 40, None)):
+        s1, *k1 = owm.synth_config(c, t)
+        s2, *k2 = oracle.synth_config(c, t)
+        assert k1 == k2
+        if n:
+            s1.n = s2.n = n
+        assert s1.n == s2.n and (s1.x0, s1.x1, s1.y0, s1.y1) == (s2.x0, s2.x1, s2.y0, s2.y1)
+        a, ba = owm.synth_cloud(s1, k1[-1], nthreads=3)
+        b, bb = oracle.synth_cloud(s2, k2[-1], nthreads=5)
+        assert a.tobytes() == b.tobytes()
+        assert list(bb) == [ba.min_x, ba.min_y, ba.max_x, ba.max_y]
+
+
 def test_synth_configs(owm):
     for c in (1, 2, 3):
         spec, W, Ov, B, mn, seed = owm.synth_config(c)

@@ -109,3 +109,49 @@ def test_host_loader_verdicts_match_oracle(owm, tmp_path, text):
         pts, hb = owm.read_xyz(f)
         np.testing.assert_array_equal(pts, want[0])
         assert text in ACCEPTED
+
+
+def test_check_results_equals_reference(tmp_path, owm):
+    """owm_check_results against the reference's own check_results
+    (optim3_func.cpp:725-794, compiled into oracle/_ref) on seeded gold/output
+    pairs: gold files in the reference's dump format ("%.2f"), outputs that
+    drop seeds, add non-seed points, repeat ids and hold the sentinel id 0."""
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    spec, W, Ov, B, _, seed = O.synth_config(1)
+    spec.n = 60_000
+    spec.x1, spec.y1 = spec.x0 + 60.0, spec.y0 + 50.0
+    xyz, bb = O.synth_cloud(spec, seed)
+    seeds, _ = O.run(xyz, bb, W, Ov, B)
+    p = O.params(bb, spec.n, W, Ov, B)
+    rng = np.random.default_rng(3)
+    cases = [
+        (seeds, seeds),  # identical
+        (seeds, rng.choice(seeds, size=len(seeds) // 2, replace=False)),  # half the seeds
+        (seeds, np.concatenate([seeds, rng.integers(1, spec.n + 1, 40)])),  # plus random points
+        (seeds[: len(seeds) // 3], np.concatenate([[0], seeds, [0]])),  # sentinel ids, gold a third
+        (rng.integers(1, spec.n + 1, 200), np.concatenate([seeds[:50], seeds[:50]])),  # repeats
+    ]
+    for k, (gold_ids, out_ids) in enumerate(cases):
+        gold_file = tmp_path / f"gold{k}.xyz"
+        owm.write_xyz_ids(gold_file, xyz, gold_ids)
+        gold = np.loadtxt(gold_file, ndmin=2)
+        for displace in (float(p.displace), 1.0, 0.25):
+            want = O.ref_check_results(gold_file, xyz, out_ids, displace)
+            got = owm.check_results(gold, xyz, out_ids, displace)
+            assert got == want, (k, displace, got, want)
+
+
+def test_check_results_sentinel_matches_like_reference(tmp_path, owm):
+    """Id 0 is the reference's sentinel {0, 0, DBL_MAX}: it matches a gold
+    point only when the gold list holds that sentinel too."""
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    xyz = np.array([[10.0, 20.0, 1.0], [30.0, 40.0, 2.0]])
+    gold_file = tmp_path / "goldS.xyz"
+    gold_file.write_text("0 0 1.7976931348623157e308\n10 20 1\n")
+    gold = np.loadtxt(gold_file, ndmin=2)
+    for ids in ([0], [0, 1], [1, 2], [2]):
+        want = O.ref_check_results(gold_file, xyz, ids, 1.0)
+        assert owm.check_results(gold, xyz, ids, 1.0) == want, ids
+    assert owm.check_results(gold, xyz, [0, 1], 1.0) == 100.0

@@ -70,11 +70,13 @@ def test_job_value_single_rank_is_points_over_time():
 
 def test_reference_arm_under_torchrun_two_ranks():
     """bench.py --impl reference launched like the multi-GPU driver: rank 0
-    alone runs the CPU baseline and prints one JSON line; rank 1 exits 0."""
+    alone runs the CPU baseline and prints one JSON line; rank 1 exits 0.
+    The arm loads no GPU code: only the oracle's libraries are mapped, and its
+    config object is the one our arm prints for the same workload."""
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"), "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-sample", "30000"]
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--points", "30000"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -83,3 +85,12 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert line["impl"] == "reference" and line["n_gpus"] == 2
     assert line["cpu_baseline"]["kind"] in ("reference", "port")
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["value"] > 0
+    assert line["libraries_loaded"] and all(p.startswith("oracle/") for p in line["libraries_loaded"])
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from oracle import oracle as O
+
+    spec, W, Ov, B, _, _ = bench.workload(2, 30000, O.synth_config)
+    xyz, bb = O.synth_cloud(spec, O.synth_config(2)[5])
+    p = O.params(bb, spec.n, W, Ov, B)
+    assert line["config"] == bench.workload_config(2, spec, W, Ov, B, p.ncells, p.ngrid)
