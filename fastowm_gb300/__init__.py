@@ -230,6 +230,17 @@ class Context:
     def launches(self) -> int:
         return lib().owm_ctx_launches(self.handle)
 
+    def device_status(self) -> int:
+        """The device status word: bit 0 non-finite input, bit 1 a bounded
+        tree walk stopped (the call returned OWM_ETIMEOUT)."""
+        st = C.c_int32()
+        _check(lib().owm_ctx_device_status(self.handle, C.byref(st)), "device_status")
+        return st.value
+
+    def set_walk_limit(self, limit: int) -> None:
+        """Step limit of the bounded tree walks (0 = their structural bounds)."""
+        _check(lib().owm_ctx_set_walk_limit(self.handle, limit), "set_walk_limit")
+
     def cloud(self, xyz, bbox=None) -> Cloud:
         a = _as_xyz(xyz)
         h = C.c_void_p()

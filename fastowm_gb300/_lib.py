@@ -90,6 +90,7 @@ SIGNATURES = {
     "owm_ctx_launches": (i64, [vp]),
     "owm_ctx_device_status": (C.c_int, [vp, P(i32)]),
     "owm_ctx_set_profiling": (C.c_int, [vp, C.c_int]),
+    "owm_ctx_set_walk_limit": (C.c_int, [vp, i32]),
     "owm_ctx_kernel_times": (C.c_int, [vp, i32, vp, P(f64), P(i64), P(i32)]),
     "owm_cloud_create": (C.c_int, [vp, P(f64), i64, P(Bbox), P(vp)]),
     "owm_cloud_destroy": (C.c_int, [vp]),

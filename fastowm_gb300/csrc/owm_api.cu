@@ -276,6 +276,12 @@ int owm_ctx_device_status(owm_ctx* c, int32_t* status) {
   return OWM_OK;
 }
 
+int owm_ctx_set_walk_limit(owm_ctx* c, int32_t limit) {
+  if (!c || limit < 0) return OWM_EINVAL;
+  c->walk_limit = limit;
+  return OWM_OK;
+}
+
 int owm_ctx_set_profiling(owm_ctx* c, int on) {
   if (!c) return OWM_EINVAL;
   if (!on) {
@@ -663,7 +669,7 @@ int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_
   }
   rc = clear_status(c);
   if (!rc)
-    rc = run_stage3(tr->t.view(), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
+    rc = run_stage3(tr->t.view(c->walk_limit), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
                     c->d_job, c->d_small + kStatusSlot, c->stream, &c->launches);
   if (!rc) rc = check_input_status(c);
   if (rc) return rc;

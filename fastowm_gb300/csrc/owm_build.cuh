@@ -18,8 +18,9 @@ struct TreeStore {
   int32_t nleaves = 0, root = 0, key_bits = 0, max_leaf = 0;
   double ox = 0, oy = 0;
 
-  TreeView view() const {
+  TreeView view(int32_t walk_limit = 0) const {
     TreeView v;
+    v.walk_limit = walk_limit;
     v.xk = xk;
     v.yk = yk;
     v.zk = zk;

@@ -40,7 +40,8 @@ __device__ __forceinline__ uint32_t cell_min_warp(const TreeView& T, const Edge&
   if (lane == 0) st[0] = T.root;
   int top = 1;
   __syncwarp();
-  const int64_t round_bound = 2 * (int64_t)T.nleaves + 16;  // every node is popped at most once
+  // every node is popped at most once (or the test limit, walk_limit)
+  const int64_t round_bound = T.walk_limit > 0 ? (int64_t)T.walk_limit : 2 * (int64_t)T.nleaves + 16;
   for (int64_t round = 0; top > 0; ++round) {
     if (round >= round_bound) {
       if (lane == 0) atomicOr(status, kStatusWalkBound);

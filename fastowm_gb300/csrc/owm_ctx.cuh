@@ -96,6 +96,8 @@ struct owm_ctx {
   cudaEvent_t side_fork = nullptr, side_join = nullptr;
   bool stage12_side = false;
   int64_t next_ticket = 1;
+  // > 0: step limit of the bounded tree walks (owm_ctx_set_walk_limit)
+  int32_t walk_limit = 0;
 };
 
 namespace owm {

@@ -85,6 +85,10 @@ struct TreeView {
   int32_t nleaves;
   int32_t root;
   double ox, oy;        // origin of the float boxes
+  // > 0: step limit of the bounded tree walks (stage-1 walk steps, stage-3
+  // cell-walk rounds) in place of their structural bounds; lets a test make
+  // a walk give up on a well-formed tree (owm_ctx_set_walk_limit)
+  int32_t walk_limit = 0;
 };
 
 // ---------------------------------------------------------------------------

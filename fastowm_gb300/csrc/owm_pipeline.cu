@@ -92,7 +92,7 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   int rc = compute_edges(p, t.ox, t.oy, false, ex, ey, c->stream, &c->launches);
   if (rc) return rc;
   QueryJob j;
-  j.tree = t.view();
+  j.tree = t.view(c->walk_limit);
   j.ex = ex;
   j.ey = ey;
   j.ncols = (int32_t)p.ncols;
@@ -231,8 +231,8 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
   }
   rc = c->stage12_side
-           ? run_stage3_query(c->tree.view(), p, s3, d_ns3, s3scratch, s3cap, c->d_small + kStatusSlot, s, &c->launches)
-           : run_stage3(c->tree.view(), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
+           ? run_stage3_query(c->tree.view(c->walk_limit), p, s3, d_ns3, s3scratch, s3cap, c->d_small + kStatusSlot, s, &c->launches)
+           : run_stage3(c->tree.view(c->walk_limit), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
                         c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));

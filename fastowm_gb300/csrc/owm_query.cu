@@ -131,7 +131,7 @@ __device__ __forceinline__ void query_warp(const QueryJob* __restrict__ jobs, in
   // A well-formed depth-first walk visits each node at most once per phase;
   // the bound only guards against a corrupted hierarchy (then: status bit,
   // stop, no hang).
-  const int64_t step_bound = 4 * (int64_t)T.nleaves + 16;
+  const int64_t step_bound = T.walk_limit > 0 ? (int64_t)T.walk_limit : 4 * (int64_t)T.nleaves + 16;
   int64_t walked = 0;
 
   for (;;) {

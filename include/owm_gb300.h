@@ -134,6 +134,16 @@ int64_t owm_ctx_launches(const owm_ctx* ctx);
 /* Device status word: bit 0 non-finite input, bit 1 a bounded tree walk
  * overran (corrupt hierarchy; the call returned OWM_ETIMEOUT). */
 int owm_ctx_device_status(owm_ctx* ctx, int32_t* status);
+/* Step limit of this context's bounded tree walks: the stage-1 walk
+ * (owm_stage1, stage1_walk = 1) stops after `limit` node steps per window and
+ * the stage-3 cell walk after `limit` rounds per cell, instead of their
+ * structural bounds (which only a corrupt hierarchy can reach).  A walk that
+ * stops sets bit 1 of the device status word and its call returns
+ * OWM_ETIMEOUT; the context stays usable.  0 restores the structural bounds.
+ * For testing the failure path on a well-formed tree; no counterpart in the
+ * reference, which has no bounded walk (it prints CUDA errors and goes on,
+ * SYCL-CUDA-GPU/ordered/cuda/ordered_builder.inl:330-333). */
+int owm_ctx_set_walk_limit(owm_ctx* ctx, int32_t limit);
 /* Per-kernel CUDA-event timing of this context's launches (1 = on). */
 int owm_ctx_set_profiling(owm_ctx* ctx, int on);
 /* Sums the recorded kernel times by kernel name since the last call (and
@@ -225,16 +235,19 @@ int owm_stage3(owm_ctx* ctx, const owm_tree* tree, const owm_params* params, con
  * (a host that owns all GPU memory through its own pool, a plugin whose host
  * forbids allocation on the streams it lends, a real-time loop where an
  * allocation and its implicit synchronisation are not allowed).  Same
- * result as owm_stage2 (LLPs ascending), but d_win_min (int64, -1 = none)
- * and d_llp (room for ncells ids) are caller-owned DEVICE memory, npoints
- * bounds the ids, and the work runs on `stream` (a cudaStream_t; NULL = the
- * legacy default stream), which is synchronised before *n_llp is set.
+ * result as owm_stage2 (LLPs ascending), but d_win_min (int64, negative =
+ * none) and d_llp (room for ncells ids) are caller-owned DEVICE memory, and
+ * every id must lie in [0, npoints]: a larger id makes the call return
+ * OWM_EINVAL (d_llp is then undefined).  The work runs on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream of the current device), on
+ * the device that owns it (made current for the call, the caller's device
+ * restored after), and the stream is synchronised before *n_llp is set.
  * Working memory is one static device array of about 21.5 MB that every
  * GPU loading this library holds until exit; at most 1,048,576 windows per
- * call (OWM_ERANGE above that).  The first call on a device looks up the
- * array's address (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race,
- * so serialise them. */
+ * call (OWM_ERANGE above that).  The first call in each CUDA context of a
+ * device looks up the array's address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race, so serialise them. */
 int owm_stage2_noalloc(void* stream, const int64_t* d_win_min, int64_t ncells, double overlap,
                        int64_t npoints, int64_t* d_llp, int64_t* n_llp);
 

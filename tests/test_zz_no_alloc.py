@@ -3,9 +3,12 @@ allocate device memory (their host owns every device byte through its own
 pool, or forbids allocation on the streams it lends them).
 
 Called through the C ABI with caller-owned device buffers, and compared with
-the allocating owm_stage2 on two calls in a row (different inputs, so a
-stale result left in the shared static working array would show).  The ids
-are integers, so the comparison is exact.
+the allocating owm_stage2 on calls in a row (different inputs, so a stale
+result left in the shared static working array would show).  The ids are
+integers, so the comparison is exact.  Also: ids above npoints are refused
+(OWM_EINVAL) instead of giving a wrong list, overlap 0 keeps every valid
+minimum, npoints on either side of a power of two (the top key bit of the
+sort), and a stream other than the default one.
 """
 import ctypes as C
 
@@ -30,15 +33,33 @@ def _windows(F, ctx, config, n, w, h, overlap=None):
     return win, Ov, n
 
 
-def _noalloc(F, torch, win, overlap, npoints):
+def _noalloc_rc(F, torch, win, overlap, npoints, stream=None):
     d_win = torch.as_tensor(win, dtype=torch.int64).cuda()
     d_llp = torch.full((win.size,), -7, dtype=torch.int64, device="cuda")
     n = C.c_int64(-1)
-    stream = torch.cuda.current_stream().cuda_stream
-    rc = F.lib().owm_stage2_noalloc(C.c_void_p(stream), C.c_void_p(d_win.data_ptr()), win.size, overlap, npoints,
-                                    C.c_void_p(d_llp.data_ptr()), C.byref(n))
+    st = stream if stream is not None else torch.cuda.current_stream()
+    with torch.cuda.stream(st):
+        rc = F.lib().owm_stage2_noalloc(C.c_void_p(st.cuda_stream), C.c_void_p(d_win.data_ptr()), win.size, overlap,
+                                        npoints, C.c_void_p(d_llp.data_ptr()), C.byref(n))
+    torch.cuda.synchronize()
+    return rc, n.value, d_llp
+
+
+def _noalloc(F, torch, win, overlap, npoints, stream=None):
+    rc, n, d_llp = _noalloc_rc(F, torch, win, overlap, npoints, stream)
     assert rc == 0, F.lib().owm_status_string(rc)
-    return d_llp[: n.value].cpu().numpy()
+    return d_llp[:n].cpu().numpy()
+
+
+def _llp_of(win, overlap):
+    """Stage 2 restated on the host: ids that occur at least twice (overlap >
+    0) or every valid id (overlap == 0), ascending."""
+    v = np.sort(np.asarray(win, dtype=np.int64))
+    v = v[v >= 0]
+    if overlap == 0.0:
+        return v
+    u, c = np.unique(v, return_counts=True)
+    return u[c >= 2]
 
 
 def test_noalloc_stage2_matches_allocating_stage2(owm):
@@ -61,3 +82,41 @@ def test_noalloc_rejects_oversize(owm):
                                       C.c_void_p(d.data_ptr()), C.byref(n))
     assert rc == -6  # OWM_ERANGE, before any work is issued
     assert n.value == -1
+
+
+def test_noalloc_overlap_zero_and_key_width_edges(owm):
+    """overlap 0 through the entry point, and synthetic window lists whose
+    largest id is npoints itself, for npoints just below, at and just above a
+    power of two (the sort orders only the key bits that ids up to npoints
+    need, with "none" above them)."""
+    torch = pytest.importorskip("torch")
+    ctx = owm.Context(0)
+    win, _, npts = _windows(owm, ctx, 1, 200_000, 90, 100, overlap=0.0)
+    want = ctx.stage2(win.copy(), 0.0)
+    np.testing.assert_array_equal(_noalloc(owm, torch, win, 0.0, npts), want)
+    np.testing.assert_array_equal(want, _llp_of(win, 0.0))
+    rng = np.random.default_rng(11)
+    side = torch.cuda.Stream()
+    for npoints in ((1 << 20) - 2, (1 << 20) - 1, 1 << 20, (1 << 16) + 1):
+        w = rng.integers(max(0, npoints - 3000), npoints + 1, 200_000)
+        w[rng.random(w.size) < 0.1] = -1
+        w[:3] = npoints  # the largest id, repeated
+        for ov in (0.8, 0.0):
+            got = _noalloc(owm, torch, w, ov, npoints, stream=side)
+            np.testing.assert_array_equal(got, _llp_of(w, ov))
+            np.testing.assert_array_equal(got, ctx.stage2(w.copy(), ov))
+    ctx.close()
+
+
+def test_noalloc_rejects_ids_above_npoints(owm):
+    """An id above npoints names no point: OWM_EINVAL, not a wrong list; the
+    next call with valid ids is exact again (the flag is cleared per call)."""
+    torch = pytest.importorskip("torch")
+    w = np.array([5, 5, 7, 7, 9, 1001, -1], dtype=np.int64)
+    rc, _, _ = _noalloc_rc(owm, torch, w, 0.8, 1000)
+    assert rc == -1  # OWM_EINVAL
+    w[5] = 1000
+    np.testing.assert_array_equal(_noalloc(owm, torch, w, 0.8, 1000), [5, 7])
+    big = np.full(64, 1 << 40, dtype=np.int64)
+    rc, _, _ = _noalloc_rc(owm, torch, big, 0.5, 1 << 20)
+    assert rc == -1
