@@ -524,7 +524,8 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
   }
   count_launch(launches);
   bool alt = false;
-  OWM_CUDA_TRY(radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches, plan.parts > 0));
+  OWM_CUDA_TRY(
+      radix_sort(k0, v0, k1, v1, n, key_bits, true, sort_tmp, sort_bytes, s, &alt, launches, plan.parts > 0, status));
   const uint32_t* mk = alt ? k1 : k0;
   const uint32_t* perm = alt ? v1 : v0;
 

@@ -149,7 +149,7 @@ size_t scan_temp_bytes(int64_t n);
 // RadixSortPlan) at the start of temp.
 cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int64_t n, int end_bit,
                        bool iota_vals, void* temp, size_t temp_bytes, cudaStream_t s, bool* in_alt,
-                       int64_t* launches, bool first_counts_given = false);
+                       int64_t* launches, bool first_counts_given = false, uint32_t* status = nullptr);
 
 // Digit width of pass `pass` of a sort on end_bit key bits: the fewest 8-bit
 // passes, their widths balanced (differing by at most one bit, wider first):

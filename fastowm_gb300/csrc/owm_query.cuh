@@ -23,7 +23,7 @@ struct QueryJob {
 
 // Status bits of the context's device status word.
 constexpr uint32_t kStatusNonFinite = 1u;  // non-finite input coordinate
-constexpr uint32_t kStatusWalkBound = 2u;  // a tree walk exceeded its step bound
+constexpr uint32_t kStatusWalkBound = 2u;  // a tree walk exceeded its step bound, or a bounded wait ran out
 
 // Edge tables of the stage-1 windows (cells == false) or of the stage-3 cells
 // (cells == true) of params p, float offsets relative to (ox, oy).

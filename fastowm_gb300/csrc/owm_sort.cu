@@ -7,13 +7,20 @@
 //   upsweep    digit histogram of each chunk (vectorised 16-byte key loads)
 //   scan       exclusive scan of the digit-major [256 x chunks] count table
 //              (small sorts: per tile, [256 x tiles])
-//   downsweep  stable ranking inside the tile with a ballot-based warp
-//              multisplit, keys/values staged in shared memory in digit order,
-//              then written out so that each digit's run is a contiguous,
-//              coalesced stretch of the output.
+//   downsweep  stable ranking inside the tile, keys/values staged in shared
+//              memory in digit order, then written out so that each digit's
+//              run is a contiguous, coalesced stretch of the output.
+// Digits of at most 7 bits are ranked by k_rs_downsweep_rank: every thread
+// counts its 16 consecutive keys in its own byte counters (shared-memory
+// atomics, no warp vote), a word-parallel scan turns the counters into
+// ranks, and tiles arrive by TMA (cp.async.bulk.tensor, 128-byte swizzle,
+// mbarrier completion).  8-bit digits keep the ballot-multisplit kernel
+// (k_rs_downsweep_pipe).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "owm_internal.cuh"
 
@@ -474,6 +481,382 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
   }
 }
 
+// ---- ranked downsweep (digits of at most 7 bits) ------------------------------
+// Tile t = keys [4096 t, 4096 t + 4096), seen through a 2-D tensor map as 128
+// rows of 32 uint32 (rows of 128 bytes; the map covers the n / 32 full rows,
+// so rows past it -- the ragged end of the last tile -- arrive as zeros and
+// are fixed up by plain loads).  The TMA box {32, 128} lands in shared
+// memory with the 128-byte swizzle: the 16-byte chunk c of row r is stored
+// at chunk c ^ (r & 7).  Thread t owns the 16 consecutive keys 16t..16t+15
+// (row t/2, chunks 4(t&1)..4(t&1)+3), so its four 16-byte reads, taken by a
+// quarter warp at a time, hit eight different chunks of four rows: no bank
+// conflicts.
+constexpr int kRkMaxBits = 7;
+constexpr int kRkDigits = 1 << kRkMaxBits;  // 128
+constexpr int kRkQuads = kRkDigits / 4;     // byte-counter words per thread
+constexpr int kRkGroups = kBlock / 8;       // 32 groups of 8 threads
+// gt[g][d] (uint16) at g * kRkGtRow + d: word 65g + d/2, bank (g + d/2) % 32, so
+// the scan's writes (one group per lane, one digit) and the rank's reads (4
+// groups per warp, any digits) spread over the banks
+constexpr int kRkGtRow = kRkDigits + 2;
+constexpr uint32_t kRkTileBytes = kTile * 4;  // one array's tile: 16 KB
+constexpr uint32_t kStatusWaitExpired = 2u;   // the status bit of a bounded wait that ran out
+constexpr unsigned long long kRkWaitNs = 2000000000ull;  // 2 s: a TMA tile arrives in microseconds
+
+struct RkSmem {  // byte offsets into the (1024-aligned) dynamic shared memory
+  uint32_t stage[2];  // per stage: keys tile, then the values tile when present
+  uint32_t cnt, gt, S, dtot, adj, mbar, total;
+};
+__host__ __device__ constexpr RkSmem rk_layout(bool has_vals) {
+  const uint32_t stage_bytes = kRkTileBytes * (has_vals ? 2u : 1u);
+  RkSmem L{};
+  L.stage[0] = 0;
+  L.stage[1] = stage_bytes;
+  L.cnt = 2 * stage_bytes;                               // [kRkQuads][kBlock] u32: 4 byte counters
+  L.gt = L.cnt + kRkQuads * kBlock * 4;                  // [kRkGroups][kRkGtRow] u16
+  L.S = L.gt + kRkGroups * kRkGtRow * 2;                 // [kRkDigits] u32 digit start in the tile
+  L.dtot = L.S + kRkDigits * 4;                          // [kRkDigits] u32 digit count in the tile
+  L.adj = L.dtot + kRkDigits * 4;                        // [kRkDigits] u32 output offset - start
+  L.mbar = L.adj + kRkDigits * 4;                        // 2 x u64
+  L.total = L.mbar + 16;
+  return L;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Waits for the phase with the given parity, at most kRkWaitNs; false when
+// the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  const unsigned long long t0 = global_ns();
+  for (uint32_t it = 1;; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 255u) == 0 && global_ns() - t0 > kRkWaitNs) return false;
+  }
+}
+// Tile box {32 columns, 128 rows} at row `row` into shared memory dst.
+__device__ __forceinline__ void tma_tile(uint32_t dst, const CUtensorMap* map, int32_t row, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(row), "r"(bar)
+      : "memory");
+}
+
+// Thread 0: refills stage stg with tile t (keys, and values when kLoadVals);
+// returns the stage's pending bit.
+template <bool kLoadVals>
+__device__ __forceinline__ uint32_t rk_issue(const CUtensorMap* tm_k, const CUtensorMap* tm_v, uint32_t stage_sm,
+                                             uint32_t stage_stride, uint32_t bar0, int64_t t, int stg) {
+  const uint32_t bar = bar0 + 8u * stg;
+  const uint32_t dst = stage_sm + stage_stride * stg;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic accesses to the stage come first
+  mbar_expect_tx(bar, kRkTileBytes * (kLoadVals ? 2u : 1u));
+  tma_tile(dst, tm_k, (int32_t)(t * (kTile / 32)), bar);
+  if (kLoadVals) tma_tile(dst + kRkTileBytes, tm_v, (int32_t)(t * (kTile / 32)), bar);
+  return 1u << stg;
+}
+
+// Persistent downsweep of one pass with a digit of dbits <= 7 bits over the
+// chunks of k_rs_upsweep_chunk (same count table as k_rs_downsweep_pipe).
+// Per tile:
+//   count  thread t adds each of its keys to its own byte counter of the
+//          key's digit (word (d / 4, t), byte d % 4) with a shared-memory
+//          atomic add, whose returned old value is the key's rank among the
+//          thread's earlier keys of that digit (at most 15: one byte);
+//   scan   per word of four digits, lane g of a warp takes the 8 words of
+//          threads 8g..8g+7: an exclusive running sum of the words (byte-
+//          wise, at most 128, so no carries) gives each thread's offset
+//          inside its group, written back in place; the group totals, as
+//          two words of 16-bit halves, take one warp scan for the 32 groups
+//          (group offsets gt, digit totals); warp 0 scans the digit totals
+//          (S = digit starts) and moves every digit's running output offset;
+//   rank   key position = S[d] + gt[d][group] + in-group offset + own rank:
+//          stable, since the order (digit, thread, item) is the tile order
+//          within a digit; keys and values are stored there, in the tile's
+//          own stage buffer (the thread holds its keys in registers);
+//   write  each digit's run goes to its contiguous stretch of the output.
+// Two stages: tile t+1 is in flight while tile t is ranked; a stage is
+// refilled once the tile in it has been written out.  A TMA wait is bounded
+// (kRkWaitNs): if one ever runs out, the block sets kStatusWaitExpired in
+// *status, waits (bounded again) for its copies still in flight, and ends.
+template <bool kHasVals, bool kIota>
+__global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_constant__ CUtensorMap tm_k,
+                                                                 const __grid_constant__ CUtensorMap tm_v,
+                                                                 const uint32_t* __restrict__ kin,
+                                                                 const uint32_t* __restrict__ vin,
+                                                                 uint32_t* __restrict__ kout,
+                                                                 uint32_t* __restrict__ vout, int shift, int dbits,
+                                                                 int64_t ntiles, const uint32_t* __restrict__ hist,
+                                                                 int64_t n, uint32_t* __restrict__ status) {
+  constexpr bool kLoadVals = kHasVals && !kIota;
+  constexpr RkSmem L = rk_layout(kHasVals);
+  constexpr uint32_t kStageBytes = kRkTileBytes * (kHasVals ? 2u : 1u);
+  static_assert(L.stage[0] == 0 && L.stage[1] == kStageBytes, "stage s starts at s * kStageBytes");
+  extern __shared__ unsigned char rk_raw[];
+  unsigned char* base = rk_raw + ((1024u - (smem_u32(rk_raw) & 1023u)) & 1023u);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(base + L.cnt);
+  uint16_t* gt = reinterpret_cast<uint16_t*>(base + L.gt);
+  uint32_t* S = reinterpret_cast<uint32_t*>(base + L.S);
+  uint32_t* dtot = reinterpret_cast<uint32_t*>(base + L.dtot);
+  uint32_t* adj = reinterpret_cast<uint32_t*>(base + L.adj);
+  const uint32_t bar0 = smem_u32(base + L.mbar);
+
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const uint32_t dmask = (1u << dbits) - 1u;
+  const int nquads = ((1 << dbits) + 3) >> 2;
+  int64_t t0, t1;
+  chunk_tiles(ntiles, gridDim.x, blockIdx.x, &t0, &t1);
+  const int64_t full_end = (n >> 5) << 5;  // keys covered by the tensor maps
+
+  // warp 0, lane l: running output offsets of digits 4l..4l+3 (the scanned
+  // count of this chunk's first upsweep part)
+  uint32_t run[4] = {0, 0, 0, 0};
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = 4 * lane + k;
+      if (d <= (int)dmask) run[k] = hist[(int64_t)d * gridDim.x * kSubChunks + (int64_t)blockIdx.x * kSubChunks];
+    }
+  }
+  for (int i = tid; i < nquads * (kBlock / 4); i += kBlock) reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
+  uint32_t pending = 0;  // thread 0: bit s = a copy into stage s is in flight
+  const uint32_t stage_sm = smem_u32(base);  // stage s at s * kStageBytes
+  const uint32_t stage_stride = kStageBytes;
+  if (tid == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (t0 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t0, 0);
+    if (t0 + 1 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t0 + 1, 1);
+  }
+  __syncthreads();
+
+  for (int64_t t = t0; t < t1; ++t) {
+    const int stg = (int)((t - t0) & 1);
+    const bool arrived = mbar_wait_bounded(bar0 + 8u * stg, (uint32_t)(((t - t0) >> 1) & 1));
+    if (tid == 0 && arrived) pending &= ~(1u << stg);
+    uint32_t* sk = reinterpret_cast<uint32_t*>(base + (uint32_t)stg * kStageBytes);
+    uint32_t* sv = reinterpret_cast<uint32_t*>(base + (uint32_t)stg * kStageBytes + kRkTileBytes);
+    const int64_t tile_base = t * kTile;
+    const int64_t my0 = tile_base + 16 * tid;
+    uint32_t k[16], v[16];
+    {
+      const int r = tid >> 1;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int word = r * 32 + ((((tid & 1) * 4 + j) ^ (r & 7)) << 2);
+        const uint4 q = *reinterpret_cast<const uint4*>(sk + word);
+        k[4 * j] = q.x;
+        k[4 * j + 1] = q.y;
+        k[4 * j + 2] = q.z;
+        k[4 * j + 3] = q.w;
+        if (kLoadVals) {
+          const uint4 u = *reinterpret_cast<const uint4*>(sv + word);
+          v[4 * j] = u.x;
+          v[4 * j + 1] = u.y;
+          v[4 * j + 2] = u.z;
+          v[4 * j + 3] = u.w;
+        }
+      }
+    }
+    if (my0 + 16 > full_end) {  // the last tile's ragged end: past the maps, or past n
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int64_t p = my0 + i;
+        if (p >= n) {
+          k[i] = 0xFFFFFFFFu;  // after every key: the top digit, and later in tile order
+        } else if (p >= full_end) {
+          k[i] = __ldg(kin + p);
+          if (kLoadVals) v[i] = __ldg(vin + p);
+        }
+      }
+    }
+    if (kIota) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = (uint32_t)(my0 + i);
+    }
+    // count: own rank of every key among this thread's keys of its digit
+    uint32_t own[2] = {0u, 0u};  // 16 nibbles
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const uint32_t d = (k[i] >> shift) & dmask;
+      const uint32_t sh = (d & 3u) * 8u;
+      const uint32_t old = atomicAdd(cnt + (d >> 2) * kBlock + tid, 1u << sh);
+      own[i >> 3] |= ((old >> sh) & 0xFFu) << ((i & 7) * 4);
+    }
+    if (__syncthreads_or(!arrived)) {  // a tile never arrived: stop the block
+      if (tid == 0) {
+        atomicOr(status, kStatusWaitExpired);
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2)
+          if (pending & (1u << s2))
+            mbar_wait_bounded(bar0 + 8u * s2, (uint32_t)((((t - t0) + (s2 != stg ? 1 : 0)) >> 1) & 1));
+      }
+      return;
+    }
+    // scan: in-group offsets in place, group offsets gt, digit totals
+    for (int q = w; q < nquads; q += kWarps) {
+      uint32_t* gw = cnt + q * kBlock + lane * 8;
+      uint4 a = *reinterpret_cast<uint4*>(gw);
+      uint4 b = *reinterpret_cast<uint4*>(gw + 4);
+      uint32_t acc = 0, e;
+      e = acc; acc += a.x; a.x = e;
+      e = acc; acc += a.y; a.y = e;
+      e = acc; acc += a.z; a.z = e;
+      e = acc; acc += a.w; a.w = e;
+      e = acc; acc += b.x; b.x = e;
+      e = acc; acc += b.y; b.y = e;
+      e = acc; acc += b.z; b.z = e;
+      e = acc; acc += b.w; b.w = e;
+      *reinterpret_cast<uint4*>(gw) = a;
+      *reinterpret_cast<uint4*>(gw + 4) = b;
+      const uint32_t g02 = acc & 0x00FF00FFu, g13 = (acc >> 8) & 0x00FF00FFu;  // digits 4q+{0,2}, 4q+{1,3}
+      uint32_t i02 = g02, i13 = g13;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, i02, o), y = __shfl_up_sync(0xffffffffu, i13, o);
+        if (lane >= o) {
+          i02 += x;
+          i13 += y;
+        }
+      }
+      const uint32_t e02 = i02 - g02, e13 = i13 - g13;
+      uint16_t* gl = gt + lane * kRkGtRow + 4 * q;
+      gl[0] = (uint16_t)(e02 & 0xFFFFu);
+      gl[1] = (uint16_t)(e13 & 0xFFFFu);
+      gl[2] = (uint16_t)(e02 >> 16);
+      gl[3] = (uint16_t)(e13 >> 16);
+      if (lane == 31) {
+        dtot[4 * q + 0] = i02 & 0xFFFFu;
+        dtot[4 * q + 1] = i13 & 0xFFFFu;
+        dtot[4 * q + 2] = i02 >> 16;
+        dtot[4 * q + 3] = i13 >> 16;
+      }
+    }
+    __syncthreads();
+    if (w == 0) {  // digit starts and output offsets, lane l: digits 4l..4l+3
+      uint32_t c[4], sum = 0;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const int d = 4 * lane + kk;
+        c[kk] = d <= (int)dmask ? dtot[d] : 0u;
+        sum += c[kk];
+      }
+      uint32_t pre = warp_incl_scan(sum) - sum;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const int d = 4 * lane + kk;
+        if (d <= (int)dmask) {
+          S[d] = pre;
+          adj[d] = run[kk] - pre;  // output slot of tile position j of digit d: adj[d] + j
+          run[kk] += c[kk];
+        }
+        pre += c[kk];
+      }
+    }
+    __syncthreads();
+    // rank and place into the stage buffer, now in digit order
+    {
+      const uint16_t* gg = gt + (tid >> 3) * kRkGtRow;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const uint32_t d = (k[i] >> shift) & dmask;
+        const uint32_t sh = (d & 3u) * 8u;
+        const uint32_t in_group = (cnt[(d >> 2) * kBlock + tid] >> sh) & 0xFFu;
+        const uint32_t pos = S[d] + gg[d] + in_group + ((own[i >> 3] >> ((i & 7) * 4)) & 15u);
+        sk[pos] = k[i];
+        if (kHasVals) sv[pos] = v[i];
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < nquads * (kBlock / 4); i += kBlock)  // for the next tile
+      reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
+    {
+      const int tn = (int)(n - tile_base < kTile ? n - tile_base : kTile);
+      for (int j = tid; j < tn; j += kBlock) {
+        const uint32_t key = sk[j];
+        const uint32_t gp = adj[(key >> shift) & dmask] + (uint32_t)j;
+        kout[gp] = key;
+        if (kHasVals) vout[gp] = sv[j];
+      }
+    }
+    __syncthreads();  // stage stg is free again
+    if (tid == 0 && t + 2 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t + 2, stg);
+  }
+}
+
+size_t rank_smem_bytes(bool has_vals) { return rk_layout(has_vals).total + 1024; }
+
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link-time
+// dependence on the driver library).
+using EncodeTiledFn = CUresult(CUDAAPI*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                         const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                         CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                         CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// Tensor map of a uint32 array of n keys as rows of 32 (the n / 32 full
+// rows), boxes of 128 rows, 128-byte swizzle.  False when it cannot be made
+// (n < 32, a base that is not 16-byte aligned, no entry point).
+bool tile_map(CUtensorMap* m, const uint32_t* base, int64_t n) {
+  EncodeTiledFn fn = encode_tiled();
+  const int64_t rows = n >> 5;
+  if (!fn || rows <= 0 || rows > ((int64_t)1 << 31) || (reinterpret_cast<uintptr_t>(base) & 15u)) return false;
+  const cuuint64_t dims[2] = {32, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {128};
+  const cuuint32_t box[2] = {32, (cuuint32_t)(kTile / 32)};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<uint32_t*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool kHasVals, bool kIota>
+cudaError_t launch_rank(const CUtensorMap& mk, const CUtensorMap& mv, const uint32_t* kin, const uint32_t* vin,
+                        uint32_t* kout, uint32_t* vout, int shift, int dbits, int64_t ntiles, int64_t chunks,
+                        const uint32_t* hist, int64_t n, uint32_t* status, cudaStream_t s) {
+  static bool configured = false;  // per template instance
+  const size_t smem = rank_smem_bytes(kHasVals);
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_rs_downsweep_rank<kHasVals, kIota>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  OWM_LAUNCH("k_rs_downsweep", s, (k_rs_downsweep_rank<kHasVals, kIota><<<(unsigned)chunks, kBlock, smem, s>>>(
+      mk, mv, kin, vin, kout, vout, shift, dbits, ntiles, hist, n, status)));
+  return cudaGetLastError();
+}
+
 template <bool kHasVals, bool kIota>
 size_t pipe_smem_bytes() {
   constexpr bool kLoadVals = kHasVals && !kIota;
@@ -568,7 +951,7 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
 
 cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int64_t n, int end_bit,
                        bool iota_vals, void* temp, size_t temp_bytes, cudaStream_t s, bool* in_alt,
-                       int64_t* launches, bool first_counts_given) {
+                       int64_t* launches, bool first_counts_given, uint32_t* status) {
   *in_alt = false;
   if (n <= 0) return cudaSuccess;
   if (temp_bytes < radix_sort_temp_bytes(n) || end_bit <= 0 || end_bit > 32) return cudaErrorInvalidValue;
@@ -584,6 +967,14 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   // large sorts: one contiguous chunk of tiles per persistent block (two per SM)
   const int64_t chunks = sort_chunks(ntiles);
   if (first_counts_given && !chunks) return cudaErrorInvalidValue;
+  // TMA views of the four buffers for the ranked downsweep (digits <= 7 bits)
+  CUtensorMap maps[4];  // k0, k1, v0, v1
+  bool maps_ok = chunks > 0 && tile_map(&maps[0], k0, n) && tile_map(&maps[1], k1, n);
+  if (maps_ok && has_vals) maps_ok = tile_map(&maps[2], v0, n) && tile_map(&maps[3], v1, n);
+  if (!maps_ok) maps[2] = maps[3] = maps[1] = maps[0];  // unused (pipe kernel); keeps them initialised
+  if (maps_ok && !has_vals) maps[2] = maps[3] = maps[0];
+  // where a bounded wait that runs out is recorded when the caller gives no status word
+  uint32_t* st = status ? status : reinterpret_cast<uint32_t*>(static_cast<char*>(temp) + temp_bytes - 256);
   int pass = 0;
   for (int shift = 0; shift < end_bit; shift += radix_digit_bits(end_bit, pass++)) {
     // a pass sorts on bits [shift, shift + dbits); higher key bits are ignored
@@ -598,11 +989,22 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
       cudaError_t e = exclusive_scan_u32(hist, hist, (chunks * kSubChunks) << dbits, nullptr, stemp, sbytes, s, launches);
       if (e != cudaSuccess) return e;
       cudaError_t e2;
-      if (has_vals)
+      if (maps_ok && dbits <= kRkMaxBits) {
+        const CUtensorMap& mk = maps[alt ? 1 : 0];
+        const CUtensorMap& mv = maps[alt ? 3 : 2];
+        if (has_vals)
+          e2 = (first && iota_vals)
+                   ? launch_rank<true, true>(mk, mv, ka, va, kb, vb, shift, dbits, ntiles, chunks, hist, n, st, s)
+                   : launch_rank<true, false>(mk, mv, ka, va, kb, vb, shift, dbits, ntiles, chunks, hist, n, st, s);
+        else
+          e2 = launch_rank<false, false>(mk, mv, ka, nullptr, kb, nullptr, shift, dbits, ntiles, chunks, hist, n, st,
+                                         s);
+      } else if (has_vals) {
         e2 = (first && iota_vals) ? launch_pipe<true, true>(ka, va, kb, vb, shift, dbits, ntiles, chunks, hist, n, s)
                                   : launch_pipe<true, false>(ka, va, kb, vb, shift, dbits, ntiles, chunks, hist, n, s);
-      else
+      } else {
         e2 = launch_pipe<false, false>(ka, nullptr, kb, nullptr, shift, dbits, ntiles, chunks, hist, n, s);
+      }
       if (e2 != cudaSuccess) return e2;
     } else {  // small sorts: one block per tile, per-tile counts
       OWM_LAUNCH("k_rs_upsweep", s, k_rs_upsweep<<<(unsigned)ntiles, kBlock, 0, s>>>(ka, n, shift, dmask, hist, ntiles));

@@ -131,8 +131,8 @@ int owm_ctx_sync(owm_ctx* ctx);
 void* owm_ctx_stream(owm_ctx* ctx); /* the context's cudaStream_t */
 /* Number of this library's kernel launches issued on the context so far. */
 int64_t owm_ctx_launches(const owm_ctx* ctx);
-/* Device status word: bit 0 non-finite input, bit 1 a bounded tree walk
- * overran (corrupt hierarchy; the call returned OWM_ETIMEOUT). */
+/* Device status word: bit 0 non-finite input, bit 1 a bounded tree walk or
+ * bounded device wait ran out (the call returned OWM_ETIMEOUT). */
 int owm_ctx_device_status(owm_ctx* ctx, int32_t* status);
 /* Step limit of this context's bounded tree walks: the stage-1 walk
  * (owm_stage1, stage1_walk = 1) stops after `limit` node steps per window and
