@@ -289,6 +289,141 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+# The reference's GPU program (SYCL-CUDA-GPU/mainBuilder.cu, "owm-cuda") reads
+# only clouds it knows by file name: readHeader (basic/utils.h:225-311) gives
+# their point counts and boxes, map_file_atof_tbb_th (basic/utils.h:338-395)
+# reads x, y and z at columns 0, 10 and 22 of each line.  The GPU bar writes a
+# seeded synthetic cloud of one such size and box in that format and times
+# both programs on the same points.
+GPUBAR_CLOUDS = {  # name: (file name, points, (min_x, min_y, max_x, max_y))
+    "alcoy": ("INAER_2011_Alcoy.xyz", 2772832, (715244.96, 4286623.63, 716057.75, 4287447.70)),
+    "alcoy_x2": ("INAER_2011_Alcoy_CoreX2.xyz", 20380212 * 2, (714947.98, 4286501.93, 716361.06, 4288406.23)),
+    "alcoy_x4": ("INAER_2011_Alcoy_CoreX4.xyz", 20380212 * 4, (714947.98, 4286501.93, 716361.06, 4288406.23)),
+    "alcoy_x6": ("INAER_2011_Alcoy_CoreX6.xyz", 20380212 * 6, (714947.98, 4286501.93, 716361.06, 4288406.23)),
+}
+GPUBAR_W, GPUBAR_O, GPUBAR_B = 10, 0.8, 20  # owm-cuda fixes Wsize 10 and overlap 0.8 (octree_traverse.inl:18-20)
+
+
+def gpubar_points(name: str, synth_config, synth_cloud):
+    """(X, Y, Z): the cloud in integer centimetres (x, y) and millimetres (z),
+    from the project's generator (config 2 terrain) over the named cloud's box,
+    inside the box.  The exact doubles are X / 100, Y / 100, Z / 1000 -- what
+    a correctly rounded reader makes of the text."""
+    fname, n, (x0, y0, x1, y1) = GPUBAR_CLOUDS[name]
+    spec, *_, seed = synth_config(2)
+    spec.n = n
+    spec.x0, spec.y0, spec.x1, spec.y1 = x0, y0, x1, y1
+    xyz, _ = synth_cloud(spec, seed)
+    X = np.clip(np.rint(xyz[:, 0] * 100.0).astype(np.int64), int(round(x0 * 100)), int(round(x1 * 100)))
+    Y = np.clip(np.rint(xyz[:, 1] * 100.0).astype(np.int64), int(round(y0 * 100)), int(round(y1 * 100)))
+    Z = np.rint(xyz[:, 2] * 1000.0).astype(np.int64)
+    return X, Y, Z
+
+
+def gpubar_write(path: str, X, Y, Z) -> None:
+    """'%9.2f %10.2f %8.3f' lines (x at column 0, y at 10, z's digits from 22
+    on) of the non-negative integers X, Y (centimetres) and Z (millimetres)."""
+    n = X.size
+    L = 30
+    body = np.full((n, L), ord(" "), dtype=np.uint8)
+
+    def put(col, width, v, ndec):
+        end = col + width
+        ip, fp = np.divmod(v, 10 ** ndec)
+        for k in range(ndec):
+            body[:, end - 1 - k] = (48 + (fp // 10 ** k) % 10).astype(np.uint8)
+        body[:, end - 1 - ndec] = ord(".")
+        for k in range(width - ndec - 1):
+            digit = (48 + (ip // 10 ** k) % 10).astype(np.uint8)
+            body[:, end - 2 - ndec - k] = digit if k == 0 else np.where(ip >= 10 ** k, digit, np.uint8(32))
+
+    put(0, 9, X, 2)
+    put(10, 10, Y, 2)
+    put(21, 8, Z, 3)
+    body[:, L - 1] = ord("\n")
+    with open(path, "wb") as f:
+        f.write(body.tobytes())
+
+
+def run_gpubar_reference(args) -> None:
+    """The reference's own GPU program on the GB300: builds oracle/_ref/owm-cuda
+    (make -C oracle gpubar), writes the named cloud, runs it, and prints its
+    own timings (tree build; stage 1 kernel; stage 2 on the host), each the
+    mean of its 5 runs (octree_traverse.inl:67-111)."""
+    from oracle import oracle as O
+
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "gpubar"], check=True)
+    fname, n, bb = GPUBAR_CLOUDS[args.gpu_bar]
+    X, Y, Z = gpubar_points(args.gpu_bar, O.synth_config, O.synth_cloud)
+    work = Path(os.environ.get("TMPDIR", "/tmp")) / "owm_gpubar"
+    work.mkdir(parents=True, exist_ok=True)
+    path = work / fname
+    gpubar_write(str(path), X, Y, Z)
+    del X, Y, Z
+    t0 = time.perf_counter()
+    r = subprocess.run([str(ROOT / "oracle" / "_ref" / "owm-cuda"), str(path), str(args.gpu_bar_leaf)],
+                       capture_output=True, text=True, timeout=1200)
+    wall = time.perf_counter() - t0
+    path.unlink()
+    out = r.stdout
+    vals = {}
+    for key, pat in (("tree_ms", "Tree Construction CUDA time"), ("stage1_ms", "Stage1 KERNEL CUDA time"),
+                     ("stage2_ms", "Stage2 KERNEL CUDA time"), ("total_ms", "Total TIME (Tree+OWM)")):
+        for ln in out.splitlines():
+            if pat in ln:
+                vals[key] = float(ln.split(":")[1].split()[0])
+    seeds = [ln for ln in out.splitlines() if "seed points" in ln]
+    vals["seeds"] = int(seeds[-1].split(":")[1]) if seeds else None
+    line = {"gpu_bar": "reference", "program": "SYCL-CUDA-GPU/mainBuilder.cu (owm-cuda), unmodified, nvcc sm_103a",
+            "cloud": fname, "points": n, "bbox": bb, "wsize": GPUBAR_W, "overlap": GPUBAR_O,
+            "leaf_max_number": args.gpu_bar_leaf, "rc": r.returncode, "wall_s": round(wall, 2), **vals,
+            "mpts_s": round(n / (vals["total_ms"] / 1e3) / 1e6, 2) if "total_ms" in vals else None,
+            "timing": "the program's own host-clock means over its 5 runs: tree build, stage 1 (kernel + "
+                      "synchronise), stage 2 on the host; no stage 3"}
+    if r.returncode:
+        line["stderr"] = r.stderr[-2000:]
+    print(json.dumps(line), flush=True)
+
+
+def run_gpubar_ours(args, F, torch, local) -> None:
+    """Our path on the cloud the reference's GPU program is timed on (same
+    exact doubles, its header box, Wsize 10, overlap 0.8), device-resident:
+    build + stages 1-3, CUDA events, mean of 5 runs after warm-up."""
+    fname, n, (x0, y0, x1, y1) = GPUBAR_CLOUDS[args.gpu_bar]
+    X, Y, Z = gpubar_points(args.gpu_bar, F.synth_config, F.synth_cloud)
+    xyz = np.empty((n, 3), dtype=np.float64)
+    xyz[:, 0] = X / 100.0
+    xyz[:, 1] = Y / 100.0
+    xyz[:, 2] = Z / 1000.0
+    del X, Y, Z
+    ctx = F.Context(local)
+    bb = F.Bbox(x0, y0, x1, y1)
+    cloud = ctx.cloud(xyz, bb)
+    stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
+    res = {}
+    for leaf in (args.gpu_bar_leaf, 256):
+        cfg = F.run_cfg(GPUBAR_W, GPUBAR_O, GPUBAR_B, leaf)
+        info = F.RunInfo()
+        for _ in range(3):
+            seeds = ctx.run(cloud, cfg, info)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(5):
+            seeds = ctx.run(cloud, cfg, info)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        res[f"leaf_{leaf}"] = {"ms": round(ms, 3), "mpts_s": round(n / (ms / 1e3) / 1e6, 1),
+                               "llps": int(info.n_llp), "seeds": int(len(seeds))}
+    cloud.close()
+    ctx.close()
+    print(json.dumps({"gpu_bar": "ours", "cloud": fname, "points": n, "wsize": GPUBAR_W, "overlap": GPUBAR_O,
+                      "bsize": GPUBAR_B, **res,
+                      "timing": "CUDA events on the context's stream, mean of 5 owm_run calls after 3 warm-up "
+                                "calls: tree build + stages 1-3, seeds copied out"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -310,8 +445,17 @@ def main():
     ap.add_argument("--ingest-n", type=int, default=20_000_000, help="points of the ingest leg's text")
     ap.add_argument("--only", choices=["batched", "served", "ingest"], default=None,
                     help="run that leg alone and print its JSON (profiling and tuning runs)")
+    ap.add_argument("--gpu-bar", choices=sorted(GPUBAR_CLOUDS), default=None,
+                    help="time the reference's GPU program (with --impl reference) or our path (without) on the "
+                         "named cloud in the reference's own text format")
+    ap.add_argument("--gpu-bar-leaf", type=int, default=16, help="leaf size (maxNumber) of the GPU bar")
     args = ap.parse_args()
     ws, rank, local = dist_setup(args)
+    if args.gpu_bar and args.impl == "reference":
+        if rank == 0:
+            run_gpubar_reference(args)
+        barrier(ws)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
         barrier(ws)
@@ -323,6 +467,11 @@ def main():
     from fastowm_gb300 import RunInfo
 
     torch.cuda.set_device(local)
+    if args.gpu_bar:
+        if rank == 0:
+            run_gpubar_ours(args, F, torch, local)
+        barrier(ws)
+        return
     if args.only:
         ctx = F.Context(local)
         leg = {"batched": lambda: run_batched(F, torch, ctx, args, local, ws),
