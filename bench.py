@@ -442,6 +442,8 @@ def main():
                     help="leaf size (maxNumber) of the main workload; 0 = tuned by fastowm_gb300.autotune, "
                          "-1 = the workload's configured value")
     ap.add_argument("--no-ingest", action="store_true")
+    ap.add_argument("--stage1-walk", action="store_true",
+                    help="stage 1 by the per-window tree walk instead of window classes (profiling runs)")
     ap.add_argument("--ingest-n", type=int, default=20_000_000, help="points of the ingest leg's text")
     ap.add_argument("--only", choices=["batched", "served", "ingest"], default=None,
                     help="run that leg alone and print its JSON (profiling and tuning runs)")
@@ -490,7 +492,7 @@ def main():
     xyz, bb = F.synth_cloud(spec, seed, out=xyz)
     ctx = F.Context(local)
     cloud = ctx.cloud(xyz, bb)
-    cfg = F.run_cfg(W, Ov, B, mn)
+    cfg = F.run_cfg(W, Ov, B, mn, stage1_walk=args.stage1_walk)
     p = F.params(bb, spec.n, W, Ov, B)
     stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
     info = RunInfo()
@@ -503,9 +505,13 @@ def main():
     elif args.leaf == 0:
         from fastowm_gb300 import autotune
 
-        leaf_tuning = autotune.tune_leaf_single(ctx, cloud, lambda L: F.run_cfg(W, Ov, B, L))
+        leaf_tuning = autotune.tune_leaf_single(ctx, cloud, lambda L: F.run_cfg(W, Ov, B, L, stage1_walk=args.stage1_walk))
         mn = leaf_tuning["leaf"]
-    cfg = F.run_cfg(W, Ov, B, mn)
+    cfg = F.run_cfg(W, Ov, B, mn, stage1_walk=args.stage1_walk)
+    # launch shapes (gather block, cell-walk warps): exact for every choice
+    from fastowm_gb300 import autotune
+
+    shape_tuning = autotune.tune_shapes_single(ctx, cloud, cfg, walk=args.stage1_walk) if args.leaf == 0 else None
     for _ in range(args.warmup):
         seeds = ctx.run(cloud, cfg, info)
     tree_leaves = (spec.n + mn - 1) // mn
@@ -628,6 +634,7 @@ def main():
                 "config": workload_config(args.config, spec, W, Ov, B, p.ncells, p.ngrid),
                 "path": "plain GPU path, one cloud per owm_run (device-resident input)",
                 "leaf_max_number": mn, "leaf_tuning_ms": leaf_tuning["ms"] if leaf_tuning else None,
+                "launch_shapes": shape_tuning,
                 "seeds": int(len(seeds)), "l2": "inputs (2.4 GB at 100M points) larger than L2; no flush",
                 "parallelism": f"replicas x{ws}",
                 "phases_ms": {"tree": round(phase[0] / args.steps, 4), "stage1": round(phase[1] / args.steps, 4),
@@ -658,7 +665,7 @@ def summary(line: dict) -> dict:
            "cpu_baseline": (line.get("cpu_baseline") or {}).get("value")}
     if b:
         out["batched"] = {k: b.get(k) for k in ("batched_mpts", "per_tile_mpts", "speedup", "per_tile_p50_ms",
-                                                "per_tile_p99_ms", "seeds_equal")}
+                                                "per_tile_p99_ms", "seeds_equal", "leaf_classes", "launch_shapes")}
     if sv:
         out["served"] = {"saturation_mpts": sv.get("saturation_mpts"), "plain_per_tile_mpts": sv.get("plain_per_tile_mpts"),
                          "saturation_vs_plain": sv.get("saturation_vs_plain"),
@@ -712,6 +719,29 @@ def run_batched(F, torch, ctx, args, local, ws):
         if rc:
             raise F.OwmError(rc, "batch_run")
 
+    # launch shapes of the batch's kernels (one set per launch): coordinate
+    # search on the whole batch, seeds checked against the first candidate
+    saved_shapes = ctx.tuning()
+    run_once()
+    ref_out = out.copy()
+    shape_ms = {}
+    for name, values in (("gather_block", autotune.GATHER_BLOCKS), ("cell_warps", autotune.CELL_WARPS)):
+        best, best_ms = None, float("inf")
+        for v in values:
+            ctx.set_tuning(**{name: v})
+            run_once()
+            if not np.array_equal(out, ref_out):
+                raise RuntimeError(f"batched {name}={v}: seeds differ")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                run_once()
+            ms = 1e3 * (time.perf_counter() - t0) / 3
+            shape_ms[f"{name}={v}"] = round(ms, 3)
+            if ms < best_ms:
+                best, best_ms = v, ms
+        ctx.set_tuning(**{name: best})
+    batch_shapes = ctx.tuning()
     for _ in range(2):
         run_once()
     torch.cuda.synchronize()
@@ -757,6 +787,7 @@ def run_batched(F, torch, ctx, args, local, ws):
     for c in clouds:
         c.close()
     batch.close()
+    ctx.set_tuning(**saved_shapes)
     del dev
     return {"workload": f"config 4: {len(info)} tiles, {total} FP64 points, counts log-uniform [50k, 2M], "
                         f"W 8-16, overlap 0.8, B 20",
@@ -766,6 +797,7 @@ def run_batched(F, torch, ctx, args, local, ws):
             "per_tile_p99_ms": round(float(np.percentile(lat, 99)), 3),
             "seeds_equal": bool(equal), "seeds_compared": "every tile's seed array, batched vs its own plain run",
             "leaf_classes": tuned["leaves"], "class_bounds": tuned["bounds"], "graphs": True,
+            "launch_shapes": batch_shapes, "launch_shape_ms": shape_ms,
             "kernels": {k: {"ms": round(v[0], 4), "share": round(v[0] / ktot, 4), "launches": int(v[1])}
                         for k, v in sorted(kb.items(), key=lambda kv: -kv[1][0])},
             "timing": "host clock around synchronous calls, device-resident inputs; kernels: one extra "

@@ -26,7 +26,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (OWM_EAGAIN, OWM_ECUDA, OWM_OK, OWM_TREE_MAX_NUMBER, OWM_TREE_MIN_RADIUS, Bbox, Params, RunCfg, RunInfo,  # noqa: F401
-                   ServerCfg, ServerStats, SynthSpec, TileDesc, TreeCfg, TreeInfo)
+                   ServerCfg, ServerStats, SynthSpec, TileDesc, TreeCfg, TreeInfo, Tuning)
 
 __all__ = ["OwmError", "round2d", "params", "bbox_of", "read_xyz", "write_xyz_ids", "check_results",
            "synth_config", "synth_cloud", "Context", "Batch", "Server", "TreeCfg", "RunCfg", "lib"]
@@ -236,6 +236,17 @@ class Context:
         st = C.c_int32()
         _check(lib().owm_ctx_device_status(self.handle, C.byref(st)), "device_status")
         return st.value
+
+    def set_tuning(self, walk_patch_x: int = 0, cell_warps: int = 0, gather_block: int = 0) -> None:
+        """Launch shapes of this context's kernels (0 keeps a field); the
+        results do not depend on them."""
+        t = Tuning(walk_patch_x, cell_warps, gather_block, 0)
+        _check(lib().owm_ctx_set_tuning(self.handle, C.byref(t)), "set_tuning")
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        _check(lib().owm_ctx_get_tuning(self.handle, C.byref(t)), "get_tuning")
+        return t.asdict()
 
     def set_walk_limit(self, limit: int) -> None:
         """Step limit of the bounded tree walks (0 = their structural bounds)."""

@@ -43,6 +43,14 @@ class TreeCfg(C.Structure):
     _fields_ = [("policy", i32), ("max_number", i32), ("min_radius", f32), ("level", i32)]
 
 
+class Tuning(C.Structure):
+    """owm_tuning: launch shapes of a context's kernels (0 = keep the default)."""
+    _fields_ = [("walk_patch_x", i32), ("cell_warps", i32), ("gather_block", i32), ("_pad", i32)]
+
+    def asdict(self):
+        return {"walk_patch_x": self.walk_patch_x, "cell_warps": self.cell_warps, "gather_block": self.gather_block}
+
+
 class TreeInfo(C.Structure):
     _fields_ = [("npoints", i64), ("nleaves", i64), ("nnodes", i64), ("root_count", i64),
                 ("root_min_id", i64), ("max_leaf", i32), ("key_bits", i32)]
@@ -91,6 +99,8 @@ SIGNATURES = {
     "owm_ctx_device_status": (C.c_int, [vp, P(i32)]),
     "owm_ctx_set_profiling": (C.c_int, [vp, C.c_int]),
     "owm_ctx_set_walk_limit": (C.c_int, [vp, i32]),
+    "owm_ctx_set_tuning": (C.c_int, [vp, P(Tuning)]),
+    "owm_ctx_get_tuning": (C.c_int, [vp, P(Tuning)]),
     "owm_ctx_kernel_times": (C.c_int, [vp, i32, vp, P(f64), P(i64), P(i32)]),
     "owm_cloud_create": (C.c_int, [vp, P(f64), i64, P(Bbox), P(vp)]),
     "owm_cloud_destroy": (C.c_int, [vp]),

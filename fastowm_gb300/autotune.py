@@ -97,3 +97,108 @@ def tune_leaf_single(ctx, cloud, make_cfg, leaves=(32, 64, 128, 256), reps: int 
         timings[leaf] = round(float(np.median(ts)), 3)
     best = min(timings, key=timings.get)
     return {"leaf": best, "ms": timings}
+
+
+# Launch-shape candidates (owm_ctx_set_tuning); results never depend on them.
+GATHER_BLOCKS = (128, 256, 512)
+CELL_WARPS = (2, 4, 8)
+WALK_PATCHES = (2, 4, 8, 16)
+
+
+def _timed_median(fn, stream, reps: int) -> float:
+    import torch
+
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def tune_shapes_single(ctx, cloud, cfg, walk: bool = False, reps: int = 3) -> dict:
+    """Launch shapes for one cloud and run config: coordinate search over the
+    gather's block size, the stage-3 cell walk's warps per block and (for the
+    tree-walk stage 1) the walk's window patch, each timed by owm_run on the
+    device-resident cloud, every candidate's seeds checked against the first.
+    Leaves the best shapes set on ctx; returns {"tuning": {...}, "ms": {...}}."""
+    import torch
+
+    import fastowm_gb300 as F
+
+    stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
+    ref = ctx.run(cloud, cfg)
+    timings = {}
+    knobs = [("gather_block", GATHER_BLOCKS), ("cell_warps", CELL_WARPS)]
+    if walk:
+        knobs.append(("walk_patch_x", WALK_PATCHES))
+    for name, values in knobs:
+        best, best_ms = None, float("inf")
+        for v in values:
+            ctx.set_tuning(**{name: v})
+            seeds = ctx.run(cloud, cfg)  # warm-up, and the exactness check
+            if not np.array_equal(seeds, ref):
+                raise RuntimeError(f"{name}={v}: seeds differ")
+            ms = _timed_median(lambda: ctx.run(cloud, cfg), stream, reps)
+            timings[f"{name}={v}"] = round(ms, 4)
+            if ms < best_ms:
+                best, best_ms = v, ms
+        ctx.set_tuning(**{name: best})
+    return {"tuning": ctx.tuning(), "ms": timings}
+
+
+def tune_shapes_classes(ctx, bounds=DEFAULT_BOUNDS, tiles_per_class: int = 8, reps: int = 3, walk: bool = True,
+                        config: int = 4) -> dict:
+    """Launch shapes per tile size class: for each point-count band a sample
+    of tiles (config 4 generator) runs one tile per owm_run, and a coordinate
+    search picks the gather block, the cell-walk warps and -- for the
+    tree-walk stage 1 -- the walk's window patch that minimise the band's
+    total device time; every candidate's seeds are checked against the
+    first's.  Returns {"bounds": [...], "classes": [{"tuning", "ms"}, ...]};
+    ctx is left with its shapes from before."""
+    import torch
+
+    import fastowm_gb300 as F
+
+    stream = torch.cuda.ExternalStream(F.lib().owm_ctx_stream(ctx.handle))
+    saved = ctx.tuning()
+    out, lo = [], 0
+    for hi in bounds:
+        tiles = _class_tiles(F, lo, min(hi, 5_000_000), tiles_per_class, config=config)
+        lo = hi
+        if not tiles:
+            out.append(None)
+            continue
+        clouds = [(ctx.cloud(xyz, bb), cfg) for xyz, bb, cfg in tiles]
+        knobs = [("gather_block", GATHER_BLOCKS, False), ("cell_warps", CELL_WARPS, False)]
+        if walk:
+            knobs.append(("walk_patch_x", WALK_PATCHES, True))
+        timings = {}
+        for name, values, use_walk in knobs:
+            runs = [(cl, F.run_cfg(cfg.wsize, cfg.overlap, cfg.bsize, cfg.tree.max_number, stage1_walk=use_walk))
+                    for cl, cfg in clouds]
+            refs = [ctx.run(cl, c2) for cl, c2 in runs]
+            best, best_ms = None, float("inf")
+            for v in values:
+                ctx.set_tuning(**{name: v})
+                for (cl, c2), ref in zip(runs, refs):
+                    if not np.array_equal(ctx.run(cl, c2), ref):
+                        raise RuntimeError(f"{name}={v}: seeds differ")
+
+                def all_tiles():
+                    for cl, c2 in runs:
+                        ctx.run(cl, c2)
+
+                ms = _timed_median(all_tiles, stream, reps)
+                timings[f"{name}={v}"] = round(ms, 4)
+                if ms < best_ms:
+                    best, best_ms = v, ms
+            ctx.set_tuning(**{name: best})
+        out.append({"tuning": ctx.tuning(), "ms": timings})
+        for cl, _ in clouds:
+            cl.close()
+        ctx.set_tuning(**saved)
+    return {"bounds": list(bounds), "classes": out}

@@ -276,6 +276,32 @@ int owm_ctx_device_status(owm_ctx* c, int32_t* status) {
   return OWM_OK;
 }
 
+int owm_ctx_set_tuning(owm_ctx* c, const owm_tuning* t) {
+  if (!c || !t) return OWM_EINVAL;
+  owm_tuning u = c->tuning;
+  if (t->walk_patch_x) {
+    const int32_t p = t->walk_patch_x;
+    if (p < 1 || p > 32 || (p & (p - 1))) return OWM_EINVAL;
+    u.walk_patch_x = p;
+  }
+  if (t->cell_warps) {
+    if (t->cell_warps != 2 && t->cell_warps != 4 && t->cell_warps != 8) return OWM_EINVAL;
+    u.cell_warps = t->cell_warps;
+  }
+  if (t->gather_block) {
+    if (t->gather_block != 128 && t->gather_block != 256 && t->gather_block != 512) return OWM_EINVAL;
+    u.gather_block = t->gather_block;
+  }
+  c->tuning = u;
+  return OWM_OK;
+}
+
+int owm_ctx_get_tuning(owm_ctx* c, owm_tuning* t) {
+  if (!c || !t) return OWM_EINVAL;
+  *t = c->tuning;
+  return OWM_OK;
+}
+
 int owm_ctx_set_walk_limit(owm_ctx* c, int32_t limit) {
   if (!c || limit < 0) return OWM_EINVAL;
   c->walk_limit = limit;
@@ -529,6 +555,7 @@ int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm
   tr->d_xyz = static_cast<const double*>(cl->mem.ptr);
   tr->bbox = cl->bbox;
   int rc = tree_alloc(&tr->t, &tr->mem, cl->n, *cfg, c->stream);
+  tr->t.gather_block = c->tuning.gather_block;
   if (!rc) rc = c->scratch.reserve(tree_scratch_bytes(cl->n), c->stream);
   if (!rc) rc = clear_status(c);
   if (!rc)
@@ -669,7 +696,7 @@ int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_
   }
   rc = clear_status(c);
   if (!rc)
-    rc = run_stage3(tr->t.view(c->walk_limit), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
+    rc = run_stage3(tr->t.view(c->walk_limit, c->tuning.cell_warps), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
                     c->d_job, c->d_small + kStatusSlot, c->stream, &c->launches);
   if (!rc) rc = check_input_status(c);
   if (rc) return rc;

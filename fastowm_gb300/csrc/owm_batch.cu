@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) k_b_morton_counts(const double* __restric
 
 // One warp per global leaf: gather its points into sorted order as keys and
 // reduce the leaf summary.
-__global__ void __launch_bounds__(256) k_b_gather_leaves(const double* __restrict__ xyz,
+__global__ void __launch_bounds__(512) k_b_gather_leaves(const double* __restrict__ xyz,
                                                          const uint32_t* __restrict__ perm,
                                                          const TileMeta* __restrict__ meta,
                                                          const int32_t* __restrict__ leaf_off, int ntiles,
@@ -381,12 +381,13 @@ __global__ void k_b_refit(Node* __restrict__ nodes, const int32_t* __restrict__ 
 // Stage 3 of all tiles: one warp per grid cell of any tile (cell_off gives
 // each tile's first cell), answered by the tile's stage-3 job; marked cells
 // are skipped at once.
-__global__ void __launch_bounds__(kS3Warps * 32) k_b_query_cells(const QueryJob* __restrict__ jobs,
-                                                                   const int64_t* __restrict__ cell_off, int ntiles,
-                                                                   int64_t total_cells) {
-  __shared__ int32_t stack_all[kS3Warps][kS3Stack];
+template <int kW>
+__global__ void __launch_bounds__(kW * 32) k_b_query_cells(const QueryJob* __restrict__ jobs,
+                                                             const int64_t* __restrict__ cell_off, int ntiles,
+                                                             int64_t total_cells) {
+  extern __shared__ int32_t stack_all[];  // [kW][kS3Stack]
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int64_t c = (int64_t)blockIdx.x * kS3Warps + wib;
+  const int64_t c = (int64_t)blockIdx.x * kW + wib;
   if (c >= total_cells) return;  // warp-uniform
   const int t = tile_of(cell_off, ntiles, c);
   const QueryJob& J = jobs[t];
@@ -395,8 +396,24 @@ __global__ void __launch_bounds__(kS3Warps * 32) k_b_query_cells(const QueryJob*
     if (lane == 0) J.out[k] = kNone;
     return;
   }
-  const uint32_t r = cell_min_warp(J.tree, J.ex[k % J.ncols], J.ey[k / J.ncols], stack_all[wib], J.status, lane);
+  const uint32_t r =
+      cell_min_warp(J.tree, J.ex[k % J.ncols], J.ey[k / J.ncols], stack_all + wib * kS3Stack, J.status, lane);
   if (lane == 0) J.out[k] = r;
+}
+
+template <int kW>
+cudaError_t launch_b_query_cells(const QueryJob* jobs, const int64_t* cell_off, int ntiles, int64_t total_cells,
+                                 cudaStream_t s) {
+  static bool configured = false;  // per template instance
+  const size_t smem = (size_t)kW * kS3Stack * sizeof(int32_t);
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_b_query_cells<kW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  OWM_LAUNCH("k_query_s3_batch", s, (k_b_query_cells<kW><<<(unsigned)((total_cells + kW - 1) / kW), kW * 32, smem, s>>>(
+      jobs, cell_off, ntiles, total_cells)));
+  return cudaGetLastError();
 }
 
 __device__ __forceinline__ Edge bedge(double lo, double hi, double o) {
@@ -1038,11 +1055,12 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     a.nrows = m.nrows;
     a.thr = m.thr;
     a.cell_order = 0;
+    a.patch_lx = patch_log2(tuning.walk_patch_x);
     a.skip = nullptr;
     a.out = win + m.win_off;
     a.status = words;
     a.warp_begin = w1;
-    w1 += job_warps(m.ncols, m.nrows);
+    w1 += job_warps(m.ncols, m.nrows, a.patch_lx);
     QueryJob& b = j3[t];
     b = a;
     b.ex = E_cx + m.cx_off;
@@ -1054,7 +1072,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     b.skip = mark + m.cell_off;
     b.out = cmin + m.cell_off;
     b.warp_begin = w3;
-    w3 += job_warps(b.ncols, b.nrows);
+    w3 += job_warps(b.ncols, b.nrows, b.patch_lx);
   }
   (void)base_view;
   QueryJob* d_j1 = (QueryJob*)at(P.o_jobs1);
@@ -1106,6 +1124,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     // the class regions' layout (table sizes follow each tile's bbox, not only its meta)
     if (P.classes) sig.append(reinterpret_cast<const char*>(P.cls.data()), P.cls.size() * sizeof(ClassArgs));
     sig.push_back(P.classes ? 'c' : 'w');
+    sig.append(reinterpret_cast<const char*>(&tuning), sizeof(tuning));  // launch shapes
   }
   if (use_graphs && graph && sig == graph_sig) {
     OWM_CUDA_TRY(cudaGraphLaunch(graph, stream));
@@ -1196,8 +1215,9 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       if (two && cudaStreamWaitEvent(s, ev_cls, 0) != cudaSuccess) { rc2 = OWM_ECUDA; break; }
       {
         // one warp per leaf: resident warps then work on neighbouring leaves
-        int64_t blocks = std::min<int64_t>((P.nleaves * 32 + 255) / 256, (int64_t)152 * 1024);
-        OWM_LAUNCH("k_b_gather_leaves", s, k_b_gather_leaves<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(
+        const int gb = tuning.gather_block;
+        int64_t blocks = std::min<int64_t>((P.nleaves * 32 + gb - 1) / gb, (int64_t)152 * 1024 * 256 / gb);
+        OWM_LAUNCH("k_b_gather_leaves", s, k_b_gather_leaves<<<(unsigned)std::max<int64_t>(blocks, 1), gb, 0, s>>>(
             xyz, perm, d_meta, d_leafoff, ntiles, P.nleaves, xk, yk, zk, pid, nodes, words, d_cls));
         count_launch(L);
       }
@@ -1287,9 +1307,11 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
         forked = false;
       }
       if (NC > 0) {
-        if ((NC + kS3Warps - 1) / kS3Warps >= 0x7FFFFFFFll) { rc2 = OWM_ERANGE; break; }
-        OWM_LAUNCH("k_query_s3_batch", s, k_b_query_cells<<<(unsigned)((NC + kS3Warps - 1) / kS3Warps), kS3Warps * 32, 0, s>>>(
-            d_j3, d_celloff, ntiles, NC));
+        if ((NC + 1) / 2 >= 0x7FFFFFFFll) { rc2 = OWM_ERANGE; break; }
+        const cudaError_t e3 = tuning.cell_warps == 2   ? launch_b_query_cells<2>(d_j3, d_celloff, ntiles, NC, s)
+                               : tuning.cell_warps == 8 ? launch_b_query_cells<8>(d_j3, d_celloff, ntiles, NC, s)
+                                                        : launch_b_query_cells<4>(d_j3, d_celloff, ntiles, NC, s);
+        if (e3 != cudaSuccess) { rc2 = OWM_ECUDA; break; }
         count_launch(L);
         uint32_t* cf = (uint32_t*)at(P.o_cf);
         uint32_t* cp = (uint32_t*)at(P.o_cp);
@@ -1429,6 +1451,7 @@ int owm_batch_run(owm_batch* b, const owm_tile_desc* tiles, int32_t ntiles, int6
                   int64_t* offsets, owm_run_info* info) {
   if (!b || !tiles || ntiles <= 0 || !offsets || (!seeds && cap > 0)) return OWM_EINVAL;
   ProfScope prof_scope(b->ctx->active_prof());
+  b->run.tuning = b->ctx->tuning;
   int64_t l0 = b->run.launches;
   int rc = b->run.launch(tiles, ntiles);
   if (rc) return rc;

@@ -58,6 +58,7 @@ struct BatchRun {
   int32_t nclass = 0;
   int64_t class_bound[8] = {};
   int32_t class_leaf[8] = {};
+  owm_tuning tuning = {4, 4, 256, 0};  // launch shapes (a batch takes its context's)
   // results of the last launch
   std::vector<TileHost> tiles;
   int64_t total_out = 0;

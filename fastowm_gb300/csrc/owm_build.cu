@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
 // stage-1 window classes (the point is already in registers; this kernel is
 // DRAM-bound, so the classification costs next to nothing here).
 template <int L, bool kCls>
-__global__ void __launch_bounds__(256) k_gather_leaves(const double* __restrict__ xyz, const uint32_t* __restrict__ perm,
+__global__ void __launch_bounds__(512) k_gather_leaves(const double* __restrict__ xyz, const uint32_t* __restrict__ perm,
                                                        int64_t n, int32_t nleaves, double ox, double oy,
                                                        int64_t* __restrict__ xk, int64_t* __restrict__ yk,
                                                        int64_t* __restrict__ zk, uint32_t* __restrict__ pid,
@@ -384,17 +384,18 @@ void launch_gather_leaves(const double* xyz, const uint32_t* perm, int64_t n, in
   constexpr int kUnit = L < 32 ? 32 : L;
   int64_t nunits = (n + kUnit - 1) / kUnit;
   int64_t warps = nunits;
-  int64_t blocks = (warps * 32 + 255) / 256;
+  const int gb = t->gather_block;  // 128, 256 or 512 threads
+  int64_t blocks = (warps * 32 + gb - 1) / gb;
   // one warp per unit (no grid-stride reuse): the resident warps then work on
   // neighbouring units, which measured 12-15% faster than 16 blocks per SM
-  if (blocks > (int64_t)152 * 1024) blocks = (int64_t)152 * 1024;
+  if (blocks > (int64_t)152 * 1024 * 256 / gb) blocks = (int64_t)152 * 1024 * 256 / gb;
   if (cls) {
-    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, true><<<(unsigned)blocks, 256, 0, s>>>(
+    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, true><<<(unsigned)blocks, gb, 0, s>>>(
         xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid, t->nodes + (nl - 1), status, *cls));
   } else {
     ClassArgs none;
     std::memset(&none, 0, sizeof(none));
-    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, false><<<(unsigned)blocks, 256, 0, s>>>(
+    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, false><<<(unsigned)blocks, gb, 0, s>>>(
         xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid, t->nodes + (nl - 1), status, none));
   }
 }

@@ -16,11 +16,13 @@ struct TreeStore {
   int64_t point_cap = 0, node_cap = 0;
   int64_t n = 0;
   int32_t nleaves = 0, root = 0, key_bits = 0, max_leaf = 0;
+  int32_t gather_block = 256;  // threads per block of the build's gather (128, 256 or 512)
   double ox = 0, oy = 0;
 
-  TreeView view(int32_t walk_limit = 0) const {
+  TreeView view(int32_t walk_limit = 0, int32_t cell_warps = 4) const {
     TreeView v;
     v.walk_limit = walk_limit;
+    v.cell_warps = cell_warps;
     v.xk = xk;
     v.yk = yk;
     v.zk = zk;

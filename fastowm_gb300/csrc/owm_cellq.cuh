@@ -23,8 +23,7 @@ namespace owm {
 // most 32 entries behind per level); on overflow, or past the round bound, the
 // walk sets kStatusWalkBound and stops.
 
-constexpr int kS3Warps = 4;      // warps (cells) per block
-constexpr int kS3Stack = 2304;   // node stack entries per warp
+constexpr int kS3Stack = 2304;   // node stack entries per warp (the kernels run 2, 4 or 8 warps per block)
 
 __device__ __forceinline__ int64_t cq_shfl64(int64_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 

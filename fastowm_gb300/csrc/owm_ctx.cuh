@@ -98,6 +98,8 @@ struct owm_ctx {
   int64_t next_ticket = 1;
   // > 0: step limit of the bounded tree walks (owm_ctx_set_walk_limit)
   int32_t walk_limit = 0;
+  // launch shapes (owm_ctx_set_tuning); always complete (no zero fields)
+  owm_tuning tuning = {4, 4, 256, 0};
 };
 
 namespace owm {

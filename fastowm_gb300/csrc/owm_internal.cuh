@@ -89,6 +89,7 @@ struct TreeView {
   // cell-walk rounds) in place of their structural bounds; lets a test make
   // a walk give up on a well-formed tree (owm_ctx_set_walk_limit)
   int32_t walk_limit = 0;
+  int32_t cell_warps = 4;  // stage-3 cell walk: cells (warps) per block, 2, 4 or 8
 };
 
 // ---------------------------------------------------------------------------

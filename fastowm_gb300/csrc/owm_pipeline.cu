@@ -99,6 +99,7 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   j.nrows = (int32_t)p.nrows;
   j.thr = p.min_num_points;
   j.cell_order = 0;
+  j.patch_lx = patch_log2(c->tuning.walk_patch_x);
   j.skip = nullptr;
   j.out = d_win;
   j.status = c->d_small + kStatusSlot;
@@ -174,6 +175,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   }
   bool fused = false;
   c->stage12_side = false;
+  c->tree.gather_block = c->tuning.gather_block;
   if (!rc)
     rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
                     &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr,
@@ -231,8 +233,8 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
     OWM_CUDA_TRY(cudaEventRecord(c->ev[3], s));
   }
   rc = c->stage12_side
-           ? run_stage3_query(c->tree.view(c->walk_limit), p, s3, d_ns3, s3scratch, s3cap, c->d_small + kStatusSlot, s, &c->launches)
-           : run_stage3(c->tree.view(c->walk_limit), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
+           ? run_stage3_query(c->tree.view(c->walk_limit, c->tuning.cell_warps), p, s3, d_ns3, s3scratch, s3cap, c->d_small + kStatusSlot, s, &c->launches)
+           : run_stage3(c->tree.view(c->walk_limit, c->tuning.cell_warps), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
                         c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));

@@ -103,9 +103,10 @@ __device__ __forceinline__ void query_warp(const QueryJob* __restrict__ jobs, in
   const QueryJob& J = jobs[njobs > 1 ? find_job(jobs, njobs, warp) : 0];
   const TreeView T = J.tree;
   const int64_t lw = warp - J.warp_begin;
-  const int32_t gx = (J.ncols + 3) >> 2;
-  const int32_t ii = (int32_t)(lw % gx) * 4 + (lane & 3);
-  const int32_t jj = (int32_t)(lw / gx) * 8 + (lane >> 2);
+  const int32_t lx = J.patch_lx;  // patch of 2^lx columns x 2^(5 - lx) rows of windows
+  const int32_t gx = (J.ncols + (1 << lx) - 1) >> lx;
+  const int32_t ii = (int32_t)(lw % gx) * (1 << lx) + (lane & ((1 << lx) - 1));
+  const int32_t jj = (int32_t)(lw / gx) * (32 >> lx) + (lane >> lx);
   bool active = ii < J.ncols && jj < J.nrows;
   int64_t oidx = 0;
   Edge ex, ey;
@@ -278,20 +279,36 @@ __global__ void __launch_bounds__(kQBlock) k_query_persistent(const QueryJob* __
 }
 
 // ---- stage 3: one warp per cell (owm_cellq.cuh) ---------------------------------
-__global__ void __launch_bounds__(kS3Warps * 32) k_query_cells(TreeView T, const Edge* __restrict__ exs,
-                                                                 const Edge* __restrict__ eys, int32_t ncols,
-                                                                 int64_t ncells, const uint8_t* __restrict__ skip,
-                                                                 uint32_t* __restrict__ out, uint32_t* status) {
-  __shared__ int32_t stack_all[kS3Warps][kS3Stack];
+template <int kW>
+__global__ void __launch_bounds__(kW * 32) k_query_cells(TreeView T, const Edge* __restrict__ exs,
+                                                           const Edge* __restrict__ eys, int32_t ncols,
+                                                           int64_t ncells, const uint8_t* __restrict__ skip,
+                                                           uint32_t* __restrict__ out, uint32_t* status) {
+  extern __shared__ int32_t stack_all[];  // [kW][kS3Stack]
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int64_t cell = (int64_t)blockIdx.x * kS3Warps + wib;
+  const int64_t cell = (int64_t)blockIdx.x * kW + wib;
   if (cell >= ncells) return;  // warp-uniform
   if (skip && skip[cell]) {
     if (lane == 0) out[cell] = kNone;
     return;
   }
-  const uint32_t r = cell_min_warp(T, exs[cell % ncols], eys[cell / ncols], stack_all[wib], status, lane);
+  const uint32_t r = cell_min_warp(T, exs[cell % ncols], eys[cell / ncols], stack_all + wib * kS3Stack, status, lane);
   if (lane == 0) out[cell] = r;
+}
+
+template <int kW>
+cudaError_t launch_query_cells(const TreeView& t, const Edge* ex, const Edge* ey, int32_t ncols, int64_t ng,
+                               const uint8_t* skip, uint32_t* out, uint32_t* status, cudaStream_t s) {
+  static bool configured = false;  // per template instance
+  const size_t smem = (size_t)kW * kS3Stack * sizeof(int32_t);
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_query_cells<kW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  OWM_LAUNCH("k_query_s3", s, (k_query_cells<kW><<<(unsigned)((ng + kW - 1) / kW), kW * 32, smem, s>>>(
+      t, ex, ey, ncols, ng, skip, out, status)));
+  return cudaGetLastError();
 }
 
 // ---- stage 2 -----------------------------------------------------------------
@@ -510,9 +527,10 @@ int compute_edges(const owm_params& p, double ox, double oy, bool cells, Edge* d
   return OWM_OK;
 }
 
-int64_t job_warps(int32_t ncols, int32_t nrows) {
+int64_t job_warps(int32_t ncols, int32_t nrows, int32_t patch_lx) {
   if (ncols <= 0 || nrows <= 0) return 0;
-  return (int64_t)((ncols + 3) / 4) * ((nrows + 7) / 8);
+  const int32_t px = 1 << patch_lx, py = 32 >> patch_lx;
+  return (int64_t)((ncols + px - 1) / px) * ((nrows + py - 1) / py);
 }
 
 int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches,
@@ -541,7 +559,7 @@ int run_query(const QueryJob& job, QueryJob* d_job_slot, cudaStream_t s, int64_t
   QueryJob j = job;
   j.warp_begin = 0;
   OWM_CUDA_TRY(cudaMemcpyAsync(d_job_slot, &j, sizeof(QueryJob), cudaMemcpyHostToDevice, s));
-  return launch_query(d_job_slot, 1, job_warps(j.ncols, j.nrows), s, launches, name);
+  return launch_query(d_job_slot, 1, job_warps(j.ncols, j.nrows, j.patch_lx), s, launches, name);
 }
 
 size_t stage2_scratch_bytes(int64_t n) {
@@ -759,10 +777,10 @@ int run_stage3_query(const TreeView& t, const owm_params& p, uint32_t* d_out, ui
   }
   if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
   const S3Layout L = stage3_layout(scratch, ng);
-  const int64_t cblocks = (ng + kS3Warps - 1) / kS3Warps;
-  if (cblocks >= 0x7FFFFFFFll) return OWM_ERANGE;
-  OWM_LAUNCH("k_query_s3", s, k_query_cells<<<(unsigned)cblocks, kS3Warps * 32, 0, s>>>(
-      t, L.ex, L.ey, (int32_t)p.ncols_grid, ng, L.mark, L.cellmin, status));
+  if ((ng + 1) / 2 >= 0x7FFFFFFFll) return OWM_ERANGE;
+  OWM_CUDA_TRY(t.cell_warps == 2   ? launch_query_cells<2>(t, L.ex, L.ey, (int32_t)p.ncols_grid, ng, L.mark, L.cellmin, status, s)
+               : t.cell_warps == 8 ? launch_query_cells<8>(t, L.ex, L.ey, (int32_t)p.ncols_grid, ng, L.mark, L.cellmin, status, s)
+                                   : launch_query_cells<4>(t, L.ex, L.ey, (int32_t)p.ncols_grid, ng, L.mark, L.cellmin, status, s));
   count_launch(launches);
   if (ng <= kCompactSmallMax) {
     OWM_LAUNCH("k_compact_small", s, k_compact_small<<<1, kCompactBlock, 0, s>>>(L.cellmin, ng, d_out, d_count));

@@ -15,6 +15,7 @@ struct QueryJob {
   int32_t ncols, nrows;
   uint32_t thr;         // minimum number of points strictly inside
   int32_t cell_order;   // 0: out[ii*nrows + jj] (stage 1); 1: out[jj*ncols + ii]
+  int32_t patch_lx;     // a warp takes 2^patch_lx x 2^(5 - patch_lx) boxes (columns x rows)
   const uint8_t* skip;  // optional [ncols*nrows] in out order: box not queried
   uint32_t* out;        // id of the (z,id)-min point, or kNone
   uint32_t* status;     // device status word: kStatusWalkBound set if a walk overran
@@ -30,14 +31,20 @@ constexpr uint32_t kStatusWalkBound = 2u;  // a tree walk exceeded its step boun
 int compute_edges(const owm_params& p, double ox, double oy, bool cells, Edge* d_ex, Edge* d_ey, cudaStream_t s,
                   int64_t* launches);
 
-// Number of warps a job needs (4 x 8 boxes per warp).
-int64_t job_warps(int32_t ncols, int32_t nrows);
+// Number of warps a job needs (2^patch_lx x 2^(5 - patch_lx) boxes per warp).
+int64_t job_warps(int32_t ncols, int32_t nrows, int32_t patch_lx);
+// log2 of a power-of-two walk patch width (1..32).
+inline int32_t patch_log2(int32_t patch_x) {
+  int32_t l = 0;
+  while ((1 << l) < patch_x && l < 5) ++l;
+  return l;
+}
 
 // Runs jobs[0..njobs) (device array) whose warp ranges tile [0, total_warps).
 // `name` labels the launch for the per-kernel profiler.
 int launch_query(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, cudaStream_t s, int64_t* launches,
                  const char* name);
-// Persistent variant: `blocks` resident blocks pull 4 x 8 patches from the
+// Persistent variant: `blocks` resident blocks pull window patches from the
 // device counter *d_next (reset here) -- load balance for uneven jobs.
 int launch_query_persistent(const QueryJob* d_jobs, int32_t njobs, int64_t total_warps, unsigned long long* d_next,
                             int blocks, cudaStream_t s, int64_t* launches, const char* name);

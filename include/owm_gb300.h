@@ -144,6 +144,23 @@ int owm_ctx_device_status(owm_ctx* ctx, int32_t* status);
  * reference, which has no bounded walk (it prints CUDA errors and goes on,
  * SYCL-CUDA-GPU/ordered/cuda/ordered_builder.inl:330-333). */
 int owm_ctx_set_walk_limit(owm_ctx* ctx, int32_t limit);
+/* Launch shapes of this context's kernels (owm_run, owm_tree_build,
+ * owm_stage1, owm_stage3 and the batches made from the context).  Every
+ * choice gives the same results; fastowm_gb300.autotune picks them by timing.
+ * A field of 0 keeps its default.  No counterpart in the reference, whose
+ * launch knobs are the leaf size (-s, owm_optim3.cpp:27) and the -DAUTOGRID
+ * grid (SYCL-CUDA-GPU/ordered/cuda/ordered_builder.inl:306-313). */
+typedef struct {
+  int32_t walk_patch_x; /* stage-1 tree walk: each warp takes patch_x x (32 / patch_x)
+                           windows; a power of two in 1..32 (default 4) */
+  int32_t cell_warps;   /* stage-3 cell walk: cells (one warp each) per block: 2, 4 or 8
+                           (default 4) */
+  int32_t gather_block; /* build gather (one warp per leaf unit): threads per block:
+                           128, 256 or 512 (default 256) */
+  int32_t _pad;
+} owm_tuning;
+int owm_ctx_set_tuning(owm_ctx* ctx, const owm_tuning* tuning);
+int owm_ctx_get_tuning(owm_ctx* ctx, owm_tuning* tuning);
 /* Per-kernel CUDA-event timing of this context's launches (1 = on). */
 int owm_ctx_set_profiling(owm_ctx* ctx, int on);
 /* Sums the recorded kernel times by kernel name since the last call (and
