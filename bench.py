@@ -607,9 +607,9 @@ def main():
                 "frac": round(achieved / peak, 4) if achieved else None,
                 "traffic": round(traffic) if traffic else None,
                 "traffic_gbs": round(traffic / (per_launch_ms / 1e3) / 1e9, 1) if traffic else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a full-size launch at "
-                                  "leaf 256 (profiles/), per point x points; the leaf records are under 1% "
-                                  "of it" if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 24 M-point "
+                                  "case of the same generator at leaf 256 (profiles/), per point x points"
+                                  if traffic else None,
                 "ms_per_launch": round(per_launch_ms, 4), "bytes_per_launch": bytes_alg}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
