@@ -120,3 +120,20 @@ def test_noalloc_rejects_ids_above_npoints(owm):
     big = np.full(64, 1 << 40, dtype=np.int64)
     rc, _, _ = _noalloc_rc(owm, torch, big, 0.5, 1 << 20)
     assert rc == -1
+
+
+def test_noalloc_at_its_limit(owm):
+    """The allocation-free stage 2 at its largest size (1,048,576 windows) and
+    just below it (n % 32 != 0), two calls in a row: ids up to 5,000,000 make
+    23-bit sort keys (digits of 8, 8 and 7 bits), so the last pass is the
+    ranked, TMA-staged keys-only pass at a size that takes its ragged path."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(7)
+    ctx = owm.Context(0)
+    for ncells in (1 << 20, (1 << 20) - 33):
+        w = rng.integers(0, 5_000_000, ncells)
+        w[rng.random(ncells) < 0.1] = -1
+        got = _noalloc(owm, torch, w, 0.8, 5_000_000)
+        np.testing.assert_array_equal(got, _llp_of(w, 0.8))
+        np.testing.assert_array_equal(got, ctx.stage2(w.copy(), 0.8))
+    ctx.close()
