@@ -780,8 +780,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
         const uint32_t sh = (d & 3u) * 8u;
         const uint32_t in_group = (cnt[(d >> 2) * kBlock + tid] >> sh) & 0xFFu;
         const uint32_t pos = S[d] + gg[d] + in_group + ((own[i >> 3] >> ((i & 7) * 4)) & 15u);
-        sk[pos] = k[i];
-        if (kHasVals) sv[pos] = v[i];
+        if (kHasVals)
+          reinterpret_cast<uint2*>(sk)[pos] = make_uint2(k[i], v[i]);  // key and value as one word
+        else
+          sk[pos] = k[i];
       }
     }
     __syncthreads();
@@ -790,10 +792,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
     {
       const int tn = (int)(n - tile_base < kTile ? n - tile_base : kTile);
       for (int j = tid; j < tn; j += kBlock) {
-        const uint32_t key = sk[j];
-        const uint32_t gp = adj[(key >> shift) & dmask] + (uint32_t)j;
-        kout[gp] = key;
-        if (kHasVals) vout[gp] = sv[j];
+        if (kHasVals) {
+          const uint2 kv = reinterpret_cast<const uint2*>(sk)[j];
+          const uint32_t gp = adj[(kv.x >> shift) & dmask] + (uint32_t)j;
+          kout[gp] = kv.x;
+          vout[gp] = kv.y;
+        } else {
+          const uint32_t key = sk[j];
+          kout[adj[(key >> shift) & dmask] + (uint32_t)j] = key;
+        }
       }
     }
     __syncthreads();  // stage stg is free again
