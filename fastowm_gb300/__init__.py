@@ -361,6 +361,29 @@ class Context:
         _check(rc, "run_host_wait")
         return out[: n.value].copy()
 
+    def run_submit(self, cloud: Cloud, cfg: RunCfg, out: np.ndarray | None = None) -> int:
+        """Queues owm_run on a device cloud asynchronously; returns a ticket for
+        run_wait.  The cloud and the output array are kept alive until the wait."""
+        p = params(cloud.bbox, cloud.n, cfg.wsize, cfg.overlap, cfg.bsize)
+        cap = p.ncells + max(p.ngrid, 0) + 1
+        if out is None or out.size < cap:
+            out = np.empty(cap, dtype=np.int64)
+        t = C.c_int64()
+        _check(lib().owm_run_submit(self.handle, cloud.handle, C.byref(cfg), _i64p(out), out.size, C.byref(t)),
+               "run_submit")
+        if not hasattr(self, "_pending"):
+            self._pending = {}
+        self._pending[t.value] = (cloud, out)
+        return t.value
+
+    def run_wait(self, ticket: int, info: RunInfo | None = None) -> np.ndarray:
+        n = C.c_int64()
+        inf = info if info is not None else RunInfo()
+        rc = lib().owm_run_wait(self.handle, ticket, C.byref(n), C.byref(inf))
+        _, out = self._pending.pop(ticket, (None, None)) if hasattr(self, "_pending") else (None, None)
+        _check(rc, "run_wait")
+        return out[: n.value].copy()
+
 
 class Batch(_Child):
     """Many tiles built and queried together (one launch per stage)."""

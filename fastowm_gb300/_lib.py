@@ -121,6 +121,8 @@ SIGNATURES = {
     "owm_run_host": (C.c_int, [vp, P(f64), i64, P(Bbox), P(RunCfg), P(i64), i64, P(i64), P(RunInfo)]),
     "owm_run_host_submit": (C.c_int, [vp, P(f64), i64, P(Bbox), P(RunCfg), P(i64), i64, P(i64)]),
     "owm_run_host_wait": (C.c_int, [vp, i64, P(i64), P(RunInfo)]),
+    "owm_run_submit": (C.c_int, [vp, vp, P(RunCfg), P(i64), i64, P(i64)]),
+    "owm_run_wait": (C.c_int, [vp, i64, P(i64), P(RunInfo)]),
     "owm_batch_create": (C.c_int, [vp, P(vp)]),
     "owm_batch_destroy": (C.c_int, [vp]),
     "owm_batch_run": (C.c_int, [vp, P(TileDesc), i32, P(i64), i64, P(i64), P(RunInfo)]),

@@ -742,48 +742,21 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   return run_pipeline(c, static_cast<const double*>(c->input.ptr), n, bb, *cfg, seeds, cap, n_seeds, info);
 }
 
-int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, const owm_run_cfg* cfg,
-                        int64_t* seeds, int64_t cap, int64_t* ticket) {
-  ProfScope prof_scope(c ? c->active_prof() : nullptr);
-  if (!c || !xyz || !cfg || !ticket || n <= 0 || n >= 0x7FFFFFFFLL || (!seeds && cap > 0)) return OWM_EINVAL;
-  OWM_CUDA_TRY(cudaSetDevice(c->device));
-  owm_ctx::AsyncSlot& a = c->aslot[c->next_ticket & 1];
-  if (a.ticket != 0) return OWM_EAGAIN;  // both runs in flight: wait for the older one first
-  owm_bbox bb;
-  if (bbox) {
-    bb = *bbox;
-  } else if (is_device_ptr(xyz)) {
-    int rc = device_bbox(c, xyz, n, &bb);
-    if (rc) return rc;
-  } else {
-    owm_bbox_of(xyz, n, &bb);
-  }
-  if (!c->copy_stream) OWM_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-  if (!a.ready) OWM_CUDA_TRY(cudaEventCreateWithFlags(&a.ready, cudaEventDisableTiming));
-  if (!a.done) OWM_CUDA_TRY(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
-  if (!a.h_words) OWM_CUDA_TRY(cudaMallocHost(&a.h_words, 32));
-  // This slot's previous run has been waited for, so nothing reads its input
-  // buffer any more.  Reserving on the copy stream orders a (re)allocation
-  // before the copy without making the copy wait for the other run's compute.
-  int rc = a.input.reserve((size_t)n * 24 + kXyzSlack, c->copy_stream);
-  if (rc) return rc;
-  OWM_CUDA_TRY(cudaMemcpyAsync(a.input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->copy_stream));
-  // From here on the copy may still be reading xyz: a failed submit waits for
-  // it before returning, so the caller may free xyz after any return.
-  auto fail = [&](int code) {
-    cudaStreamSynchronize(c->copy_stream);
-    cudaStreamSynchronize(c->stream);
-    return code;
-  };
-  cudaError_t e = cudaEventRecord(a.ready, c->copy_stream);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, a.ready, 0);
-  if (e != cudaSuccess) {
-    set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
-    return fail(OWM_ECUDA);
-  }
+}  // extern "C"
+
+namespace {
+
+// Queues the run of slot a on the context's stream (after whatever is queued
+// there: a copy-stream event for host input), then the device->host copy of
+// its status words and of the whole seed buffer into the slot's pinned
+// staging, and hands out the ticket.  On failure the caller's fail() waits
+// for everything queued so far.
+template <class Fail>
+int submit_slot(owm_ctx* c, owm_ctx::AsyncSlot& a, const double* d_xyz, int64_t n, const owm_bbox& bb,
+                const owm_run_cfg& cfg, int64_t* seeds, int64_t cap, int64_t* ticket, const char* fn, Fail fail) {
   int64_t* d_seeds = nullptr;
   int64_t room = 0;
-  rc = run_pipeline_enqueue(c, static_cast<const double*>(a.input.ptr), n, bb, *cfg, &a.p, &d_seeds, &room);
+  int rc = run_pipeline_enqueue(c, d_xyz, n, bb, cfg, &a.p, &d_seeds, &room);
   if (rc) return fail(rc);
   if (a.h_cap < room) {
     // growth only: the old staging may still be a copy target
@@ -797,11 +770,11 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
     }
     a.h_cap = room;
   }
-  e = cudaMemcpyAsync(a.h_words, c->d_small, 32, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaMemcpyAsync(a.h_words, c->d_small, 32, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(a.h_seeds, d_seeds, (size_t)room * 8, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaEventRecord(a.done, c->stream);
   if (e != cudaSuccess) {
-    set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
+    set_last_cuda_error(e, fn, __FILE__, __LINE__);
     return fail(OWM_ECUDA);
   }
   a.seeds = seeds;
@@ -810,6 +783,92 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
   a.ticket = c->next_ticket++;
   *ticket = a.ticket;
   return OWM_OK;
+}
+
+// The slot the next ticket uses, with its events and pinned status words
+// created; nullptr (and *rc) when both runs are still in flight or creation
+// failed.
+owm_ctx::AsyncSlot* next_slot(owm_ctx* c, int* rc) {
+  owm_ctx::AsyncSlot& a = c->aslot[c->next_ticket & 1];
+  *rc = OWM_OK;
+  if (a.ticket != 0) {
+    *rc = OWM_EAGAIN;  // both runs in flight: wait for the older one first
+    return nullptr;
+  }
+  cudaError_t e = cudaSuccess;
+  if (!a.ready) e = cudaEventCreateWithFlags(&a.ready, cudaEventDisableTiming);
+  if (e == cudaSuccess && !a.done) e = cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming);
+  if (e == cudaSuccess && !a.h_words) e = cudaMallocHost(&a.h_words, 32);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "owm_run_submit", __FILE__, __LINE__);
+    *rc = OWM_ECUDA;
+    return nullptr;
+  }
+  return &a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int owm_run_submit(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int64_t* seeds, int64_t cap,
+                   int64_t* ticket) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
+  if (!c || !cl || !cfg || !ticket || (!seeds && cap > 0)) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  int rc = OWM_OK;
+  owm_ctx::AsyncSlot* a = next_slot(c, &rc);
+  if (!a) return rc;
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(c->side_stream);
+    cudaStreamSynchronize(c->stream);
+    return code;
+  };
+  return submit_slot(c, *a, static_cast<const double*>(cl->mem.ptr), cl->n, cl->bbox, *cfg, seeds, cap, ticket,
+                     "owm_run_submit", fail);
+}
+
+int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, const owm_run_cfg* cfg,
+                        int64_t* seeds, int64_t cap, int64_t* ticket) {
+  ProfScope prof_scope(c ? c->active_prof() : nullptr);
+  if (!c || !xyz || !cfg || !ticket || n <= 0 || n >= 0x7FFFFFFFLL || (!seeds && cap > 0)) return OWM_EINVAL;
+  OWM_CUDA_TRY(cudaSetDevice(c->device));
+  int rc = OWM_OK;
+  owm_ctx::AsyncSlot* ap = next_slot(c, &rc);
+  if (!ap) return rc;
+  owm_ctx::AsyncSlot& a = *ap;
+  owm_bbox bb;
+  if (bbox) {
+    bb = *bbox;
+  } else if (is_device_ptr(xyz)) {
+    rc = device_bbox(c, xyz, n, &bb);
+    if (rc) return rc;
+  } else {
+    owm_bbox_of(xyz, n, &bb);
+  }
+  if (!c->copy_stream) OWM_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  // This slot's previous run has been waited for, so nothing reads its input
+  // buffer any more.  Reserving on the copy stream orders a (re)allocation
+  // before the copy without making the copy wait for the other run's compute.
+  rc = a.input.reserve((size_t)n * 24 + kXyzSlack, c->copy_stream);
+  if (rc) return rc;
+  OWM_CUDA_TRY(cudaMemcpyAsync(a.input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->copy_stream));
+  // From here on the copy may still be reading xyz: a failed submit waits for
+  // it before returning, so the caller may free xyz after any return.
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamSynchronize(c->side_stream);
+    cudaStreamSynchronize(c->stream);
+    return code;
+  };
+  cudaError_t e = cudaEventRecord(a.ready, c->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, a.ready, 0);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
+    return fail(OWM_ECUDA);
+  }
+  return submit_slot(c, a, static_cast<const double*>(a.input.ptr), n, bb, *cfg, seeds, cap, ticket,
+                     "owm_run_host_submit", fail);
 }
 
 int owm_run_host_wait(owm_ctx* c, int64_t ticket, int64_t* n_seeds, owm_run_info* info) {
@@ -839,6 +898,10 @@ int owm_run_host_wait(owm_ctx* c, int64_t ticket, int64_t* n_seeds, owm_run_info
   if (total > a.cap || total > a.room) return OWM_ERANGE;
   if (total > 0) std::memcpy(a.seeds, a.h_seeds, (size_t)total * 8);
   return OWM_OK;
+}
+
+int owm_run_wait(owm_ctx* c, int64_t ticket, int64_t* n_seeds, owm_run_info* info) {
+  return owm_run_host_wait(c, ticket, n_seeds, info);
 }
 
 }  // extern "C"

@@ -319,6 +319,18 @@ int owm_run_host_submit(owm_ctx* ctx, const double* xyz, int64_t n, const owm_bb
                         const owm_run_cfg* cfg, int64_t* seeds, int64_t cap, int64_t* ticket);
 int owm_run_host_wait(owm_ctx* ctx, int64_t ticket, int64_t* n_seeds, owm_run_info* info);
 
+/* Asynchronous form of owm_run on a device cloud: submit queues the run and
+ * the device->host copy of the seeds and returns a ticket at once, so the
+ * host work of the next submit (parameters, launches) overlaps this run on
+ * the GPU; wait (owm_run_host_wait takes the same tickets) blocks until the
+ * run is done and writes its seeds and counts.  Same two slots, OWM_EAGAIN
+ * rule and results as owm_run_host_submit; the cloud and seeds must stay
+ * valid until wait returns.  info's timings are left zero.  No counterpart
+ * in the reference. */
+int owm_run_submit(owm_ctx* ctx, const owm_cloud* cloud, const owm_run_cfg* cfg, int64_t* seeds,
+                   int64_t cap, int64_t* ticket);
+int owm_run_wait(owm_ctx* ctx, int64_t ticket, int64_t* n_seeds, owm_run_info* info);
+
 /* ---- batched tiles ----------------------------------------------------- */
 /* Many independent tiles (own bbox, Wsize, overlap, Bsize, leaf size) built
  * and queried together: one sort over all tiles, one launch per stage, with
