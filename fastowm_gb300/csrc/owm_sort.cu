@@ -494,9 +494,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_pipe(const uint32_t*
 constexpr int kRkMaxBits = 7;
 constexpr int kRkDigits = 1 << kRkMaxBits;  // 128
 constexpr int kRkQuads = kRkDigits / 4;     // byte-counter words per thread
-constexpr int kRkGroups = kBlock / 8;       // 32 groups of 8 threads
+constexpr int kRkGroups = kBlock / 16;      // 16 groups of 16 threads
 // gt[g][d] (uint16) at g * kRkGtRow + d: word 65g + d/2, bank (g + d/2) % 32, so
-// the scan's writes (one group per lane, one digit) and the rank's reads (4
+// the scan's writes (one group per lane, one digit) and the rank's reads (2
 // groups per warp, any digits) spread over the banks
 constexpr int kRkGtRow = kRkDigits + 2;
 constexpr uint32_t kRkTileBytes = kTile * 4;  // one array's tile: 16 KB
@@ -536,16 +536,20 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 }
 // Waits for the phase with the given parity, at most kRkWaitNs; false when
 // the limit ran out.
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;  // the usual case: the tile is there; no timer read
   const unsigned long long t0 = global_ns();
   for (uint32_t it = 1;; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
+    if (mbar_try(bar, parity)) return true;
     if ((it & 255u) == 0 && global_ns() - t0 > kRkWaitNs) return false;
   }
 }
@@ -558,8 +562,8 @@ __device__ __forceinline__ void tma_tile(uint32_t dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Thread 0: refills stage stg with tile t (keys, and values when kLoadVals);
-// returns the stage's pending bit.
+// The issuing thread: refills stage stg with tile t (keys, and values when
+// kLoadVals); returns the stage's pending bit.
 template <bool kLoadVals>
 __device__ __forceinline__ uint32_t rk_issue(const CUtensorMap* tm_k, const CUtensorMap* tm_v, uint32_t stage_sm,
                                              uint32_t stage_stride, uint32_t bar0, int64_t t, int stg) {
@@ -579,20 +583,26 @@ __device__ __forceinline__ uint32_t rk_issue(const CUtensorMap* tm_k, const CUte
 //          key's digit (word (d / 4, t), byte d % 4) with a shared-memory
 //          atomic add, whose returned old value is the key's rank among the
 //          thread's earlier keys of that digit (at most 15: one byte);
-//   scan   per word of four digits, lane g of a warp takes the 8 words of
-//          threads 8g..8g+7: an exclusive running sum of the words (byte-
-//          wise, at most 128, so no carries) gives each thread's offset
+//   scan   per word of four digits, each half warp's lane g takes the 16
+//          words of threads 16g..16g+15 (two words at once per warp): an
+//          exclusive running sum of the words (byte-wise, at most 240
+//          before the last word, so no carries) gives each thread's offset
 //          inside its group, written back in place; the group totals, as
-//          two words of 16-bit halves, take one warp scan for the 32 groups
-//          (group offsets gt, digit totals); warp 0 scans the digit totals
-//          (S = digit starts) and moves every digit's running output offset;
-//   rank   key position = S[d] + gt[d][group] + in-group offset + own rank:
-//          stable, since the order (digit, thread, item) is the tile order
-//          within a digit; keys and values are stored there, in the tile's
-//          own stage buffer (the thread holds its keys in registers);
+//          two words of 16-bit halves, take one 16-lane scan for the 16
+//          groups (group offsets gt, digit totals);
+//   starts warp 0 scans the digit totals (S = digit starts) and moves every
+//          digit's running output offset, while every thread adds up the
+//          rest of each key's position: gt[group][d] + in-group offset + own
+//          rank (its loads overlap warp 0's scan);
+//   rank   key position = S[d] + that sum: stable, since the order (digit,
+//          thread, item) is the tile order within a digit; each key and its
+//          value are stored there, in the tile's own stage buffer (the
+//          thread holds them in registers);
 //   write  each digit's run goes to its contiguous stretch of the output.
-// Two stages: tile t+1 is in flight while tile t is ranked; a stage is
-// refilled once the tile in it has been written out.  A TMA wait is bounded
+// Two stages: tile t+1 is in flight while tile t is ranked.  The stage of
+// tile t - 1, written out at the end of the last iteration, is refilled with
+// tile t + 1 during tile t's starts phase, by a lane of warp 1, which has
+// slack there (warp 0 scans the digit starts).  A TMA wait is bounded
 // (kRkWaitNs): if one ever runs out, the block sets kStatusWaitExpired in
 // *status, waits (bounded again) for its copies still in flight, and ends.
 template <bool kHasVals, bool kIota>
@@ -635,22 +645,25 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
     }
   }
   for (int i = tid; i < nquads * (kBlock / 4); i += kBlock) reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
-  uint32_t pending = 0;  // thread 0: bit s = a copy into stage s is in flight
+  // Thread kIssuer (warp 1, lane 0) issues the tile copies, during the digit-
+  // start phase, where warp 1 has slack; its bit s of pending: a copy into
+  // stage s is in flight.
+  constexpr int kIssuer = 32;
+  uint32_t pending = 0;
   const uint32_t stage_sm = smem_u32(base);  // stage s at s * kStageBytes
   const uint32_t stage_stride = kStageBytes;
   if (tid == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar0 + 8, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    if (t0 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t0, 0);
-    if (t0 + 1 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t0 + 1, 1);
   }
   __syncthreads();
+  if (tid == kIssuer && t0 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t0, 0);
 
   for (int64_t t = t0; t < t1; ++t) {
     const int stg = (int)((t - t0) & 1);
     const bool arrived = mbar_wait_bounded(bar0 + 8u * stg, (uint32_t)(((t - t0) >> 1) & 1));
-    if (tid == 0 && arrived) pending &= ~(1u << stg);
+    if (tid == kIssuer && arrived) pending &= ~(1u << stg);
     uint32_t* sk = reinterpret_cast<uint32_t*>(base + (uint32_t)stg * kStageBytes);
     uint32_t* sv = reinterpret_cast<uint32_t*>(base + (uint32_t)stg * kStageBytes + kRkTileBytes);
     const int64_t tile_base = t * kTile;
@@ -701,7 +714,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
       own[i >> 3] |= ((old >> sh) & 0xFFu) << ((i & 7) * 4);
     }
     if (__syncthreads_or(!arrived)) {  // a tile never arrived: stop the block
-      if (tid == 0) {
+      if (tid == kIssuer) {
         atomicOr(status, kStatusWaitExpired);
 #pragma unroll
         for (int s2 = 0; s2 < 2; ++s2)
@@ -710,76 +723,117 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
       }
       return;
     }
-    // scan: in-group offsets in place, group offsets gt, digit totals
-    for (int q = w; q < nquads; q += kWarps) {
-      uint32_t* gw = cnt + q * kBlock + lane * 8;
-      uint4 a = *reinterpret_cast<uint4*>(gw);
-      uint4 b = *reinterpret_cast<uint4*>(gw + 4);
-      uint32_t acc = 0, e;
-      e = acc; acc += a.x; a.x = e;
-      e = acc; acc += a.y; a.y = e;
-      e = acc; acc += a.z; a.z = e;
-      e = acc; acc += a.w; a.w = e;
-      e = acc; acc += b.x; b.x = e;
-      e = acc; acc += b.y; b.y = e;
-      e = acc; acc += b.z; b.z = e;
-      e = acc; acc += b.w; b.w = e;
-      *reinterpret_cast<uint4*>(gw) = a;
-      *reinterpret_cast<uint4*>(gw + 4) = b;
-      const uint32_t g02 = acc & 0x00FF00FFu, g13 = (acc >> 8) & 0x00FF00FFu;  // digits 4q+{0,2}, 4q+{1,3}
-      uint32_t i02 = g02, i13 = g13;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t x = __shfl_up_sync(0xffffffffu, i02, o), y = __shfl_up_sync(0xffffffffu, i13, o);
-        if (lane >= o) {
-          i02 += x;
-          i13 += y;
-        }
-      }
-      const uint32_t e02 = i02 - g02, e13 = i13 - g13;
-      uint16_t* gl = gt + lane * kRkGtRow + 4 * q;
-      gl[0] = (uint16_t)(e02 & 0xFFFFu);
-      gl[1] = (uint16_t)(e13 & 0xFFFFu);
-      gl[2] = (uint16_t)(e02 >> 16);
-      gl[3] = (uint16_t)(e13 >> 16);
-      if (lane == 31) {
-        dtot[4 * q + 0] = i02 & 0xFFFFu;
-        dtot[4 * q + 1] = i13 & 0xFFFFu;
-        dtot[4 * q + 2] = i02 >> 16;
-        dtot[4 * q + 3] = i13 >> 16;
-      }
-    }
-    __syncthreads();
-    if (w == 0) {  // digit starts and output offsets, lane l: digits 4l..4l+3
-      uint32_t c[4], sum = 0;
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        const int d = 4 * lane + kk;
-        c[kk] = d <= (int)dmask ? dtot[d] : 0u;
-        sum += c[kk];
-      }
-      uint32_t pre = warp_incl_scan(sum) - sum;
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        const int d = 4 * lane + kk;
-        if (d <= (int)dmask) {
-          S[d] = pre;
-          adj[d] = run[kk] - pre;  // output slot of tile position j of digit d: adj[d] + j
-          run[kk] += c[kk];
-        }
-        pre += c[kk];
-      }
-    }
-    __syncthreads();
-    // rank and place into the stage buffer, now in digit order
+    // scan: in-group offsets in place, group offsets gt, digit totals.
+    // Groups of 16 threads: lanes 0-15 take quad q, lanes 16-31 quad q + 8,
+    // lane g of a half the 16 words of threads 16g..16g+15.  Lane g takes its
+    // four 16-byte chunks starting at chunk r = (g >> 1) & 3, so that each
+    // quarter warp's 16-byte accesses cover the 32 banks once.
     {
-      const uint16_t* gg = gt + (tid >> 3) * kRkGtRow;
+      const int g = lane & 15, hw = lane >> 4, r = (g >> 1) & 3;
+      for (int q0 = w; q0 < nquads; q0 += 2 * kWarps) {
+        const int q = q0 + kWarps * hw;
+        const bool live = q < nquads;
+        uint32_t* gw = cnt + q * kBlock + 16 * g;
+        uint4 L[4], T[4], W[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          L[j] = live ? *reinterpret_cast<const uint4*>(gw + 4 * ((j + r) & 3)) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) T[c] = (r & 1) ? L[(c + 3) & 3] : L[c];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) W[c] = (r & 2) ? T[(c + 2) & 3] : T[c];  // W[c] = chunk c
+        // exclusive byte-wise running sum of the 16 words: at most 15 * 16 =
+        // 240 per byte before the last word, so no carries; the group totals
+        // (up to 256) are formed in 16-bit halves
+        uint32_t acc = 0, e;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          e = acc; acc += W[c].x; W[c].x = e;
+          e = acc; acc += W[c].y; W[c].y = e;
+          e = acc; acc += W[c].z; W[c].z = e;
+          if (c < 3) {
+            e = acc; acc += W[c].w; W[c].w = e;
+          }
+        }
+        const uint32_t last = W[3].w;
+        W[3].w = acc;
+        const uint32_t g02 = (acc & 0x00FF00FFu) + (last & 0x00FF00FFu);  // digits 4q+{0,2}
+        const uint32_t g13 = ((acc >> 8) & 0x00FF00FFu) + ((last >> 8) & 0x00FF00FFu);  // digits 4q+{1,3}
+#pragma unroll
+        for (int c = 0; c < 4; ++c) T[c] = (r & 1) ? W[(c + 1) & 3] : W[c];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) L[c] = (r & 2) ? T[(c + 2) & 3] : T[c];  // L[j] = chunk (j + r) & 3
+        if (live) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) *reinterpret_cast<uint4*>(gw + 4 * ((j + r) & 3)) = L[j];
+        }
+        uint32_t i02 = g02, i13 = g13;
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+          const uint32_t x = __shfl_up_sync(0xffffffffu, i02, o, 16), y = __shfl_up_sync(0xffffffffu, i13, o, 16);
+          if (g >= o) {
+            i02 += x;
+            i13 += y;
+          }
+        }
+        if (live) {
+          const uint32_t e02 = i02 - g02, e13 = i13 - g13;
+          uint16_t* gl = gt + g * kRkGtRow + 4 * q;
+          gl[0] = (uint16_t)(e02 & 0xFFFFu);
+          gl[1] = (uint16_t)(e13 & 0xFFFFu);
+          gl[2] = (uint16_t)(e02 >> 16);
+          gl[3] = (uint16_t)(e13 >> 16);
+          if (g == 15) {
+            dtot[4 * q + 0] = i02 & 0xFFFFu;
+            dtot[4 * q + 1] = i13 & 0xFFFFu;
+            dtot[4 * q + 2] = i02 >> 16;
+            dtot[4 * q + 3] = i13 >> 16;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // the other stage's tile (t - 1) was written out in the last iteration:
+    // refill it with tile t + 1
+    if (tid == kIssuer && t + 1 < t1)
+      pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t + 1, stg ^ 1);
+    if (w == 0) {  // digit starts and output offsets, lane l: digits 4l..4l+3
+      // entries of digits above dmask in the last word are zero counts (the
+      // scan wrote them) and are never read back
+      const uint4 c = lane < nquads ? *reinterpret_cast<const uint4*>(dtot + 4 * lane) : make_uint4(0, 0, 0, 0);
+      const uint32_t sum = c.x + c.y + c.z + c.w;
+      const uint32_t pre = warp_incl_scan(sum) - sum;
+      if (lane < nquads) {
+        const uint4 st = make_uint4(pre, pre + c.x, pre + c.x + c.y, pre + c.x + c.y + c.z);
+        *reinterpret_cast<uint4*>(S + 4 * lane) = st;
+        // output slot of tile position j of digit d: adj[d] + j
+        *reinterpret_cast<uint4*>(adj + 4 * lane) = make_uint4(run[0] - st.x, run[1] - st.y, run[2] - st.z, run[3] - st.w);
+        run[0] += c.x;
+        run[1] += c.y;
+        run[2] += c.z;
+        run[3] += c.w;
+      }
+    }
+    // partial positions (all but the digit start): their loads overlap warp
+    // 0's digit starts
+    uint32_t part[16];
+    {
+      const uint16_t* gg = gt + (tid >> 4) * kRkGtRow;
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const uint32_t d = (k[i] >> shift) & dmask;
         const uint32_t sh = (d & 3u) * 8u;
         const uint32_t in_group = (cnt[(d >> 2) * kBlock + tid] >> sh) & 0xFFu;
-        const uint32_t pos = S[d] + gg[d] + in_group + ((own[i >> 3] >> ((i & 7) * 4)) & 15u);
+        part[i] = gg[d] + in_group + ((own[i >> 3] >> ((i & 7) * 4)) & 15u);
+      }
+    }
+    __syncthreads();
+    // rank and place into the stage buffer, now in digit order
+    {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const uint32_t d = (k[i] >> shift) & dmask;
+        const uint32_t pos = S[d] + part[i];
         if (kHasVals)
           reinterpret_cast<uint2*>(sk)[pos] = make_uint2(k[i], v[i]);  // key and value as one word
         else
@@ -791,7 +845,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
       reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
     {
       const int tn = (int)(n - tile_base < kTile ? n - tile_base : kTile);
-      for (int j = tid; j < tn; j += kBlock) {
+      auto put = [&](int j) {
         if (kHasVals) {
           const uint2 kv = reinterpret_cast<const uint2*>(sk)[j];
           const uint32_t gp = adj[(kv.x >> shift) & dmask] + (uint32_t)j;
@@ -801,10 +855,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_rs_downsweep_rank(const __grid_co
           const uint32_t key = sk[j];
           kout[adj[(key >> shift) & dmask] + (uint32_t)j] = key;
         }
+      };
+      if (tn == kTile) {
+#pragma unroll 4
+        for (int i = 0; i < kItems; ++i) put(tid + i * kBlock);
+      } else {
+        for (int j = tid; j < tn; j += kBlock) put(j);
       }
     }
     __syncthreads();  // stage stg is free again
-    if (tid == 0 && t + 2 < t1) pending |= rk_issue<kLoadVals>(&tm_k, &tm_v, stage_sm, stage_stride, bar0, t + 2, stg);
   }
 }
 
