@@ -510,7 +510,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     if (plan.parts) {
       const MortonIntKey kf{kx0, ky0, (1ll << bits_axis) - 1, shx, shy};
       OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey><<<(unsigned)plan.parts, 256, 0, s>>>(
-          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0)) - 1u, k0, first_counts));
+          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0, true)) - 1u, k0, first_counts));
     } else {
       OWM_LAUNCH("k_morton", s, k_morton_int<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
     }
@@ -518,7 +518,7 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
     if (plan.parts) {
       const MortonFpKey kf{ox, oy, scale, (float)((1u << bits_axis) - 1u)};
       OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey><<<(unsigned)plan.parts, 256, 0, s>>>(
-          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0)) - 1u, k0, first_counts));
+          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0, true)) - 1u, k0, first_counts));
     } else {
       OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
     }

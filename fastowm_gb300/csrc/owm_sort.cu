@@ -1,6 +1,6 @@
 // Device-wide primitives: exclusive scan and an on-chip-staged LSD radix sort
-// (the fewest passes of digits of at most 8 bits, their widths balanced:
-// radix_digit_bits; reduce-then-scan).
+// (the fewest passes of digits of at most 8 bits, or 7 bits for large sorts,
+// their widths balanced: radix_digit_bits; reduce-then-scan).
 //
 // Radix pass over tiles of 4096 keys.  Large sorts split the tiles into one
 // contiguous chunk per persistent block:
@@ -14,8 +14,9 @@
 // counts its 16 consecutive keys in its own byte counters (shared-memory
 // atomics, no warp vote), a word-parallel scan turns the counters into
 // ranks, and tiles arrive by TMA (cp.async.bulk.tensor, 128-byte swizzle,
-// mbarrier completion).  8-bit digits keep the ballot-multisplit kernel
-// (k_rs_downsweep_pipe).
+// mbarrier completion).  Large sorts whose buffers no tensor map can view
+// (a base not 16-byte aligned, no driver entry point) fall back to the
+// ballot-multisplit kernel (k_rs_downsweep_pipe).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -1042,9 +1043,10 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   // where a bounded wait that runs out is recorded when the caller gives no status word
   uint32_t* st = status ? status : reinterpret_cast<uint32_t*>(static_cast<char*>(temp) + temp_bytes - 256);
   int pass = 0;
-  for (int shift = 0; shift < end_bit; shift += radix_digit_bits(end_bit, pass++)) {
+  const bool large = chunks > 0;  // digits of at most 7 bits: every pass ranked
+  for (int shift = 0; shift < end_bit; shift += radix_digit_bits(end_bit, pass++, large)) {
     // a pass sorts on bits [shift, shift + dbits); higher key bits are ignored
-    const int dbits = radix_digit_bits(end_bit, pass);
+    const int dbits = radix_digit_bits(end_bit, pass, large);
     const uint32_t dmask = (1u << dbits) - 1u;
     if (chunks) {
       if (!(first && first_counts_given))
