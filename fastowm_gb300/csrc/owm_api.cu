@@ -156,7 +156,7 @@ using namespace owm;
 struct owm_cloud {
   owm_ctx* ctx;
   int device;  // destroy needs no context (it may already be gone)
-  DeviceBuffer mem;
+  DeviceBuffer mem;  // n records of kCloudStride doubles (x, y, z, pad)
   int64_t n;
   owm_bbox bbox;
 };
@@ -166,7 +166,7 @@ struct owm_tree {
   int device;
   DeviceBuffer mem;
   TreeStore t;
-  const double* d_xyz;  // borrowed from the cloud (stage 3 reads LLP coordinates)
+  const double* d_xyz;  // borrowed from the cloud, kCloudStride doubles a point (stage 3 reads LLP coordinates)
   owm_bbox bbox;
   owm_tree_cfg cfg;
 };
@@ -363,7 +363,7 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
   if (bbox) {
     bb = *bbox;
   } else if (is_device_ptr(xyz)) {
-    int rc = device_bbox(c, xyz, n, &bb);
+    int rc = device_bbox(c, xyz, 3, n, &bb);
     if (rc) return rc;
   } else {
     owm_bbox_of(xyz, n, &bb);
@@ -376,17 +376,30 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
   cl->device = c->device;
   cl->n = n;
   cl->bbox = bb;
-  if (cl->mem.reserve((size_t)n * 24 + kXyzSlack, c->stream) != OWM_OK) {
+  if (cl->mem.reserve((size_t)n * 8 * kCloudStride, c->stream) != OWM_OK) {
     delete cl;
     return OWM_ENOMEM;
   }
-  cudaError_t e = cudaMemcpyAsync(cl->mem.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream);
+  // the points as 32-byte records: from device memory directly, from host
+  // memory (or a device pointer not 8-byte aligned) through a device copy
+  DeviceBuffer stage;
+  const double* src = xyz;
+  int rc = OWM_OK;
+  cudaError_t e = cudaSuccess;
+  if (!is_device_ptr(xyz) || (reinterpret_cast<uintptr_t>(xyz) & 7u) != 0) {
+    rc = stage.reserve((size_t)n * 24, c->stream);
+    if (!rc) e = cudaMemcpyAsync(stage.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream);
+    src = static_cast<const double*>(stage.ptr);
+  }
+  if (!rc && e == cudaSuccess) rc = pad_points(src, n, static_cast<double*>(cl->mem.ptr), c->stream, &c->launches);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) {
-    set_last_cuda_error(e, "cloud copy", __FILE__, __LINE__);
+  stage.release(c->stream);
+  if (rc || e != cudaSuccess) {
+    if (e != cudaSuccess) set_last_cuda_error(e, "cloud copy", __FILE__, __LINE__);
+    cudaStreamSynchronize(c->stream);
     cl->mem.release(c->stream);
     delete cl;
-    return OWM_ECUDA;
+    return rc ? rc : OWM_ECUDA;
   }
   *out = cl;
   return OWM_OK;
@@ -413,7 +426,27 @@ int owm_cloud_copy_out(const owm_cloud* cl, double* xyz, int64_t n) {
   if (!cl || !xyz || n < 0 || n > cl->n) return OWM_EINVAL;
   if (n == 0) return OWM_OK;
   OWM_CUDA_TRY(cudaSetDevice(cl->device));
-  OWM_CUDA_TRY(cudaMemcpy(xyz, cl->mem.ptr, (size_t)n * 24, cudaMemcpyDefault));
+  // the records' x, y, z into plain points: in a device copy, then to xyz
+  // (its own stream and memory: the cloud's context may be busy or gone)
+  double* tmp = nullptr;
+  cudaStream_t s = nullptr;
+  int64_t launches = 0;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&tmp), (size_t)n * 24, s);
+  int rc = e == cudaSuccess ? unpad_points(static_cast<const double*>(cl->mem.ptr), n, tmp, s, &launches) : OWM_ECUDA;
+  if (!rc) e = cudaMemcpyAsync(xyz, tmp, (size_t)n * 24, cudaMemcpyDefault, s);
+  if (s) {
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (tmp) cudaFreeAsync(tmp, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  if (rc) return rc;
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "owm_cloud_copy_out", __FILE__, __LINE__);
+    return OWM_ECUDA;
+  }
   return OWM_OK;
 }
 
@@ -423,7 +456,7 @@ int finish_parsed_cloud(owm_ctx* c, DeviceBuffer& mem, int64_t n, int64_t declar
                         owm_cloud** out) {
   owm_bbox bb = hb;
   if (declared < 0) {
-    int rc = device_bbox(c, static_cast<const double*>(mem.ptr), n, &bb);
+    int rc = device_bbox(c, static_cast<const double*>(mem.ptr), kCloudStride, n, &bb);
     if (rc) return rc;
   }
   if (!std::isfinite(bb.min_x) || !std::isfinite(bb.max_x) || !std::isfinite(bb.min_y) ||
@@ -559,7 +592,7 @@ int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm
   if (!rc) rc = c->scratch.reserve(tree_scratch_bytes(cl->n), c->stream);
   if (!rc) rc = clear_status(c);
   if (!rc)
-    rc = build_tree(tr->d_xyz, cl->n, cl->bbox, *cfg, &tr->t, c->scratch.ptr, c->scratch.cap,
+    rc = build_tree(tr->d_xyz, kCloudStride, cl->n, cl->bbox, *cfg, &tr->t, c->scratch.ptr, c->scratch.cap,
                     c->d_small + kStatusSlot, c->stream, &c->launches);
   if (!rc) rc = check_input_status(c);
   if (rc) {
@@ -696,7 +729,7 @@ int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_
   }
   rc = clear_status(c);
   if (!rc)
-    rc = run_stage3(tr->t.view(c->walk_limit, c->tuning.cell_warps), tr->d_xyz, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
+    rc = run_stage3(tr->t.view(c->walk_limit, c->tuning.cell_warps), tr->d_xyz, kCloudStride, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
                     c->d_job, c->d_small + kStatusSlot, c->stream, &c->launches);
   if (!rc) rc = check_input_status(c);
   if (rc) return rc;
@@ -719,7 +752,8 @@ int owm_run(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int64_t* se
   ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !cl || !cfg || !n_seeds || (!seeds && cap > 0)) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
-  return run_pipeline(c, static_cast<const double*>(cl->mem.ptr), cl->n, cl->bbox, *cfg, seeds, cap, n_seeds, info);
+  return run_pipeline(c, static_cast<const double*>(cl->mem.ptr), kCloudStride, cl->n, cl->bbox, *cfg, seeds, cap,
+                      n_seeds, info);
 }
 
 int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox, const owm_run_cfg* cfg,
@@ -731,7 +765,7 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   if (bbox) {
     bb = *bbox;
   } else if (is_device_ptr(xyz)) {
-    int rc = device_bbox(c, xyz, n, &bb);
+    int rc = device_bbox(c, xyz, 3, n, &bb);
     if (rc) return rc;
   } else {
     owm_bbox_of(xyz, n, &bb);
@@ -739,7 +773,7 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   int rc = c->input.reserve((size_t)n * 24 + kXyzSlack, c->stream);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
-  return run_pipeline(c, static_cast<const double*>(c->input.ptr), n, bb, *cfg, seeds, cap, n_seeds, info);
+  return run_pipeline(c, static_cast<const double*>(c->input.ptr), 3, n, bb, *cfg, seeds, cap, n_seeds, info);
 }
 
 }  // extern "C"
@@ -752,11 +786,11 @@ namespace {
 // staging, and hands out the ticket.  On failure the caller's fail() waits
 // for everything queued so far.
 template <class Fail>
-int submit_slot(owm_ctx* c, owm_ctx::AsyncSlot& a, const double* d_xyz, int64_t n, const owm_bbox& bb,
+int submit_slot(owm_ctx* c, owm_ctx::AsyncSlot& a, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb,
                 const owm_run_cfg& cfg, int64_t* seeds, int64_t cap, int64_t* ticket, const char* fn, Fail fail) {
   int64_t* d_seeds = nullptr;
   int64_t room = 0;
-  int rc = run_pipeline_enqueue(c, d_xyz, n, bb, cfg, &a.p, &d_seeds, &room);
+  int rc = run_pipeline_enqueue(c, d_xyz, stride, n, bb, cfg, &a.p, &d_seeds, &room);
   if (rc) return fail(rc);
   if (a.h_cap < room) {
     // growth only: the old staging may still be a copy target
@@ -824,7 +858,8 @@ int owm_run_submit(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int6
     cudaStreamSynchronize(c->stream);
     return code;
   };
-  return submit_slot(c, *a, static_cast<const double*>(cl->mem.ptr), cl->n, cl->bbox, *cfg, seeds, cap, ticket,
+  return submit_slot(c, *a, static_cast<const double*>(cl->mem.ptr), kCloudStride, cl->n, cl->bbox, *cfg, seeds, cap,
+                     ticket,
                      "owm_run_submit", fail);
 }
 
@@ -841,7 +876,7 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
   if (bbox) {
     bb = *bbox;
   } else if (is_device_ptr(xyz)) {
-    rc = device_bbox(c, xyz, n, &bb);
+    rc = device_bbox(c, xyz, 3, n, &bb);
     if (rc) return rc;
   } else {
     owm_bbox_of(xyz, n, &bb);
@@ -867,7 +902,7 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
     set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
     return fail(OWM_ECUDA);
   }
-  return submit_slot(c, a, static_cast<const double*>(a.input.ptr), n, bb, *cfg, seeds, cap, ticket,
+  return submit_slot(c, a, static_cast<const double*>(a.input.ptr), 3, n, bb, *cfg, seeds, cap, ticket,
                      "owm_run_host_submit", fail);
 }
 

@@ -38,13 +38,14 @@ namespace {
 // Integer form: when the domain's ends share sign and exponent, the order key
 // of a double is linear in its value over the domain, so the cell index is
 // (key(v) - key(lo)) >> shift -- no FP64 arithmetic at all.
+template <int kStride>
 __global__ void k_morton_int(const double* __restrict__ xyz, int64_t n, int64_t kx0, int64_t ky0, int shx, int shy,
                              int bits, uint32_t* __restrict__ keys) {
   const int64_t qmax = (1ll << bits) - 1;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t qx = (dkey(__ldg(xyz + 3 * i)) - kx0) >> shx;
-    int64_t qy = (dkey(__ldg(xyz + 3 * i + 1)) - ky0) >> shy;
+    int64_t qx = (dkey(__ldg(xyz + kStride * i)) - kx0) >> shx;
+    int64_t qy = (dkey(__ldg(xyz + kStride * i + 1)) - ky0) >> shy;
     qx = qx < 0 ? 0 : (qx > qmax ? qmax : qx);
     qy = qy < 0 ? 0 : (qy > qmax ? qmax : qy);
     keys[i] = (spread_bits16((uint32_t)qx) << 1) | spread_bits16((uint32_t)qy);
@@ -52,12 +53,13 @@ __global__ void k_morton_int(const double* __restrict__ xyz, int64_t n, int64_t 
 }
 
 // General form (domain spans exponents): scaled FP64 offsets.
+template <int kStride>
 __global__ void k_morton(const double* __restrict__ xyz, int64_t n, double ox, double oy, double scale,
                          int bits, uint32_t* __restrict__ keys) {
   const float qmax = (float)((1u << bits) - 1u);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    double x = __ldg(xyz + 3 * i), y = __ldg(xyz + 3 * i + 1);
+    double x = __ldg(xyz + kStride * i), y = __ldg(xyz + kStride * i + 1);
     float fx = (float)((x - ox) * scale), fy = (float)((y - oy) * scale);
     fx = fminf(fmaxf(fx, 0.0f), qmax);
     fy = fminf(fmaxf(fy, 0.0f), qmax);
@@ -93,7 +95,7 @@ struct MortonFpKey {
 // part's counts of the sort's first digit (key & dmask0) into
 // counts[d * gridDim.x + blockIdx.x]: the first radix pass then needs no
 // separate read of the keys.
-template <class KeyOf>
+template <class KeyOf, int kStride>
 __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict__ xyz, int64_t n, KeyOf key_of,
                                                        int64_t ntiles, uint32_t dmask0, uint32_t* __restrict__ keys,
                                                        uint32_t* __restrict__ counts) {
@@ -107,7 +109,7 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
   for (; i + 3 * 256 < e; i += 4 * 256) {  // four points in flight per thread
     uint32_t k[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) k[u] = key_of(xyz + 3 * (i + u * 256));
+    for (int u = 0; u < 4; ++u) k[u] = key_of(xyz + kStride * (i + u * 256));
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       keys[i + u * 256] = k[u];
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
     }
   }
   for (; i < e; i += 256) {
-    const uint32_t k = key_of(xyz + 3 * i);
+    const uint32_t k = key_of(xyz + kStride * i);
     keys[i] = k;
     atomicAdd(hw + (k & dmask0), 1u);
   }
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
 // With kCls, every chunk of 32 gathered points is also folded into the
 // stage-1 window classes (the point is already in registers; this kernel is
 // DRAM-bound, so the classification costs next to nothing here).
-template <int L, bool kCls>
+template <int L, bool kCls, int kStride>
 __global__ void __launch_bounds__(512) k_gather_leaves(const double* __restrict__ xyz, const uint32_t* __restrict__ perm,
                                                        int64_t n, int32_t nleaves, double ox, double oy,
                                                        int64_t* __restrict__ xk, int64_t* __restrict__ yk,
@@ -157,7 +159,7 @@ __global__ void __launch_bounds__(512) k_gather_leaves(const double* __restrict_
       uint32_t src = 0;
       if (valid) {
         src = __ldg(perm + pos);
-        finite &= load_point16(xyz, src, x, y, z);
+        finite &= load_point16<kStride>(xyz, src, x, y, z);
         xk[pos] = x;
         yk[pos] = y;
         zk[pos] = z;
@@ -185,6 +187,7 @@ __global__ void __launch_bounds__(512) k_gather_leaves(const double* __restrict_
   if (!finite) atomicOr(status, 1u);
 }
 
+template <int kStride>
 __global__ void k_gather(const double* __restrict__ xyz, const uint32_t* __restrict__ perm, int64_t n,
                          int64_t* __restrict__ xk, int64_t* __restrict__ yk, int64_t* __restrict__ zk,
                          uint32_t* __restrict__ pid, uint32_t* __restrict__ status) {
@@ -193,7 +196,7 @@ __global__ void k_gather(const double* __restrict__ xyz, const uint32_t* __restr
        pos += (int64_t)gridDim.x * blockDim.x) {
     uint32_t src = __ldg(perm + pos);
     int64_t x, y, z;
-    finite &= load_point16(xyz, src, x, y, z);
+    finite &= load_point16<kStride>(xyz, src, x, y, z);
     xk[pos] = x;
     yk[pos] = y;
     zk[pos] = z;
@@ -378,7 +381,7 @@ int grid_for(int64_t n, int block) {
   return (int)g;
 }
 
-template <int L>
+template <int L, int kStride>
 void launch_gather_leaves(const double* xyz, const uint32_t* perm, int64_t n, int32_t nl, double ox, double oy,
                           TreeStore* t, uint32_t* status, cudaStream_t s, const ClassArgs* cls) {
   constexpr int kUnit = L < 32 ? 32 : L;
@@ -390,14 +393,33 @@ void launch_gather_leaves(const double* xyz, const uint32_t* perm, int64_t n, in
   // neighbouring units, which measured 12-15% faster than 16 blocks per SM
   if (blocks > (int64_t)152 * 1024 * 256 / gb) blocks = (int64_t)152 * 1024 * 256 / gb;
   if (cls) {
-    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, true><<<(unsigned)blocks, gb, 0, s>>>(
+    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, true, kStride><<<(unsigned)blocks, gb, 0, s>>>(
         xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid, t->nodes + (nl - 1), status, *cls));
   } else {
     ClassArgs none;
     std::memset(&none, 0, sizeof(none));
-    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, false><<<(unsigned)blocks, gb, 0, s>>>(
+    OWM_LAUNCH("k_gather_leaves", s, k_gather_leaves<L, false, kStride><<<(unsigned)blocks, gb, 0, s>>>(
         xyz, perm, n, nl, ox, oy, t->xk, t->yk, t->zk, t->pid, t->nodes + (nl - 1), status, none));
   }
+}
+
+template <int kStride>
+int gather_leaves_for(int32_t L, const double* xyz, const uint32_t* perm, int64_t n, int32_t nl, double ox, double oy,
+                      TreeStore* t, uint32_t* status, cudaStream_t s, const ClassArgs* cls) {
+  switch (L) {
+    case 1: launch_gather_leaves<1, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 2: launch_gather_leaves<2, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 4: launch_gather_leaves<4, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 8: launch_gather_leaves<8, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 16: launch_gather_leaves<16, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 32: launch_gather_leaves<32, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 64: launch_gather_leaves<64, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 128: launch_gather_leaves<128, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    case 256: launch_gather_leaves<256, kStride>(xyz, perm, n, nl, ox, oy, t, status, s, cls); break;
+    default:
+      return OWM_EINVAL;  // unreachable: leaf_size() gives powers of two up to 256
+  }
+  return OWM_OK;
 }
 
 }  // namespace
@@ -459,12 +481,13 @@ size_t tree_scratch_bytes(int64_t n) {
   return a + 1024;
 }
 
-int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
+int build_tree(const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
                void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
                const ClassArgs* cls, bool* fused, cudaEvent_t cls_ready, cudaEvent_t gather_done) {
   if (fused) *fused = false;
-  if (n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
-  if ((reinterpret_cast<uintptr_t>(d_xyz) & 15u) != 0) return OWM_EINVAL;  // the gather reads 16-byte words
+  if (n <= 0 || n >= 0x7FFFFFFFLL || (stride != 3 && stride != 4)) return OWM_EINVAL;
+  // the gather reads 16-byte words; a 32-byte record is one sector
+  if ((reinterpret_cast<uintptr_t>(d_xyz) & (stride == 4 ? 31u : 15u)) != 0) return OWM_EINVAL;
   if (scratch_bytes < tree_scratch_bytes(n)) return OWM_ENOMEM;
   char* sp = static_cast<char*>(scratch);
   auto take = [&](size_t bytes) {
@@ -509,18 +532,32 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
       morton_int_shifts(oy, oy + 2.0 * R, bits_axis, &ky0, &shy)) {
     if (plan.parts) {
       const MortonIntKey kf{kx0, ky0, (1ll << bits_axis) - 1, shx, shy};
-      OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey><<<(unsigned)plan.parts, 256, 0, s>>>(
-          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0, true)) - 1u, k0, first_counts));
+      const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, true)) - 1u;
+      if (stride == 4)
+        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey, 4><<<(unsigned)plan.parts, 256, 0, s>>>(
+            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
+      else
+        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey, 3><<<(unsigned)plan.parts, 256, 0, s>>>(
+            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
+    } else if (stride == 4) {
+      OWM_LAUNCH("k_morton", s, k_morton_int<4><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
     } else {
-      OWM_LAUNCH("k_morton", s, k_morton_int<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
+      OWM_LAUNCH("k_morton", s, k_morton_int<3><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
     }
   } else {
     if (plan.parts) {
       const MortonFpKey kf{ox, oy, scale, (float)((1u << bits_axis) - 1u)};
-      OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey><<<(unsigned)plan.parts, 256, 0, s>>>(
-          d_xyz, n, kf, plan.ntiles, (1u << radix_digit_bits(key_bits, 0, true)) - 1u, k0, first_counts));
+      const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, true)) - 1u;
+      if (stride == 4)
+        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey, 4><<<(unsigned)plan.parts, 256, 0, s>>>(
+            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
+      else
+        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey, 3><<<(unsigned)plan.parts, 256, 0, s>>>(
+            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
+    } else if (stride == 4) {
+      OWM_LAUNCH("k_morton", s, k_morton<4><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
     } else {
-      OWM_LAUNCH("k_morton", s, k_morton<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+      OWM_LAUNCH("k_morton", s, k_morton<3><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
     }
   }
   count_launch(launches);
@@ -568,24 +605,17 @@ int build_tree(const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_tre
 
   if (fixed) {
     if (cls && cls_ready) OWM_CUDA_TRY(cudaStreamWaitEvent(s, cls_ready, 0));
-    switch (L) {
-      case 1: launch_gather_leaves<1>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 2: launch_gather_leaves<2>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 4: launch_gather_leaves<4>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 8: launch_gather_leaves<8>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 16: launch_gather_leaves<16>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 32: launch_gather_leaves<32>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 64: launch_gather_leaves<64>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 128: launch_gather_leaves<128>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      case 256: launch_gather_leaves<256>(d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls); break;
-      default:
-        return OWM_EINVAL;  // unreachable: leaf_size() gives powers of two up to 256
-    }
+    const int grc = stride == 4 ? gather_leaves_for<4>(L, d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls)
+                                : gather_leaves_for<3>(L, d_xyz, perm, n, nl, t->ox, t->oy, t, status, s, cls);
+    if (grc) return grc;
     count_launch(launches);
     if (fused && cls) *fused = true;
     if (cls && gather_done) OWM_CUDA_TRY(cudaEventRecord(gather_done, s));
   } else {
-    OWM_LAUNCH("k_gather", s, k_gather<<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status));
+    if (stride == 4)
+      OWM_LAUNCH("k_gather", s, k_gather<4><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status));
+    else
+      OWM_LAUNCH("k_gather", s, k_gather<3><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, perm, n, t->xk, t->yk, t->zk, t->pid, status));
     count_launch(launches);
     int64_t blocks = ((int64_t)nl * 32 + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;

@@ -107,14 +107,22 @@ namespace owm {
 int clear_status(owm_ctx* c);
 // Reads the status word (syncs); OWM_EINVAL if the input had a non-finite value.
 int check_input_status(owm_ctx* c);
-int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out);
+// Device points are AoS records of `stride` doubles: 4 for a cloud's 32-byte
+// records (x, y, z, pad: one DRAM sector per point for the build's random
+// gather), 3 for plain x, y, z (a caller's device array, host input copied in).
+constexpr int kCloudStride = 4;
+// n plain points (device, 8-byte aligned) into 32-byte records (32-byte
+// aligned dst), and back; queued on s.
+int pad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches);
+int unpad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches);
+int device_bbox(owm_ctx* c, const double* d_xyz, int stride, int64_t n, owm_bbox* out);
 int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Edge* ey, uint32_t* d_win);
-int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+int run_pipeline(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
                  int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info);
 // The device part of run_pipeline: enqueues the whole run on c->stream and
 // leaves the status words in c->d_small and the assembled seeds (room slots)
 // at *d_seeds; no host sync (except inside the min-radius build).
-int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
-                         owm_params* p, int64_t** d_seeds, int64_t* room);
+int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb,
+                         const owm_run_cfg& cfg, owm_params* p, int64_t** d_seeds, int64_t* room);
 
 }  // namespace owm

@@ -130,10 +130,6 @@ __device__ __forceinline__ void write_leaf_seg(Node* nd, const LeafAcc& a, int32
   }
 }
 
-// load_point with two aligned 16-byte reads instead of three 8-byte ones (a
-// third fewer random requests in the build's gather): the point's 24 bytes lie
-// in the 32 bytes from the 16-byte boundary at or below x.  Needs a 16-byte
-// aligned xyz with kXyzSlack readable bytes after the last point.
 // Read-only 16-byte load whose L2 miss asks for 64 bytes (the prefetch-size
 // hint), for gathers of random points.
 __device__ __forceinline__ double2 ldg_l2_64(const double2* p) {
@@ -142,13 +138,34 @@ __device__ __forceinline__ double2 ldg_l2_64(const double2* p) {
   return r;
 }
 
+// load_point with two aligned 16-byte reads instead of three 8-byte ones, for
+// AoS records of kStride doubles.  kStride 4 (a cloud's 32-byte records,
+// x, y, z, pad): the point is one aligned 32-byte sector.  kStride 3 (plain
+// 24-byte points): the point lies in the 32 bytes from the 16-byte boundary at
+// or below x, which straddle two sectors for half the points; needs kXyzSlack
+// readable bytes after the last point.  xyz 16-byte aligned (32 for kStride 4).
+// Both take the 64-byte hint: without it a random miss fetched more (123
+// instead of 67 bytes read per point, 32-byte records, 24 M points).
+template <int kStride>
 __device__ __forceinline__ bool load_point16(const double* __restrict__ xyz, uint32_t src, int64_t& x, int64_t& y,
                                              int64_t& z) {
-  const int64_t e = 3 * (int64_t)src;
-  const int odd = (int)(e & 1);
-  const double2* w = reinterpret_cast<const double2*>(xyz + (e - odd));
-  const double2 a = ldg_l2_64(w), b = ldg_l2_64(w + 1);
-  const double dx = odd ? a.y : a.x, dy = odd ? b.x : a.y, dz = odd ? b.y : b.x;
+  static_assert(kStride == 3 || kStride == 4, "records of 3 or 4 doubles");
+  double dx, dy, dz;
+  if (kStride == 4) {
+    const double2* w = reinterpret_cast<const double2*>(xyz + 4 * (int64_t)src);
+    const double2 a = ldg_l2_64(w), b = ldg_l2_64(w + 1);
+    dx = a.x;
+    dy = a.y;
+    dz = b.x;
+  } else {
+    const int64_t e = 3 * (int64_t)src;
+    const int odd = (int)(e & 1);
+    const double2* w = reinterpret_cast<const double2*>(xyz + (e - odd));
+    const double2 a = ldg_l2_64(w), b = ldg_l2_64(w + 1);
+    dx = odd ? a.y : a.x;
+    dy = odd ? b.x : a.y;
+    dz = odd ? b.y : b.x;
+  }
   x = dkey(dx);
   y = dkey(dy);
   z = dkey(dz);

@@ -570,13 +570,21 @@ __global__ void __launch_bounds__(256) k_nl_starts(const char* __restrict__ text
 }
 
 struct ParseOut {
-  double* vals;             // [nlines][3]
+  double* vals;             // [nlines][4]: cloud records x, y, z, 0
   uint8_t* status;          // [nlines]
   int64_t* slow;            // queued line indices
   unsigned long long* nslow;
   unsigned long long* first_error;  // lowest error line (atomic min)
   unsigned long long* nblank;       // blank lines
 };
+
+// Line i's point as record i of a cloud (two 16-byte stores: the whole
+// 32-byte record, pad included).
+__device__ __forceinline__ void put_record(double* vals, int64_t i, const double* v) {
+  double2* d = reinterpret_cast<double2*>(vals + 4 * i);
+  d[0] = make_double2(v[0], v[1]);
+  d[1] = make_double2(v[2], 0.0);
+}
 
 // One thread per line i: [starts[i], starts[i+1] - 1) (the newline excluded).
 // A warp takes 32 consecutive lines: their text is one contiguous span, which
@@ -614,9 +622,7 @@ __global__ void __launch_bounds__(256, 4) k_parse(const char* __restrict__ text,
       }
       o.status[i] = (uint8_t)st;
       if (st == kLinePoint) {
-        o.vals[3 * i] = v[0];
-        o.vals[3 * i + 1] = v[1];
-        o.vals[3 * i + 2] = v[2];
+        put_record(o.vals, i, v);
       } else if (st == kLineSlow) {
         o.slow[atomicAdd(o.nslow, 1ull)] = i;
       } else if (st == kLineError) {
@@ -642,9 +648,7 @@ __global__ void __launch_bounds__(128) k_parse_slow(const char* __restrict__ tex
     const int st = parse_line<true>(tc, starts[i], v, big);
     o.status[i] = (uint8_t)st;
     if (st == kLinePoint) {
-      o.vals[3 * i] = v[0];
-      o.vals[3 * i + 1] = v[1];
-      o.vals[3 * i + 2] = v[2];
+      put_record(o.vals, i, v);
     } else {
       atomicMin(o.first_error, (unsigned long long)i);  // a queued line is a point or an error
     }
@@ -662,16 +666,17 @@ __global__ void k_line_flags(const uint8_t* __restrict__ status, int64_t nlines,
   }
 }
 
-// Points [0, n) of the flagged lines, in line order, into out (AoS).
+// Points [0, n) of the flagged lines, in line order, into out (cloud records).
 __global__ void k_compact_points(const double* __restrict__ vals, const uint32_t* __restrict__ is_point,
                                  const uint32_t* __restrict__ pos, int64_t nlines, int64_t n, double* __restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlines;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (!is_point[i] || pos[i] >= (uint64_t)n) continue;
     const int64_t j = pos[i];
-    out[3 * j] = vals[3 * i];
-    out[3 * j + 1] = vals[3 * i + 1];
-    out[3 * j + 2] = vals[3 * i + 2];
+    const double2* r = reinterpret_cast<const double2*>(vals + 4 * i);
+    double2* d = reinterpret_cast<double2*>(out + 4 * j);
+    d[0] = r[0];
+    d[1] = r[1];
   }
 }
 
@@ -806,7 +811,7 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   // (k_nl_starts numbers newlines from begin, so its index is shifted by hdr_nl)
   // per-line values in their own buffer: when the first n lines are all
   // points it becomes the cloud as it is (no compaction)
-  rc = vbuf.reserve((size_t)nlines * 24 + kXyzSlack, s);
+  rc = vbuf.reserve((size_t)nlines * 8 * kCloudStride, s);
   if (rc) return rc;
   const size_t lb = a256((size_t)(nlines + 1 + hdr_nl + 1) * 8) + a256((size_t)nlines) +
                     2 * a256((size_t)nlines * 4) + a256((size_t)nlines * 8) + a256(scan_temp_bytes(nlines)) + 1024;
@@ -886,7 +891,7 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
     vbuf.ptr = nullptr;
     vbuf.cap = 0;
   } else if (!rc) {
-    rc = out_mem->reserve((size_t)n * 24 + kXyzSlack, s);
+    rc = out_mem->reserve((size_t)n * 8 * kCloudStride, s);
     if (!rc) {
       OWM_LAUNCH("k_compact_points", s, k_compact_points<<<grid_of(nlines, 256), 256, 0, s>>>(
           vals, is_point, pos, nlines, n, static_cast<double*>(out_mem->ptr)));

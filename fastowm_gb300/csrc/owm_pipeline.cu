@@ -15,11 +15,11 @@ namespace owm {
 
 namespace {
 
-__global__ void k_bbox(const double* __restrict__ xyz, int64_t n, long long* __restrict__ out) {
+__global__ void k_bbox(const double* __restrict__ xyz, int stride, int64_t n, long long* __restrict__ out) {
   long long x0 = 0x7FFFFFFFFFFFFFFFll, y0 = 0x7FFFFFFFFFFFFFFFll;
   long long x1 = (long long)0x8000000000000000ull, y1 = (long long)0x8000000000000000ull;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    long long x = dkey(xyz[3 * i]), y = dkey(xyz[3 * i + 1]);
+    long long x = dkey(xyz[stride * i]), y = dkey(xyz[stride * i + 1]);
     x0 = min(x0, x);
     x1 = max(x1, x);
     y0 = min(y0, y);
@@ -36,6 +36,27 @@ __global__ void k_bbox(const double* __restrict__ xyz, int64_t n, long long* __r
     atomicMin(out + 1, y0);
     atomicMax(out + 2, x1);
     atomicMax(out + 3, y1);
+  }
+}
+
+// Plain x, y, z points into a cloud's 32-byte records (x, y, z, 0), each
+// record written whole (two 16-byte stores), and back.
+__global__ void k_pad_points(const double* __restrict__ src, int64_t n, double* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = src[3 * i], y = src[3 * i + 1], z = src[3 * i + 2];
+    double2* d = reinterpret_cast<double2*>(dst + 4 * i);
+    d[0] = make_double2(x, y);
+    d[1] = make_double2(z, 0.0);
+  }
+}
+
+__global__ void k_unpad_points(const double* __restrict__ src, int64_t n, double* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2* r = reinterpret_cast<const double2*>(src + 4 * i);
+    const double2 a = r[0], b = r[1];
+    dst[3 * i] = a.x;
+    dst[3 * i + 1] = a.y;
+    dst[3 * i + 2] = b.x;
   }
 }
 
@@ -68,7 +89,7 @@ int check_input_status(owm_ctx* c) {
   return OWM_OK;
 }
 
-int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out) {
+int device_bbox(owm_ctx* c, const double* d_xyz, int stride, int64_t n, owm_bbox* out) {
   long long init[4] = {0x7FFFFFFFFFFFFFFFll, 0x7FFFFFFFFFFFFFFFll, (long long)0x8000000000000000ull,
                        (long long)0x8000000000000000ull};
   long long* d = reinterpret_cast<long long*>(c->d_small + kBboxSlot);
@@ -77,7 +98,7 @@ int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out) {
   OWM_CUDA_TRY(cudaMemcpyAsync(d, h, sizeof(init), cudaMemcpyHostToDevice, c->stream));
   int64_t g = std::min<int64_t>((n + 255) / 256, 152 * 8);
   const unsigned gb = (unsigned)std::max<int64_t>(g, 1);
-  OWM_LAUNCH("k_bbox", c->stream, k_bbox<<<gb, 256, 0, c->stream>>>(d_xyz, n, d));
+  OWM_LAUNCH("k_bbox", c->stream, k_bbox<<<gb, 256, 0, c->stream>>>(d_xyz, stride, n, d));
   count_launch(&c->launches);
   OWM_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(init), cudaMemcpyDeviceToHost, c->stream));
   OWM_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -85,6 +106,22 @@ int device_bbox(owm_ctx* c, const double* d_xyz, int64_t n, owm_bbox* out) {
   out->min_y = dkey_inv(h[1]);
   out->max_x = dkey_inv(h[2]);
   out->max_y = dkey_inv(h[3]);
+  return OWM_OK;
+}
+
+int pad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches) {
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+  OWM_LAUNCH("k_pad_points", s, k_pad_points<<<g, 256, 0, s>>>(src, n, dst));
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
+  return OWM_OK;
+}
+
+int unpad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches) {
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+  OWM_LAUNCH("k_unpad_points", s, k_unpad_points<<<g, 256, 0, s>>>(src, n, dst));
+  count_launch(launches);
+  OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
 }
 
@@ -107,8 +144,8 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   return run_query(j, c->d_job, c->stream, &c->launches, "k_query_s1");
 }
 
-int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
-                         owm_params* p_out, int64_t** d_seeds, int64_t* room_out) {
+int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb,
+                         const owm_run_cfg& cfg, owm_params* p_out, int64_t** d_seeds, int64_t* room_out) {
   if (validate_tree_cfg(&cfg.tree) != OWM_OK) return OWM_EINVAL;
   owm_params& p = *p_out;
   int rc = owm_params_compute(&bb, n, cfg.wsize, cfg.overlap, cfg.bsize, &p);
@@ -177,7 +214,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   c->stage12_side = false;
   c->tree.gather_block = c->tuning.gather_block;
   if (!rc)
-    rc = build_tree(d_xyz, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
+    rc = build_tree(d_xyz, stride, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
                     &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr,
                     forked ? c->ev[6] : nullptr);
   void* s2scratch = static_cast<char*>(c->scratch.ptr) + tbytes + cbytes;
@@ -208,7 +245,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
       rc = bitmap2 ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, ss, &c->launches, true, true)
                    : stage2(ss);
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[3], ss));
-    if (!rc) rc = run_stage3_mark(d_xyz, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
+    if (!rc) rc = run_stage3_mark(d_xyz, stride, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   // join (again, if the gather already did): nothing queued on s after this
@@ -234,7 +271,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   }
   rc = c->stage12_side
            ? run_stage3_query(c->tree.view(c->walk_limit, c->tuning.cell_warps), p, s3, d_ns3, s3scratch, s3cap, c->d_small + kStatusSlot, s, &c->launches)
-           : run_stage3(c->tree.view(c->walk_limit, c->tuning.cell_warps), d_xyz, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
+           : run_stage3(c->tree.view(c->walk_limit, c->tuning.cell_warps), d_xyz, stride, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
                         c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));
@@ -248,12 +285,12 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int64_t n, const owm_b
   return OWM_OK;
 }
 
-int run_pipeline(owm_ctx* c, const double* d_xyz, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+int run_pipeline(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
                  int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
   owm_params p;
   int64_t* s64 = nullptr;
   int64_t room = 0;
-  int rc = run_pipeline_enqueue(c, d_xyz, n, bb, cfg, &p, &s64, &room);
+  int rc = run_pipeline_enqueue(c, d_xyz, stride, n, bb, cfg, &p, &s64, &room);
   if (rc) return rc;
   cudaStream_t s = c->stream;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small, 32, cudaMemcpyDeviceToHost, s));

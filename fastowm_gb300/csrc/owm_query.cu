@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact_small(const uint32_t*
 // ---- stage 3 -----------------------------------------------------------------
 // LLP grid (owm_optim3.cpp:192-197 + countNeighbors, optim3_func.cpp:503-539):
 // a cell is occupied when an LLP lies strictly inside its box.
-__global__ void k_s3_mark(const double* __restrict__ xyz, const uint32_t* __restrict__ llp,
+__global__ void k_s3_mark(const double* __restrict__ xyz, int stride, const uint32_t* __restrict__ llp,
                           const uint32_t* __restrict__ nllp, int64_t cap, const Edge* __restrict__ ex,
                           const Edge* __restrict__ ey, int32_t ncols, int32_t nrows, double min_x, double min_y,
                           double bsize, uint8_t* __restrict__ mark) {
@@ -469,8 +469,8 @@ __global__ void k_s3_mark(const double* __restrict__ xyz, const uint32_t* __rest
     uint32_t id = llp[k];
     double x = 0.0, y = 0.0;  // id 0 is the sentinel point {0, 0, DBL_MAX}
     if (id > 0) {
-      x = xyz[3 * (int64_t)(id - 1)];
-      y = xyz[3 * (int64_t)(id - 1) + 1];
+      x = xyz[stride * (int64_t)(id - 1)];
+      y = xyz[stride * (int64_t)(id - 1) + 1];
     }
     const int64_t xk = dkey(x), yk = dkey(y);
     // candidate cells around floor((v - min)/B); the exact test decides
@@ -751,14 +751,14 @@ int run_stage3_prepare(double ox, double oy, const owm_params& p, void* scratch,
   return OWM_OK;
 }
 
-int run_stage3_mark(const double* d_xyz, const owm_params& p, const uint32_t* d_llp, const uint32_t* d_nllp,
+int run_stage3_mark(const double* d_xyz, int stride, const owm_params& p, const uint32_t* d_llp, const uint32_t* d_nllp,
                     int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches) {
   const int64_t ng = p.ngrid;
   if (p.bsize == 0 || ng <= 0) return OWM_OK;
   if (scratch_bytes < stage3_scratch_bytes(ng)) return OWM_ENOMEM;
   const S3Layout L = stage3_layout(scratch, ng);
   if (llp_cap > 0) {
-    OWM_LAUNCH("k_s3_mark", s, k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, d_llp, d_nllp, llp_cap, L.ex, L.ey,
+    OWM_LAUNCH("k_s3_mark", s, k_s3_mark<<<grid1d(llp_cap), 256, 0, s>>>(d_xyz, stride, d_llp, d_nllp, llp_cap, L.ex, L.ey,
                                                                        (int32_t)p.ncols_grid, (int32_t)p.nrows_grid,
                                                                        p.bbox.min_x, p.bbox.min_y, (double)p.bsize,
                                                                        L.mark));
@@ -796,12 +796,12 @@ int run_stage3_query(const TreeView& t, const owm_params& p, uint32_t* d_out, ui
   return OWM_OK;
 }
 
-int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
+int run_stage3(const TreeView& t, const double* d_xyz, int stride, const owm_params& p, const uint32_t* d_llp,
                const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
                size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches) {
   (void)d_job_slot;
   int rc = run_stage3_prepare(t.ox, t.oy, p, scratch, scratch_bytes, s, launches);
-  if (!rc) rc = run_stage3_mark(d_xyz, p, d_llp, d_nllp, llp_cap, scratch, scratch_bytes, s, launches);
+  if (!rc) rc = run_stage3_mark(d_xyz, stride, p, d_llp, d_nllp, llp_cap, scratch, scratch_bytes, s, launches);
   if (rc) return rc;
   return run_stage3_query(t, p, d_out, d_count, scratch, scratch_bytes, status, s, launches);
 }

@@ -85,10 +85,11 @@ int run_stage2_into(const uint32_t* d_win, uint32_t* k0, uint32_t* k1, uint32_t*
                     int64_t npoints, double overlap, uint32_t* d_llp, uint32_t* d_count, void* temp,
                     size_t temp_bytes, cudaStream_t s, int64_t* launches);
 
-// Stage 3: mark cells holding an LLP (x, y read from the input cloud), query
-// the rest, compact in cell order.  d_out gets the ids, *d_count their number.
+// Stage 3: mark cells holding an LLP (x, y read from the input points: AoS
+// records of `stride` doubles, 3 or 4), query the rest, compact in cell
+// order.  d_out gets the ids, *d_count their number.
 size_t stage3_scratch_bytes(int64_t ngrid);
-int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, const uint32_t* d_llp,
+int run_stage3(const TreeView& t, const double* d_xyz, int stride, const owm_params& p, const uint32_t* d_llp,
                const uint32_t* d_nllp, int64_t llp_cap, uint32_t* d_out, uint32_t* d_count, void* scratch,
                size_t scratch_bytes, QueryJob* d_job_slot, uint32_t* status, cudaStream_t s, int64_t* launches);
 // The same in three parts on one scratch layout: the cell edge tables (float
@@ -97,7 +98,7 @@ int run_stage3(const TreeView& t, const double* d_xyz, const owm_params& p, cons
 // compaction (need the tree hierarchy).
 int run_stage3_prepare(double ox, double oy, const owm_params& p, void* scratch, size_t scratch_bytes,
                        cudaStream_t s, int64_t* launches);
-int run_stage3_mark(const double* d_xyz, const owm_params& p, const uint32_t* d_llp, const uint32_t* d_nllp,
+int run_stage3_mark(const double* d_xyz, int stride, const owm_params& p, const uint32_t* d_llp, const uint32_t* d_nllp,
                     int64_t llp_cap, void* scratch, size_t scratch_bytes, cudaStream_t s, int64_t* launches);
 int run_stage3_query(const TreeView& t, const owm_params& p, uint32_t* d_out, uint32_t* d_count, void* scratch,
                      size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches);

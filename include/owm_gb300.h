@@ -171,8 +171,11 @@ int owm_ctx_kernel_times(owm_ctx* ctx, int32_t cap, char (*names)[64], double* m
 
 /* ---- device cloud ------------------------------------------------------ */
 typedef struct owm_cloud owm_cloud;
-/* Copies n AoS points (host or device pointer) to the device.  bbox NULL =
- * exact data min/max.  Replaces the cloud array built by readXYZfile. */
+/* Copies n AoS points (x, y, z doubles; host or device pointer) to the
+ * device, where the cloud keeps each point as a 32-byte record (x, y, z,
+ * pad), so that each random point read of the build's gather is one aligned
+ * DRAM sector (a 24-byte point straddles two sectors half the time).  bbox
+ * NULL = exact data min/max.  Replaces the cloud array built by readXYZfile. */
 int owm_cloud_create(owm_ctx* ctx, const double* xyz, int64_t n, const owm_bbox* bbox,
                      owm_cloud** out);
 int owm_cloud_destroy(owm_cloud* cloud);
