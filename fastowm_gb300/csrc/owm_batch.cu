@@ -1201,7 +1201,7 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
       const RadixSortPlan sp = radix_sort_plan(N);
       if (sp.parts) {  // the Morton pass also counts the sort's first digit
         OWM_LAUNCH("k_b_morton", s, k_b_morton_counts<<<(unsigned)sp.parts, 256, 0, s>>>(
-            xyz, N, d_ptoff, d_meta, ntiles, P.mbits, sp.ntiles, (1u << radix_digit_bits(key_bits, 0, true)) - 1u, k0,
+            xyz, N, d_ptoff, d_meta, ntiles, P.mbits, sp.ntiles, (1u << radix_digit_bits(key_bits, 0, radix_ranked_widths(N, key_bits))) - 1u, k0,
             (uint32_t*)at(P.o_sort)));
       } else {
         OWM_LAUNCH("k_b_morton", s, k_b_morton<<<gsz(N), 256, 0, s>>>(xyz, N, d_ptoff, d_meta, ntiles, P.mbits, k0));

@@ -532,7 +532,7 @@ int build_tree(const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, c
       morton_int_shifts(oy, oy + 2.0 * R, bits_axis, &ky0, &shy)) {
     if (plan.parts) {
       const MortonIntKey kf{kx0, ky0, (1ll << bits_axis) - 1, shx, shy};
-      const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, true)) - 1u;
+      const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, radix_ranked_widths(n, key_bits))) - 1u;
       if (stride == 4)
         OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey, 4><<<(unsigned)plan.parts, 256, 0, s>>>(
             d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
@@ -547,7 +547,7 @@ int build_tree(const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, c
   } else {
     if (plan.parts) {
       const MortonFpKey kf{ox, oy, scale, (float)((1u << bits_axis) - 1u)};
-      const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, true)) - 1u;
+      const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, radix_ranked_widths(n, key_bits))) - 1u;
       if (stride == 4)
         OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey, 4><<<(unsigned)plan.parts, 256, 0, s>>>(
             d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));

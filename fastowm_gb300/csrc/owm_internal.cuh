@@ -153,19 +153,25 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
                        int64_t* launches, bool first_counts_given = false, uint32_t* status = nullptr);
 
 // Digit width of pass `pass` of a sort on end_bit key bits: the fewest passes
-// of at most 8 bits (small sorts) or, for large (chunked) sorts, of at most 7
-// bits, which the ranked downsweep handles; widths balanced (differing by at
-// most one bit, wider first): 20 bits -> 7, 7, 6 either way; 23 -> 8, 8, 7
-// or 6, 6, 6, 5.  Four ranked passes cost less than two ballot-multisplit
-// 8-bit passes and a ranked 7-bit one.  Producers that count the first digit
-// (RadixSortPlan) use the large-sort widths.
-__host__ __device__ __forceinline__ int radix_digit_bits(int end_bit, int pass, bool large = false) {
-  const int np = large ? (end_bit + 6) / 7 : (end_bit + 7) / 8;
+// of at most 8 bits, or (ranked) of at most 7 bits, which the ranked
+// downsweep handles; widths balanced (differing by at most one bit, wider
+// first): 20 bits -> 7, 7, 6 either way; 23 -> 8, 8, 7 or 6, 6, 6, 5.
+__host__ __device__ __forceinline__ int radix_digit_bits(int end_bit, int pass, bool ranked = false) {
+  const int np = ranked ? (end_bit + 6) / 7 : (end_bit + 7) / 8;
   return end_bit / np + (pass < end_bit % np ? 1 : 0);
+}
+// Whether a large (chunked) sort of n keys on end_bit bits takes the ranked
+// widths: when they need no more passes than 8-bit digits, or from 4 M keys
+// (a ranked pass costs about 0.39 ms per 100 M keys and an 8-bit ballot-
+// multisplit pass 0.69, each with about 12 us of upsweep, scan and launches:
+// the extra pass pays from about 2.3 M keys for 23-24 bits, 5 M for 16).
+// Producers that count the first digit (RadixSortPlan) use the same rule.
+inline bool radix_ranked_widths(int64_t n, int end_bit) {
+  return (end_bit + 6) / 7 == (end_bit + 7) / 8 || n >= ((int64_t)4 << 20);
 }
 
 // Layout of a large sort's count table, for producers of keys that also count
-// the first pass's digits (bits 0..radix_digit_bits(end_bit, 0, true)-1) on the fly.  The keys are split into
+// the first pass's digits (bits 0..radix_digit_bits(end_bit, 0, radix_ranked_widths(n, end_bit))-1) on the fly.  The keys are split into
 // `parts` contiguous ranges (sort_part_range); count[d * parts + p] is the
 // number of keys of part p whose low byte is d, at the start of the sort's
 // temp.  parts == 0: the sort takes its small-sort path (counts not given).

@@ -1043,10 +1043,10 @@ cudaError_t radix_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, i
   // where a bounded wait that runs out is recorded when the caller gives no status word
   uint32_t* st = status ? status : reinterpret_cast<uint32_t*>(static_cast<char*>(temp) + temp_bytes - 256);
   int pass = 0;
-  const bool large = chunks > 0;  // digits of at most 7 bits: every pass ranked
-  for (int shift = 0; shift < end_bit; shift += radix_digit_bits(end_bit, pass++, large)) {
+  const bool ranked = chunks > 0 && radix_ranked_widths(n, end_bit);  // digits of at most 7 bits
+  for (int shift = 0; shift < end_bit; shift += radix_digit_bits(end_bit, pass++, ranked)) {
     // a pass sorts on bits [shift, shift + dbits); higher key bits are ignored
-    const int dbits = radix_digit_bits(end_bit, pass, large);
+    const int dbits = radix_digit_bits(end_bit, pass, ranked);
     const uint32_t dmask = (1u << dbits) - 1u;
     if (chunks) {
       if (!(first && first_counts_given))
