@@ -150,8 +150,8 @@ __global__ void k_scan_parts(const uint32_t* in, uint32_t* out, int64_t nparts, 
   if (threadIdx.x == 0 && total) *total = tot;
 }
 
-__global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int64_t n,
-                            const uint32_t* __restrict__ part) {
+// Down-sweep of block b from an already scanned chunk offset part[b].
+__global__ void k_scan_down_scanned(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __restrict__ part) {
   int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   uint32_t s = 0;
@@ -161,6 +161,32 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restric
     s += v[k];
   }
   uint32_t off = block_excl_scan(s, nullptr) + part[blockIdx.x];
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t p = base + k;
+    if (p < n) out[p] = off;
+    off += v[k];
+  }
+}
+
+// Block b scans its chunk from the sum of the chunk totals before it, which
+// it adds up itself (at most kScanChunk of them, in L2), so no separate scan
+// of the totals is needed; the last block writes the grand total.
+__global__ void k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __restrict__ part,
+                            uint32_t* __restrict__ total) {
+  uint32_t before = 0;
+  for (int64_t i = threadIdx.x; i < (int64_t)blockIdx.x; i += kScanBlock) before += part[i];
+  uint32_t base_off;
+  block_excl_scan(before, &base_off);
+  if (total && threadIdx.x == 0 && blockIdx.x == gridDim.x - 1) *total = base_off + part[blockIdx.x];
+  int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t p = base + k;
+    v[k] = p < n ? in[p] : 0u;
+    s += v[k];
+  }
+  uint32_t off = block_excl_scan(s, nullptr) + base_off;
   for (int k = 0; k < kScanItems; ++k) {
     int64_t p = base + k;
     if (p < n) out[p] = off;
@@ -1003,16 +1029,17 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
   uint32_t* part = static_cast<uint32_t*>(temp);
   OWM_LAUNCH("k_scan_reduce", s, k_scan_reduce<<<(unsigned)parts, kScanBlock, 0, s>>>(in, n, part));
   count_launch(launches, 2);
-  if (parts <= (int64_t)kScanChunk) {
-    OWM_LAUNCH("k_scan_parts", s, k_scan_parts<<<1, kScanBlock, 0, s>>>(part, part, parts, total));
-    count_launch(launches);
-  } else {  // more than 2^26 values: scan the partial sums in place, recursively
-    const size_t pb = ((size_t)(parts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
-    cudaError_t e = exclusive_scan_u32(part, part, parts, total, static_cast<char*>(temp) + pb, temp_bytes - pb, s,
-                                       launches);
-    if (e != cudaSuccess) return e;
+  if (parts <= (int64_t)kScanChunk) {  // each down-sweep block adds up the chunk totals before it
+    OWM_LAUNCH("k_scan_down", s, k_scan_down<<<(unsigned)parts, kScanBlock, 0, s>>>(in, out, n, part, total));
+    return cudaGetLastError();
   }
-  OWM_LAUNCH("k_scan_down", s, k_scan_down<<<(unsigned)parts, kScanBlock, 0, s>>>(in, out, n, part));
+  // more than 2^26 values: scan the chunk totals in place, recursively; each
+  // down-sweep block then reads its scanned offset
+  const size_t pb = ((size_t)(parts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
+  cudaError_t e = exclusive_scan_u32(part, part, parts, total, static_cast<char*>(temp) + pb, temp_bytes - pb, s,
+                                     launches);
+  if (e != cudaSuccess) return e;
+  OWM_LAUNCH("k_scan_down_scanned", s, k_scan_down_scanned<<<(unsigned)parts, kScanBlock, 0, s>>>(in, out, n, part));
   return cudaGetLastError();
 }
 
