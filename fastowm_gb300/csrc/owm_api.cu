@@ -157,16 +157,25 @@ struct owm_cloud {
   owm_ctx* ctx;
   int device;  // destroy needs no context (it may already be gone)
   DeviceBuffer mem;  // n records of kCloudStride doubles (x, y, z, pad)
+  DeviceBuffer xy;   // n (x, y) pairs
   int64_t n;
   owm_bbox bbox;
 };
+
+namespace {
+// The kernels' view of a cloud: its records and its x, y array.
+PointsView cloud_points(const owm_cloud* cl) {
+  return PointsView{static_cast<const double*>(cl->mem.ptr), kCloudStride, static_cast<const double*>(cl->xy.ptr),
+                    kCloudXyStride};
+}
+}  // namespace
 
 struct owm_tree {
   owm_ctx* ctx;
   int device;
   DeviceBuffer mem;
   TreeStore t;
-  const double* d_xyz;  // borrowed from the cloud, kCloudStride doubles a point (stage 3 reads LLP coordinates)
+  const double* d_xy;  // borrowed from the cloud: its x, y array (stage 3 reads LLP coordinates)
   owm_bbox bbox;
   owm_tree_cfg cfg;
 };
@@ -376,7 +385,10 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
   cl->device = c->device;
   cl->n = n;
   cl->bbox = bb;
-  if (cl->mem.reserve((size_t)n * 8 * kCloudStride, c->stream) != OWM_OK) {
+  if (cl->mem.reserve((size_t)n * 8 * kCloudStride, c->stream) != OWM_OK ||
+      cl->xy.reserve((size_t)n * 8 * kCloudXyStride, c->stream) != OWM_OK) {
+    cl->mem.release(c->stream);
+    cudaStreamSynchronize(c->stream);
     delete cl;
     return OWM_ENOMEM;
   }
@@ -391,13 +403,16 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
     if (!rc) e = cudaMemcpyAsync(stage.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream);
     src = static_cast<const double*>(stage.ptr);
   }
-  if (!rc && e == cudaSuccess) rc = pad_points(src, n, static_cast<double*>(cl->mem.ptr), c->stream, &c->launches);
+  if (!rc && e == cudaSuccess)
+    rc = pad_points(src, n, static_cast<double*>(cl->mem.ptr), static_cast<double*>(cl->xy.ptr), c->stream,
+                    &c->launches);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   stage.release(c->stream);
   if (rc || e != cudaSuccess) {
     if (e != cudaSuccess) set_last_cuda_error(e, "cloud copy", __FILE__, __LINE__);
     cudaStreamSynchronize(c->stream);
     cl->mem.release(c->stream);
+    cl->xy.release(c->stream);
     delete cl;
     return rc ? rc : OWM_ECUDA;
   }
@@ -409,6 +424,7 @@ int owm_cloud_destroy(owm_cloud* cl) {
   if (!cl) return OWM_OK;
   cudaSetDevice(cl->device);
   if (cl->mem.ptr) cudaFree(cl->mem.ptr);  // synchronising free; no stream or context needed
+  if (cl->xy.ptr) cudaFree(cl->xy.ptr);
   cudaGetLastError();
   delete cl;
   return OWM_OK;
@@ -452,11 +468,11 @@ int owm_cloud_copy_out(const owm_cloud* cl, double* xyz, int64_t n) {
 
 namespace {
 // Wraps parsed device points as a cloud (bbox: the header's, else the data's).
-int finish_parsed_cloud(owm_ctx* c, DeviceBuffer& mem, int64_t n, int64_t declared, const owm_bbox& hb,
-                        owm_cloud** out) {
+int finish_parsed_cloud(owm_ctx* c, DeviceBuffer& mem, DeviceBuffer& xy, int64_t n, int64_t declared,
+                        const owm_bbox& hb, owm_cloud** out) {
   owm_bbox bb = hb;
   if (declared < 0) {
-    int rc = device_bbox(c, static_cast<const double*>(mem.ptr), kCloudStride, n, &bb);
+    int rc = device_bbox(c, static_cast<const double*>(xy.ptr), kCloudXyStride, n, &bb);
     if (rc) return rc;
   }
   if (!std::isfinite(bb.min_x) || !std::isfinite(bb.max_x) || !std::isfinite(bb.min_y) ||
@@ -470,6 +486,9 @@ int finish_parsed_cloud(owm_ctx* c, DeviceBuffer& mem, int64_t n, int64_t declar
   cl->mem = mem;
   mem.ptr = nullptr;
   mem.cap = 0;
+  cl->xy = xy;
+  xy.ptr = nullptr;
+  xy.cap = 0;
   *out = cl;
   return OWM_OK;
 }
@@ -497,7 +516,7 @@ int owm_cloud_parse_xyz(owm_ctx* c, const char* text, int64_t nbytes, owm_cloud*
   owm_bbox hb{};
   int rc = xyz_header(htext, hbytes, &data_off, &declared, &hb);
   if (rc) return rc;
-  DeviceBuffer dt, pts;
+  DeviceBuffer dt, pts, pxy;
   // the parser's 16-byte loads want an aligned copy with readable slack
   rc = dt.reserve((size_t)((nbytes + 15) & ~(int64_t)15) + 32, c->stream);
   if (rc) return rc;
@@ -508,10 +527,14 @@ int owm_cloud_parse_xyz(owm_ctx* c, const char* text, int64_t nbytes, owm_cloud*
     return OWM_ECUDA;
   }
   int64_t n = 0;
-  rc = parse_device_text(c, static_cast<const char*>(dt.ptr), nbytes, data_off, declared, &pts, &n, &c->launches);
+  rc = parse_device_text(c, static_cast<const char*>(dt.ptr), nbytes, data_off, declared, &pts, &pxy, &n,
+                         &c->launches);
   dt.release(c->stream);
-  if (!rc) rc = finish_parsed_cloud(c, pts, n, declared, hb, out);
-  if (rc) pts.release(c->stream);
+  if (!rc) rc = finish_parsed_cloud(c, pts, pxy, n, declared, hb, out);
+  if (rc) {
+    pts.release(c->stream);
+    pxy.release(c->stream);
+  }
   return rc;
 }
 
@@ -533,7 +556,7 @@ int owm_cloud_load_xyz(owm_ctx* c, const char* path, owm_cloud** out) {
   constexpr int64_t kChunk = (int64_t)64 << 20;
   char* pin[2] = {nullptr, nullptr};
   cudaEvent_t done[2] = {nullptr, nullptr};
-  DeviceBuffer dt, pts;
+  DeviceBuffer dt, pts, pxy;
   int rc = OWM_OK;
   int64_t data_off = 0, declared = -1;
   owm_bbox hb{};
@@ -569,10 +592,14 @@ int owm_cloud_load_xyz(owm_ctx* c, const char* path, owm_cloud** out) {
   }
   int64_t n = 0;
   if (!rc)
-    rc = parse_device_text(c, static_cast<const char*>(dt.ptr), nbytes, data_off, declared, &pts, &n, &c->launches);
+    rc = parse_device_text(c, static_cast<const char*>(dt.ptr), nbytes, data_off, declared, &pts, &pxy, &n,
+                           &c->launches);
   cleanup();
-  if (!rc) rc = finish_parsed_cloud(c, pts, n, declared, hb, out);
-  if (rc) pts.release(c->stream);
+  if (!rc) rc = finish_parsed_cloud(c, pts, pxy, n, declared, hb, out);
+  if (rc) {
+    pts.release(c->stream);
+    pxy.release(c->stream);
+  }
   return rc;
 }
 
@@ -585,14 +612,14 @@ int owm_tree_build(owm_ctx* c, const owm_cloud* cl, const owm_tree_cfg* cfg, owm
   tr->ctx = c;
   tr->device = c->device;
   tr->cfg = *cfg;
-  tr->d_xyz = static_cast<const double*>(cl->mem.ptr);
+  tr->d_xy = static_cast<const double*>(cl->xy.ptr);
   tr->bbox = cl->bbox;
   int rc = tree_alloc(&tr->t, &tr->mem, cl->n, *cfg, c->stream);
   tr->t.gather_block = c->tuning.gather_block;
   if (!rc) rc = c->scratch.reserve(tree_scratch_bytes(cl->n), c->stream);
   if (!rc) rc = clear_status(c);
   if (!rc)
-    rc = build_tree(tr->d_xyz, kCloudStride, cl->n, cl->bbox, *cfg, &tr->t, c->scratch.ptr, c->scratch.cap,
+    rc = build_tree(cloud_points(cl), cl->n, cl->bbox, *cfg, &tr->t, c->scratch.ptr, c->scratch.cap,
                     c->d_small + kStatusSlot, c->stream, &c->launches);
   if (!rc) rc = check_input_status(c);
   if (rc) {
@@ -729,7 +756,7 @@ int owm_stage3(owm_ctx* c, const owm_tree* tr, const owm_params* p, const int64_
   }
   rc = clear_status(c);
   if (!rc)
-    rc = run_stage3(tr->t.view(c->walk_limit, c->tuning.cell_warps), tr->d_xyz, kCloudStride, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
+    rc = run_stage3(tr->t.view(c->walk_limit, c->tuning.cell_warps), tr->d_xy, kCloudXyStride, *p, l32, d_nllp, n_llp, s3, d_cnt, c->scratch.ptr, c->scratch.cap,
                     c->d_job, c->d_small + kStatusSlot, c->stream, &c->launches);
   if (!rc) rc = check_input_status(c);
   if (rc) return rc;
@@ -752,7 +779,7 @@ int owm_run(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int64_t* se
   ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !cl || !cfg || !n_seeds || (!seeds && cap > 0)) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
-  return run_pipeline(c, static_cast<const double*>(cl->mem.ptr), kCloudStride, cl->n, cl->bbox, *cfg, seeds, cap,
+  return run_pipeline(c, cloud_points(cl), cl->n, cl->bbox, *cfg, seeds, cap,
                       n_seeds, info);
 }
 
@@ -773,7 +800,8 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   int rc = c->input.reserve((size_t)n * 24 + kXyzSlack, c->stream);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
-  return run_pipeline(c, static_cast<const double*>(c->input.ptr), 3, n, bb, *cfg, seeds, cap, n_seeds, info);
+  return run_pipeline(c, plain_points(static_cast<const double*>(c->input.ptr)), n, bb, *cfg, seeds, cap, n_seeds,
+                      info);
 }
 
 }  // extern "C"
@@ -786,11 +814,11 @@ namespace {
 // staging, and hands out the ticket.  On failure the caller's fail() waits
 // for everything queued so far.
 template <class Fail>
-int submit_slot(owm_ctx* c, owm_ctx::AsyncSlot& a, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb,
+int submit_slot(owm_ctx* c, owm_ctx::AsyncSlot& a, const PointsView& pts, int64_t n, const owm_bbox& bb,
                 const owm_run_cfg& cfg, int64_t* seeds, int64_t cap, int64_t* ticket, const char* fn, Fail fail) {
   int64_t* d_seeds = nullptr;
   int64_t room = 0;
-  int rc = run_pipeline_enqueue(c, d_xyz, stride, n, bb, cfg, &a.p, &d_seeds, &room);
+  int rc = run_pipeline_enqueue(c, pts, n, bb, cfg, &a.p, &d_seeds, &room);
   if (rc) return fail(rc);
   if (a.h_cap < room) {
     // growth only: the old staging may still be a copy target
@@ -858,7 +886,7 @@ int owm_run_submit(owm_ctx* c, const owm_cloud* cl, const owm_run_cfg* cfg, int6
     cudaStreamSynchronize(c->stream);
     return code;
   };
-  return submit_slot(c, *a, static_cast<const double*>(cl->mem.ptr), kCloudStride, cl->n, cl->bbox, *cfg, seeds, cap,
+  return submit_slot(c, *a, cloud_points(cl), cl->n, cl->bbox, *cfg, seeds, cap,
                      ticket,
                      "owm_run_submit", fail);
 }
@@ -902,7 +930,7 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
     set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
     return fail(OWM_ECUDA);
   }
-  return submit_slot(c, a, static_cast<const double*>(a.input.ptr), 3, n, bb, *cfg, seeds, cap, ticket,
+  return submit_slot(c, a, plain_points(static_cast<const double*>(a.input.ptr)), n, bb, *cfg, seeds, cap, ticket,
                      "owm_run_host_submit", fail);
 }
 

@@ -69,12 +69,20 @@ __global__ void k_morton(const double* __restrict__ xyz, int64_t n, double ox, d
 
 // Morton key of one point, integer form (k_morton_int) and FP64 form
 // (k_morton), for the counting variant below.
+// x and y of a point at p: one 16-byte load from a compact x, y array
+// (stride 2), two 8-byte loads from plain points.
+template <int kStride>
+__device__ __forceinline__ double2 load_xy(const double* __restrict__ p) {
+  if (kStride == 2) return __ldg(reinterpret_cast<const double2*>(p));
+  return make_double2(__ldg(p), __ldg(p + 1));
+}
+
 struct MortonIntKey {
   int64_t kx0, ky0, qmax;
   int shx, shy;
-  __device__ __forceinline__ uint32_t operator()(const double* __restrict__ p) const {
-    int64_t qx = (dkey(__ldg(p)) - kx0) >> shx;
-    int64_t qy = (dkey(__ldg(p + 1)) - ky0) >> shy;
+  __device__ __forceinline__ uint32_t operator()(double2 v) const {
+    int64_t qx = (dkey(v.x) - kx0) >> shx;
+    int64_t qy = (dkey(v.y) - ky0) >> shy;
     qx = qx < 0 ? 0 : (qx > qmax ? qmax : qx);
     qy = qy < 0 ? 0 : (qy > qmax ? qmax : qy);
     return (spread_bits16((uint32_t)qx) << 1) | spread_bits16((uint32_t)qy);
@@ -83,8 +91,8 @@ struct MortonIntKey {
 struct MortonFpKey {
   double ox, oy, scale;
   float qmax;
-  __device__ __forceinline__ uint32_t operator()(const double* __restrict__ p) const {
-    float fx = (float)((__ldg(p) - ox) * scale), fy = (float)((__ldg(p + 1) - oy) * scale);
+  __device__ __forceinline__ uint32_t operator()(double2 v) const {
+    float fx = (float)((v.x - ox) * scale), fy = (float)((v.y - oy) * scale);
     fx = fminf(fmaxf(fx, 0.0f), qmax);
     fy = fminf(fmaxf(fy, 0.0f), qmax);
     return (spread_bits16((uint32_t)fx) << 1) | spread_bits16((uint32_t)fy);
@@ -109,7 +117,7 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
   for (; i + 3 * 256 < e; i += 4 * 256) {  // four points in flight per thread
     uint32_t k[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) k[u] = key_of(xyz + kStride * (i + u * 256));
+    for (int u = 0; u < 4; ++u) k[u] = key_of(load_xy<kStride>(xyz + kStride * (i + u * 256)));
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       keys[i + u * 256] = k[u];
@@ -117,7 +125,7 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
     }
   }
   for (; i < e; i += 256) {
-    const uint32_t k = key_of(xyz + kStride * i);
+    const uint32_t k = key_of(load_xy<kStride>(xyz + kStride * i));
     keys[i] = k;
     atomicAdd(hw + (k & dmask0), 1u);
   }
@@ -481,13 +489,18 @@ size_t tree_scratch_bytes(int64_t n) {
   return a + 1024;
 }
 
-int build_tree(const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
+int build_tree(const PointsView& pts, int64_t n, const owm_bbox& bb, const owm_tree_cfg& cfg, TreeStore* t,
                void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
                const ClassArgs* cls, bool* fused, cudaEvent_t cls_ready, cudaEvent_t gather_done) {
   if (fused) *fused = false;
-  if (n <= 0 || n >= 0x7FFFFFFFLL || (stride != 3 && stride != 4)) return OWM_EINVAL;
+  const int stride = pts.rec_stride;
+  const double* d_xyz = pts.rec;
+  if (n <= 0 || n >= 0x7FFFFFFFLL || (stride != 3 && stride != 4) || (pts.xy_stride != 2 && pts.xy_stride != 3))
+    return OWM_EINVAL;
   // the gather reads 16-byte words; a 32-byte record is one sector
   if ((reinterpret_cast<uintptr_t>(d_xyz) & (stride == 4 ? 31u : 15u)) != 0) return OWM_EINVAL;
+  const double* d_xy = pts.xy;
+  const bool xy2 = pts.xy_stride == 2;  // the Morton pass reads x, y from a compact array
   if (scratch_bytes < tree_scratch_bytes(n)) return OWM_ENOMEM;
   char* sp = static_cast<char*>(scratch);
   auto take = [&](size_t bytes) {
@@ -533,31 +546,31 @@ int build_tree(const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, c
     if (plan.parts) {
       const MortonIntKey kf{kx0, ky0, (1ll << bits_axis) - 1, shx, shy};
       const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, radix_ranked_widths(n, key_bits))) - 1u;
-      if (stride == 4)
-        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey, 4><<<(unsigned)plan.parts, 256, 0, s>>>(
-            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
+      if (xy2)
+        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey, 2><<<(unsigned)plan.parts, 256, 0, s>>>(
+            d_xy, n, kf, plan.ntiles, dm0, k0, first_counts));
       else
         OWM_LAUNCH("k_morton", s, k_morton_counts<MortonIntKey, 3><<<(unsigned)plan.parts, 256, 0, s>>>(
-            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
-    } else if (stride == 4) {
-      OWM_LAUNCH("k_morton", s, k_morton_int<4><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
+            d_xy, n, kf, plan.ntiles, dm0, k0, first_counts));
+    } else if (xy2) {
+      OWM_LAUNCH("k_morton", s, k_morton_int<2><<<grid_for(n, 256), 256, 0, s>>>(d_xy, n, kx0, ky0, shx, shy, bits_axis, k0));
     } else {
-      OWM_LAUNCH("k_morton", s, k_morton_int<3><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, kx0, ky0, shx, shy, bits_axis, k0));
+      OWM_LAUNCH("k_morton", s, k_morton_int<3><<<grid_for(n, 256), 256, 0, s>>>(d_xy, n, kx0, ky0, shx, shy, bits_axis, k0));
     }
   } else {
     if (plan.parts) {
       const MortonFpKey kf{ox, oy, scale, (float)((1u << bits_axis) - 1u)};
       const uint32_t dm0 = (1u << radix_digit_bits(key_bits, 0, radix_ranked_widths(n, key_bits))) - 1u;
-      if (stride == 4)
-        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey, 4><<<(unsigned)plan.parts, 256, 0, s>>>(
-            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
+      if (xy2)
+        OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey, 2><<<(unsigned)plan.parts, 256, 0, s>>>(
+            d_xy, n, kf, plan.ntiles, dm0, k0, first_counts));
       else
         OWM_LAUNCH("k_morton", s, k_morton_counts<MortonFpKey, 3><<<(unsigned)plan.parts, 256, 0, s>>>(
-            d_xyz, n, kf, plan.ntiles, dm0, k0, first_counts));
-    } else if (stride == 4) {
-      OWM_LAUNCH("k_morton", s, k_morton<4><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+            d_xy, n, kf, plan.ntiles, dm0, k0, first_counts));
+    } else if (xy2) {
+      OWM_LAUNCH("k_morton", s, k_morton<2><<<grid_for(n, 256), 256, 0, s>>>(d_xy, n, ox, oy, scale, bits_axis, k0));
     } else {
-      OWM_LAUNCH("k_morton", s, k_morton<3><<<grid_for(n, 256), 256, 0, s>>>(d_xyz, n, ox, oy, scale, bits_axis, k0));
+      OWM_LAUNCH("k_morton", s, k_morton<3><<<grid_for(n, 256), 256, 0, s>>>(d_xy, n, ox, oy, scale, bits_axis, k0));
     }
   }
   count_launch(launches);

@@ -60,10 +60,23 @@ size_t tree_scratch_bytes(int64_t n);
 bool morton_int_shifts(double lo, double hi, int bits, int64_t* klo, int* shift);
 int choose_key_bits(int64_t n, int policy, double side, float min_radius, int32_t leaf);
 
+// Device points as the kernels read them: `rec`, AoS records of rec_stride
+// doubles for the random reads of the gather (4: a cloud's 32-byte records
+// x, y, z, pad, 32-byte aligned; 3: plain x, y, z, 16-byte aligned with
+// kXyzSlack readable bytes after the last point), and `xy`, x and y of point i
+// at xy[xy_stride * i] and the next double, for the streaming reads that need
+// no z (the Morton pass, a bbox, stage 3's LLP marks): 2 for a cloud's x, y
+// array, 3 for plain points (then xy == rec).
+struct PointsView {
+  const double* rec;
+  int rec_stride;
+  const double* xy;
+  int xy_stride;
+};
+inline PointsView plain_points(const double* xyz) { return PointsView{xyz, 3, xyz, 3}; }
+
 // Builds the tree of n device points into t (whose arrays must be allocated
-// with enough capacity): AoS records of `stride` doubles, 4 (a cloud's 32-byte
-// records x, y, z, pad; 32-byte aligned) or 3 (plain x, y, z; 16-byte aligned,
-// kXyzSlack readable bytes after the last point).  Scratch is caller-provided.
+// with enough capacity).  Scratch is caller-provided.
 // Non-finite input coordinates set bit 0 of *status (device word).  With cls,
 // the fixed-leaf gather also folds every point into the stage-1 window
 // classes (*fused says whether it did; the min-radius build does not); when
@@ -72,7 +85,7 @@ int choose_key_bits(int64_t n, int policy, double side, float min_radius, int32_
 // gather_done (if given) is recorded on s right after that gather, so the
 // classes may be finished on another stream while the hierarchy is built.
 struct ClassArgs;
-int build_tree(const double* d_xyz, int stride, int64_t n, const owm_bbox& bbox, const owm_tree_cfg& cfg, TreeStore* t,
+int build_tree(const PointsView& pts, int64_t n, const owm_bbox& bbox, const owm_tree_cfg& cfg, TreeStore* t,
                void* scratch, size_t scratch_bytes, uint32_t* status, cudaStream_t s, int64_t* launches,
                const ClassArgs* cls = nullptr, bool* fused = nullptr, cudaEvent_t cls_ready = nullptr,
                cudaEvent_t gather_done = nullptr);

@@ -26,10 +26,10 @@ constexpr int kBboxSlot = 8;  // 4 x int64 (8-byte aligned)
 bool is_device_ptr(const void* p);
 // Device ingest of .xyz text (owm_ingest.cu): the header of host text, and
 // the parse of device text (16-byte aligned, 16 readable bytes of slack) into
-// a point buffer of *n_out points.
+// a cloud's two point buffers (records, x, y array) of *n_out points.
 int xyz_header(const char* text, int64_t nbytes, int64_t* data_off, int64_t* declared, owm_bbox* hb);
 int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t data_off, int64_t declared,
-                      DeviceBuffer* out_mem, int64_t* n_out, int64_t* launches);
+                      DeviceBuffer* out_mem, DeviceBuffer* out_xy, int64_t* n_out, int64_t* launches);
 int64_t total_launches();
 int tree_alloc(TreeStore* t, DeviceBuffer* mem, int64_t n, const owm_tree_cfg& cfg, cudaStream_t s);
 int validate_tree_cfg(const owm_tree_cfg* cfg);
@@ -107,22 +107,25 @@ namespace owm {
 int clear_status(owm_ctx* c);
 // Reads the status word (syncs); OWM_EINVAL if the input had a non-finite value.
 int check_input_status(owm_ctx* c);
-// Device points are AoS records of `stride` doubles: 4 for a cloud's 32-byte
-// records (x, y, z, pad: one DRAM sector per point for the build's random
-// gather), 3 for plain x, y, z (a caller's device array, host input copied in).
+// A cloud keeps its points twice: as 32-byte records (x, y, z, pad: one DRAM
+// sector per point for the build's random gather) and as a compact x, y array
+// (16 bytes a point, for the passes that stream x and y only).  A caller's
+// device array or host input copied in is read as plain x, y, z.
 constexpr int kCloudStride = 4;
-// n plain points (device, 8-byte aligned) into 32-byte records (32-byte
-// aligned dst), and back; queued on s.
-int pad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches);
+constexpr int kCloudXyStride = 2;
+// n plain points (device, 8-byte aligned) into records and the x, y array
+// (both 32-byte aligned), and records back to plain points; queued on s.
+int pad_points(const double* src, int64_t n, double* rec, double* xy, cudaStream_t s, int64_t* launches);
 int unpad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches);
-int device_bbox(owm_ctx* c, const double* d_xyz, int stride, int64_t n, owm_bbox* out);
+// bbox of n points whose x, y lie at d_xy[stride * i] and the next double.
+int device_bbox(owm_ctx* c, const double* d_xy, int stride, int64_t n, owm_bbox* out);
 int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Edge* ey, uint32_t* d_win);
-int run_pipeline(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+int run_pipeline(owm_ctx* c, const PointsView& pts, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
                  int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info);
 // The device part of run_pipeline: enqueues the whole run on c->stream and
 // leaves the status words in c->d_small and the assembled seeds (room slots)
 // at *d_seeds; no host sync (except inside the min-radius build).
-int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb,
-                         const owm_run_cfg& cfg, owm_params* p, int64_t** d_seeds, int64_t* room);
+int run_pipeline_enqueue(owm_ctx* c, const PointsView& pts, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+                         owm_params* p, int64_t** d_seeds, int64_t* room);
 
 }  // namespace owm

@@ -571,6 +571,7 @@ __global__ void __launch_bounds__(256) k_nl_starts(const char* __restrict__ text
 
 struct ParseOut {
   double* vals;             // [nlines][4]: cloud records x, y, z, 0
+  double* xy;               // [nlines][2]: the cloud's x, y array
   uint8_t* status;          // [nlines]
   int64_t* slow;            // queued line indices
   unsigned long long* nslow;
@@ -579,11 +580,12 @@ struct ParseOut {
 };
 
 // Line i's point as record i of a cloud (two 16-byte stores: the whole
-// 32-byte record, pad included).
-__device__ __forceinline__ void put_record(double* vals, int64_t i, const double* v) {
-  double2* d = reinterpret_cast<double2*>(vals + 4 * i);
+// 32-byte record, pad included) and entry i of its x, y array.
+__device__ __forceinline__ void put_record(const ParseOut& o, int64_t i, const double* v) {
+  double2* d = reinterpret_cast<double2*>(o.vals + 4 * i);
   d[0] = make_double2(v[0], v[1]);
   d[1] = make_double2(v[2], 0.0);
+  reinterpret_cast<double2*>(o.xy)[i] = make_double2(v[0], v[1]);
 }
 
 // One thread per line i: [starts[i], starts[i+1] - 1) (the newline excluded).
@@ -622,7 +624,7 @@ __global__ void __launch_bounds__(256, 4) k_parse(const char* __restrict__ text,
       }
       o.status[i] = (uint8_t)st;
       if (st == kLinePoint) {
-        put_record(o.vals, i, v);
+        put_record(o, i, v);
       } else if (st == kLineSlow) {
         o.slow[atomicAdd(o.nslow, 1ull)] = i;
       } else if (st == kLineError) {
@@ -648,7 +650,7 @@ __global__ void __launch_bounds__(128) k_parse_slow(const char* __restrict__ tex
     const int st = parse_line<true>(tc, starts[i], v, big);
     o.status[i] = (uint8_t)st;
     if (st == kLinePoint) {
-      put_record(o.vals, i, v);
+      put_record(o, i, v);
     } else {
       atomicMin(o.first_error, (unsigned long long)i);  // a queued line is a point or an error
     }
@@ -666,17 +668,21 @@ __global__ void k_line_flags(const uint8_t* __restrict__ status, int64_t nlines,
   }
 }
 
-// Points [0, n) of the flagged lines, in line order, into out (cloud records).
+// Points [0, n) of the flagged lines, in line order, into out (cloud records)
+// and out_xy (its x, y array).
 __global__ void k_compact_points(const double* __restrict__ vals, const uint32_t* __restrict__ is_point,
-                                 const uint32_t* __restrict__ pos, int64_t nlines, int64_t n, double* __restrict__ out) {
+                                 const uint32_t* __restrict__ pos, int64_t nlines, int64_t n, double* __restrict__ out,
+                                 double* __restrict__ out_xy) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlines;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (!is_point[i] || pos[i] >= (uint64_t)n) continue;
     const int64_t j = pos[i];
     const double2* r = reinterpret_cast<const double2*>(vals + 4 * i);
     double2* d = reinterpret_cast<double2*>(out + 4 * j);
-    d[0] = r[0];
+    const double2 a = r[0];
+    d[0] = a;
     d[1] = r[1];
+    reinterpret_cast<double2*>(out_xy)[j] = a;
   }
 }
 
@@ -760,7 +766,7 @@ int xyz_header(const char* text, int64_t nbytes, int64_t* data_off, int64_t* dec
 // Parses device text [0, nbytes) (16 bytes of slack after it, 16-byte
 // aligned) whose data lines start at data_off, into the cloud's buffer.
 int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t data_off, int64_t declared,
-                      DeviceBuffer* out_mem, int64_t* n_out, int64_t* launches) {
+                      DeviceBuffer* out_mem, DeviceBuffer* out_xy, int64_t* n_out, int64_t* launches) {
   cudaStream_t s = c->stream;
   int rc = ensure_pow10(c->device);
   if (rc) return rc;
@@ -771,14 +777,14 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   // newline positions in [begin, data_off) must not count: the count runs from data_off
   // itself, so tiles use the exact byte range [data_off, nbytes)
   // working buffers, released on every return (early CUDA-error returns included)
-  DeviceBuffer tmp, vbuf, work;
+  DeviceBuffer tmp, vbuf, xybuf, work;
   struct Release {
-    DeviceBuffer* b[3];
+    DeviceBuffer* b[4];
     cudaStream_t s;
     ~Release() {
       for (DeviceBuffer* x : b) x->release(s);
     }
-  } release_all{{&tmp, &vbuf, &work}, s};
+  } release_all{{&tmp, &vbuf, &xybuf, &work}, s};
   const size_t tb = a256((size_t)ntiles * 4) * 2 + a256(scan_temp_bytes(ntiles)) + 256;
   rc = tmp.reserve(tb, s);
   if (rc) return rc;
@@ -812,6 +818,7 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   // per-line values in their own buffer: when the first n lines are all
   // points it becomes the cloud as it is (no compaction)
   rc = vbuf.reserve((size_t)nlines * 8 * kCloudStride, s);
+  if (!rc) rc = xybuf.reserve((size_t)nlines * 8 * kCloudXyStride, s);
   if (rc) return rc;
   const size_t lb = a256((size_t)(nlines + 1 + hdr_nl + 1) * 8) + a256((size_t)nlines) +
                     2 * a256((size_t)nlines * 4) + a256((size_t)nlines * 8) + a256(scan_temp_bytes(nlines)) + 1024;
@@ -839,7 +846,7 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
   if (nlines > nl) OWM_CUDA_TRY(cudaMemcpyAsync(starts + nlines, &endpos, 8, cudaMemcpyHostToDevice, s));
   const unsigned long long init[3] = {0ull, ~0ull, 0ull};  // queued lines, first error line, blank lines
   OWM_CUDA_TRY(cudaMemcpyAsync(dwords, init, 24, cudaMemcpyHostToDevice, s));
-  ParseOut po{vals, status, slow, dwords, dwords + 1, dwords + 2};
+  ParseOut po{vals, static_cast<double*>(xybuf.ptr), status, slow, dwords, dwords + 1, dwords + 2};
   OWM_LAUNCH("k_parse", s, k_parse<<<grid_of((nlines + 31) / 32 * 32, 256), 256, 0, s>>>(dtext, starts, nlines, nbytes, po));
   OWM_LAUNCH("k_parse_slow", s, k_parse_slow<<<152 * 2, 128, 0, s>>>(dtext, starts, po));
   count_launch(launches, 2);
@@ -890,11 +897,16 @@ int parse_device_text(owm_ctx* c, const char* dtext, int64_t nbytes, int64_t dat
     *out_mem = vbuf;
     vbuf.ptr = nullptr;
     vbuf.cap = 0;
+    out_xy->release(s);
+    *out_xy = xybuf;
+    xybuf.ptr = nullptr;
+    xybuf.cap = 0;
   } else if (!rc) {
     rc = out_mem->reserve((size_t)n * 8 * kCloudStride, s);
+    if (!rc) rc = out_xy->reserve((size_t)n * 8 * kCloudXyStride, s);
     if (!rc) {
       OWM_LAUNCH("k_compact_points", s, k_compact_points<<<grid_of(nlines, 256), 256, 0, s>>>(
-          vals, is_point, pos, nlines, n, static_cast<double*>(out_mem->ptr)));
+          vals, is_point, pos, nlines, n, static_cast<double*>(out_mem->ptr), static_cast<double*>(out_xy->ptr)));
       count_launch(launches);
     }
   }

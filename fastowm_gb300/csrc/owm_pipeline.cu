@@ -40,13 +40,15 @@ __global__ void k_bbox(const double* __restrict__ xyz, int stride, int64_t n, lo
 }
 
 // Plain x, y, z points into a cloud's 32-byte records (x, y, z, 0), each
-// record written whole (two 16-byte stores), and back.
-__global__ void k_pad_points(const double* __restrict__ src, int64_t n, double* __restrict__ dst) {
+// record written whole (two 16-byte stores), and its x, y array; and back.
+__global__ void k_pad_points(const double* __restrict__ src, int64_t n, double* __restrict__ rec,
+                             double* __restrict__ xy) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = src[3 * i], y = src[3 * i + 1], z = src[3 * i + 2];
-    double2* d = reinterpret_cast<double2*>(dst + 4 * i);
+    double2* d = reinterpret_cast<double2*>(rec + 4 * i);
     d[0] = make_double2(x, y);
     d[1] = make_double2(z, 0.0);
+    reinterpret_cast<double2*>(xy)[i] = make_double2(x, y);
   }
 }
 
@@ -109,9 +111,9 @@ int device_bbox(owm_ctx* c, const double* d_xyz, int stride, int64_t n, owm_bbox
   return OWM_OK;
 }
 
-int pad_points(const double* src, int64_t n, double* dst, cudaStream_t s, int64_t* launches) {
+int pad_points(const double* src, int64_t n, double* rec, double* xy, cudaStream_t s, int64_t* launches) {
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
-  OWM_LAUNCH("k_pad_points", s, k_pad_points<<<g, 256, 0, s>>>(src, n, dst));
+  OWM_LAUNCH("k_pad_points", s, k_pad_points<<<g, 256, 0, s>>>(src, n, rec, xy));
   count_launch(launches);
   OWM_CUDA_TRY(cudaGetLastError());
   return OWM_OK;
@@ -144,8 +146,8 @@ int run_stage1(owm_ctx* c, const TreeStore& t, const owm_params& p, Edge* ex, Ed
   return run_query(j, c->d_job, c->stream, &c->launches, "k_query_s1");
 }
 
-int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb,
-                         const owm_run_cfg& cfg, owm_params* p_out, int64_t** d_seeds, int64_t* room_out) {
+int run_pipeline_enqueue(owm_ctx* c, const PointsView& pts, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+                         owm_params* p_out, int64_t** d_seeds, int64_t* room_out) {
   if (validate_tree_cfg(&cfg.tree) != OWM_OK) return OWM_EINVAL;
   owm_params& p = *p_out;
   int rc = owm_params_compute(&bb, n, cfg.wsize, cfg.overlap, cfg.bsize, &p);
@@ -214,7 +216,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n,
   c->stage12_side = false;
   c->tree.gather_block = c->tuning.gather_block;
   if (!rc)
-    rc = build_tree(d_xyz, stride, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
+    rc = build_tree(pts, n, bb, cfg.tree, &c->tree, c->scratch.ptr, tbytes, c->d_small + kStatusSlot, s,
                     &c->launches, cfg.stage1_walk ? nullptr : &cls, &fused, forked ? c->side_join : nullptr,
                     forked ? c->ev[6] : nullptr);
   void* s2scratch = static_cast<char*>(c->scratch.ptr) + tbytes + cbytes;
@@ -245,7 +247,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n,
       rc = bitmap2 ? run_stage2_bitmap(win, nc, n, p.overlap, llp, d_nllp, s2scratch, s2cap, ss, &c->launches, true, true)
                    : stage2(ss);
     if (!rc) OWM_CUDA_TRY(cudaEventRecord(c->ev[3], ss));
-    if (!rc) rc = run_stage3_mark(d_xyz, stride, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
+    if (!rc) rc = run_stage3_mark(pts.xy, pts.xy_stride, p, llp, d_nllp, nc, s3scratch, s3cap, ss, &c->launches);
     OWM_CUDA_TRY(cudaEventRecord(c->side_join, ss));
   }
   // join (again, if the gather already did): nothing queued on s after this
@@ -271,7 +273,7 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n,
   }
   rc = c->stage12_side
            ? run_stage3_query(c->tree.view(c->walk_limit, c->tuning.cell_warps), p, s3, d_ns3, s3scratch, s3cap, c->d_small + kStatusSlot, s, &c->launches)
-           : run_stage3(c->tree.view(c->walk_limit, c->tuning.cell_warps), d_xyz, stride, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
+           : run_stage3(c->tree.view(c->walk_limit, c->tuning.cell_warps), pts.xy, pts.xy_stride, p, llp, d_nllp, nc, s3, d_ns3, s3scratch, s3cap, c->d_job,
                         c->d_small + kStatusSlot, s, &c->launches);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaEventRecord(c->ev[4], s));
@@ -285,12 +287,12 @@ int run_pipeline_enqueue(owm_ctx* c, const double* d_xyz, int stride, int64_t n,
   return OWM_OK;
 }
 
-int run_pipeline(owm_ctx* c, const double* d_xyz, int stride, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
+int run_pipeline(owm_ctx* c, const PointsView& pts, int64_t n, const owm_bbox& bb, const owm_run_cfg& cfg,
                  int64_t* seeds, int64_t cap, int64_t* n_seeds, owm_run_info* info) {
   owm_params p;
   int64_t* s64 = nullptr;
   int64_t room = 0;
-  int rc = run_pipeline_enqueue(c, d_xyz, stride, n, bb, cfg, &p, &s64, &room);
+  int rc = run_pipeline_enqueue(c, pts, n, bb, cfg, &p, &s64, &room);
   if (rc) return rc;
   cudaStream_t s = c->stream;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->h_small, c->d_small, 32, cudaMemcpyDeviceToHost, s));

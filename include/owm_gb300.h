@@ -174,7 +174,8 @@ typedef struct owm_cloud owm_cloud;
 /* Copies n AoS points (x, y, z doubles; host or device pointer) to the
  * device, where the cloud keeps each point as a 32-byte record (x, y, z,
  * pad), so that each random point read of the build's gather is one aligned
- * DRAM sector (a 24-byte point straddles two sectors half the time).  bbox
+ * DRAM sector (a 24-byte point straddles two sectors half the time), and in a
+ * compact x, y array for the passes that need no z: 48 bytes a point.  bbox
  * NULL = exact data min/max.  Replaces the cloud array built by readXYZfile. */
 int owm_cloud_create(owm_ctx* ctx, const double* xyz, int64_t n, const owm_bbox* bbox,
                      owm_cloud** out);
