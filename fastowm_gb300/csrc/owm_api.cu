@@ -94,6 +94,16 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+bool device_ptr_on(const void* p, int device) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == device);
+}
+
 int DeviceBuffer::reserve(size_t bytes, cudaStream_t s) {
   if (bytes <= cap) return OWM_OK;
   if (ptr) {
@@ -368,18 +378,37 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
   if (!c || !xyz || !out || n <= 0 || n >= 0x7FFFFFFFLL) return OWM_EINVAL;
   *out = nullptr;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
+  // The kernels read xyz itself only when it is device memory of this
+  // context's device, 8-byte aligned; host memory, another device's memory or
+  // an unaligned pointer go through a device copy first (DeviceBuffer's
+  // stream-ordered free releases it on every return).
+  const bool host = !is_device_ptr(xyz);
+  const bool direct = device_ptr_on(xyz, c->device) && (reinterpret_cast<uintptr_t>(xyz) & 7u) == 0;
+  struct Stage {
+    DeviceBuffer b;
+    cudaStream_t s;
+    ~Stage() { b.release(s); }
+  } stage{{}, c->stream};
+  const double* src = xyz;
+  if (!direct) {
+    if (stage.b.reserve((size_t)n * 24, c->stream) != OWM_OK) return OWM_ENOMEM;
+    OWM_CUDA_TRY(cudaMemcpyAsync(stage.b.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
+    src = static_cast<const double*>(stage.b.ptr);
+  }
   owm_bbox bb;
   if (bbox) {
     bb = *bbox;
-  } else if (is_device_ptr(xyz)) {
-    int rc = device_bbox(c, xyz, 3, n, &bb);
-    if (rc) return rc;
-  } else {
+  } else if (host) {
     owm_bbox_of(xyz, n, &bb);
+  } else {
+    int rc = device_bbox(c, src, 3, n, &bb);
+    if (rc) return rc;
   }
   if (!std::isfinite(bb.min_x) || !std::isfinite(bb.max_x) || !std::isfinite(bb.min_y) ||
-      !std::isfinite(bb.max_y) || bb.max_x < bb.min_x || bb.max_y < bb.min_y)
+      !std::isfinite(bb.max_y) || bb.max_x < bb.min_x || bb.max_y < bb.min_y) {
+    cudaStreamSynchronize(c->stream);
     return OWM_EINVAL;
+  }
   owm_cloud* cl = new owm_cloud();
   cl->ctx = c;
   cl->device = c->device;
@@ -392,22 +421,10 @@ int owm_cloud_create(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* b
     delete cl;
     return OWM_ENOMEM;
   }
-  // the points as 32-byte records: from device memory directly, from host
-  // memory (or a device pointer not 8-byte aligned) through a device copy
-  DeviceBuffer stage;
-  const double* src = xyz;
-  int rc = OWM_OK;
-  cudaError_t e = cudaSuccess;
-  if (!is_device_ptr(xyz) || (reinterpret_cast<uintptr_t>(xyz) & 7u) != 0) {
-    rc = stage.reserve((size_t)n * 24, c->stream);
-    if (!rc) e = cudaMemcpyAsync(stage.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream);
-    src = static_cast<const double*>(stage.ptr);
-  }
-  if (!rc && e == cudaSuccess)
-    rc = pad_points(src, n, static_cast<double*>(cl->mem.ptr), static_cast<double*>(cl->xy.ptr), c->stream,
-                    &c->launches);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  stage.release(c->stream);
+  // the points as 32-byte records and the x, y array
+  int rc = pad_points(src, n, static_cast<double*>(cl->mem.ptr), static_cast<double*>(cl->xy.ptr), c->stream,
+                      &c->launches);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
   if (rc || e != cudaSuccess) {
     if (e != cudaSuccess) set_last_cuda_error(e, "cloud copy", __FILE__, __LINE__);
     cudaStreamSynchronize(c->stream);
@@ -687,7 +704,7 @@ int owm_stage1(owm_ctx* c, const owm_tree* tr, const owm_params* p, int64_t* win
   if (!rc) rc = run_stage1(c, tr->t, *p, ex, ey, win);
   if (!rc) rc = check_input_status(c);
   if (rc) return rc;
-  bool dev = is_device_ptr(win_min);
+  bool dev = device_ptr_on(win_min, c->device);  // written by a kernel only on this device
   rc = u32_to_i64_ids(win, nullptr, nc, dev ? win_min : w64, c->stream, &c->launches);
   if (rc) return rc;
   if (!dev) OWM_CUDA_TRY(cudaMemcpyAsync(win_min, w64, (size_t)nc * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -788,18 +805,20 @@ int owm_run_host(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox* bbox,
   ProfScope prof_scope(c ? c->active_prof() : nullptr);
   if (!c || !xyz || !cfg || !n_seeds || n <= 0 || n >= 0x7FFFFFFFLL || (!seeds && cap > 0)) return OWM_EINVAL;
   OWM_CUDA_TRY(cudaSetDevice(c->device));
+  // device input: its bbox from the copy on this device (xyz may be another device's memory)
+  const bool host = !is_device_ptr(xyz);
   owm_bbox bb;
-  if (bbox) {
+  if (bbox)
     bb = *bbox;
-  } else if (is_device_ptr(xyz)) {
-    int rc = device_bbox(c, xyz, 3, n, &bb);
-    if (rc) return rc;
-  } else {
+  else if (host)
     owm_bbox_of(xyz, n, &bb);
-  }
   int rc = c->input.reserve((size_t)n * 24 + kXyzSlack, c->stream);
   if (rc) return rc;
   OWM_CUDA_TRY(cudaMemcpyAsync(c->input.ptr, xyz, (size_t)n * 24, cudaMemcpyDefault, c->stream));
+  if (!bbox && !host) {
+    rc = device_bbox(c, static_cast<const double*>(c->input.ptr), 3, n, &bb);
+    if (rc) return rc;
+  }
   return run_pipeline(c, plain_points(static_cast<const double*>(c->input.ptr)), n, bb, *cfg, seeds, cap, n_seeds,
                       info);
 }
@@ -900,15 +919,13 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
   owm_ctx::AsyncSlot* ap = next_slot(c, &rc);
   if (!ap) return rc;
   owm_ctx::AsyncSlot& a = *ap;
+  // device input: its bbox from the copy on this device, below (xyz may be another device's memory)
+  const bool host = !is_device_ptr(xyz);
   owm_bbox bb;
-  if (bbox) {
+  if (bbox)
     bb = *bbox;
-  } else if (is_device_ptr(xyz)) {
-    rc = device_bbox(c, xyz, 3, n, &bb);
-    if (rc) return rc;
-  } else {
+  else if (host)
     owm_bbox_of(xyz, n, &bb);
-  }
   if (!c->copy_stream) OWM_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
   // This slot's previous run has been waited for, so nothing reads its input
   // buffer any more.  Reserving on the copy stream orders a (re)allocation
@@ -929,6 +946,10 @@ int owm_run_host_submit(owm_ctx* c, const double* xyz, int64_t n, const owm_bbox
   if (e != cudaSuccess) {
     set_last_cuda_error(e, "owm_run_host_submit", __FILE__, __LINE__);
     return fail(OWM_ECUDA);
+  }
+  if (!bbox && !host) {  // on c->stream after the copy; synchronous
+    rc = device_bbox(c, static_cast<const double*>(a.input.ptr), 3, n, &bb);
+    if (rc) return fail(rc);
   }
   return submit_slot(c, a, plain_points(static_cast<const double*>(a.input.ptr)), n, bb, *cfg, seeds, cap, ticket,
                      "owm_run_host_submit", fail);

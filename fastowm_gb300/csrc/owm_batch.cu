@@ -978,7 +978,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
   double* xyz = (double*)at(P.o_xyz);
   const int64_t N = P.npts;
   // tiles already back to back in one device buffer are used in place
-  bool in_place = is_device_ptr(td[0].xyz);
+  // (on this device: the kernels read them directly)
+  bool in_place = device_ptr_on(td[0].xyz, device);
   for (int32_t t = 1; t < ntiles && in_place; ++t) in_place = td[t].xyz == td[0].xyz + 3 * P.pt_off[t];
   if (in_place) xyz = const_cast<double*>(td[0].xyz);
   // points in (host or device sources)

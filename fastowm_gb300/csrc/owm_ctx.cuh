@@ -24,6 +24,9 @@ constexpr int kS3Slot = 4;
 constexpr int kBboxSlot = 8;  // 4 x int64 (8-byte aligned)
 
 bool is_device_ptr(const void* p);
+// Device memory of the given device (or managed memory), which that device's
+// kernels may read and write directly.
+bool device_ptr_on(const void* p, int device);
 // Device ingest of .xyz text (owm_ingest.cu): the header of host text, and
 // the parse of device text (16-byte aligned, 16 readable bytes of slack) into
 // a cloud's two point buffers (records, x, y array) of *n_out points.
