@@ -232,7 +232,9 @@ __global__ void __launch_bounds__(kBlock) k_rs_upsweep(const uint32_t* __restric
 // chunk blockIdx.x / kSubChunks (gridDim.x / kSubChunks chunks), into
 // hist[d * gridDim.x + blockIdx.x].  The scanned entry of a chunk's first
 // part is then that chunk's output base.  Keys are 16-byte aligned.
-__global__ void __launch_bounds__(kBlock) k_rs_upsweep_chunk(const uint32_t* __restrict__ keys, int64_t n,
+// At most 32 registers a thread (8 bytes spill): 8 blocks per SM, so the
+// 4 x 304 parts run in one wave (36 registers: 7 blocks, 1.14 waves).
+__global__ void __maxnreg__(32) k_rs_upsweep_chunk(const uint32_t* __restrict__ keys, int64_t n,
                                                              int shift, uint32_t dmask, uint32_t* __restrict__ hist,
                                                              int64_t ntiles) {
   __shared__ uint32_t h[kWarps][kRadix];
