@@ -11,7 +11,7 @@ CPP-TBB-CPU/application/owm_optim3.cpp):
     Context.stage1  stage1                 (optim3_func.cpp:541-561)
     Context.stage2  std::sort + stage2     (owm_optim3.cpp:160-188, optim3_func.cpp:610-625)
     Context.stage3  LLP grid + stage3      (owm_optim3.cpp:192-205, optim3_func.cpp:627-662)
-    Context.run     the driver's loop body, result = stage-3 ids ++ LLPs
+    Context.run     owm_optim3.cpp's loop body, result = stage-3 ids ++ LLPs
 
 Point ids are 1-based positions in the input order (the reference's
 cloud[] index); -1 means "no minimum".  Every compute call runs on the GPU;

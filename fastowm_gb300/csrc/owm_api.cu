@@ -5,7 +5,7 @@
 //   readXYZfile -> owm_xyz_read + owm_cloud_create
 //   parallel_qtree + storeMinAndNumPoints -> owm_tree_build
 //   stage1 / stage2 / grid + stage3 -> owm_stage1 / owm_stage2 / owm_stage3
-//   the driver's loop body -> owm_run
+//   the application's loop body -> owm_run
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -1,4 +1,4 @@
-// Host-side parts of the OWM path that carry no device work: the driver's
+// Host-side parts of the OWM path that carry no device work: the reference application's
 // parameter arithmetic, cloud file I/O and the tolerant GOLD score (the
 // seeded synthetic cloud generator is owm_synth.c).
 //
@@ -38,7 +38,7 @@ const char* owm_status_string(int s) {
 
 int owm_version(void) { return 10000; }
 
-// owm_optim3.cpp:92-132, with the driver's types: Npoints counts the
+// owm_optim3.cpp:92-132, with the reference application's types: Npoints counts the
 // sentinel (so Density uses Npoints-1), minNumPoints is uint32 then handed
 // to stage1 as ushort, nCols/nRows/nColsg/nRowsg are ushort.
 int owm_params_compute(const owm_bbox* bbox, int64_t npoints, uint32_t Wsize, double Overlap,

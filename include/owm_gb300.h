@@ -46,7 +46,7 @@ typedef struct {
   double min_x, min_y, max_x, max_y;
 } owm_bbox;
 
-/* Derived OWM parameters, computed with the reference driver's arithmetic
+/* Derived OWM parameters, computed with the reference application's arithmetic
  * and integer types (owm_optim3.cpp:92-132): Width/Height = round2d(extent),
  * Density = N/(W*H), minNumPoints = (uint32)(0.5*Density*Wsize^2) passed on
  * as ushort, Displace = round2d(Wsize*(1-Overlap)), nCols/nRows as ushort,

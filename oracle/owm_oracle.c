@@ -61,7 +61,7 @@ typedef struct {
 
 static double round2d(double z) { return round(z * 100.0) / 100.0; }
 
-/* owm_optim3.cpp:92-132 with the driver's integer types. */
+/* owm_optim3.cpp:92-132 with the reference application's integer types. */
 int oracle_params_compute(const double* bbox, int64_t n, uint32_t Wsize, double Overlap,
                           uint32_t Bsize, oracle_params* p) {
   if (n <= 0 || n >= 0xFFFFFFFFLL || !(Overlap >= 0.0 && Overlap < 1.0) || Wsize == 0) return -1;

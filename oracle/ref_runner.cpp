@@ -6,7 +6,7 @@
 // an in-memory cloud.  TBB / oneDPL are replaced by the scheduling-only
 // stand-ins under oracle/shim.
 //
-// What this file adds is the reference driver's glue, restated from
+// What this file adds is the reference application's glue, restated from
 // CPP-TBB-CPU/application/owm_optim3.cpp:
 //   * cloud with sentinel point 0 = {0, 0, DBL_MAX}   (optim3_func.cpp:702-708)
 //   * getRadius / getCenter -> parallel_qtree -> storeMinAndNumPoints

@@ -4,7 +4,7 @@
 // else; it carries no arithmetic of the algorithm.
 //
 // Names provided (exactly those used by CPP-TBB-CPU/src/optim3_func.cpp and
-// CPP-TBB-CPU/include/optim3_func.hpp, plus the driver's global_control and
+// CPP-TBB-CPU/include/optim3_func.hpp, plus the reference application's global_control and
 // tick_count):
 //   blocked_range<T>, blocked_range2d<R,C>, parallel_for (range form and
 //   index-step form), parallel_reduce (functional form, 2-D range),
