@@ -249,8 +249,8 @@ __global__ void k_bc_prep(const ClassArgs* __restrict__ cls) {
   for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nmax; i += gridDim.x * blockDim.x) {
     if (i < A.nx) cls_range_one(A.Lx, A.Rx, A.nx, i, A.sxl + i, A.sxh + i);
     if (i < A.ny) cls_range_one(A.Ly, A.Ry, A.ny, i, A.syl + i, A.syh + i);
-    if (i < A.qx) const_cast<int2*>(A.tabx)[i] = cls_table_one(A.Lx, A.Rx, A.nx, A.kx0, A.shx, i);
-    if (i < A.qy) const_cast<int2*>(A.taby)[i] = cls_table_one(A.Ly, A.Ry, A.ny, A.ky0, A.shy, i);
+    if (i < A.qx) const_cast<ClsCell*>(A.tabx)[i] = cls_table_one(A.Lx, A.Rx, A.nx, A.kx0, A.shx, i);
+    if (i < A.qy) const_cast<ClsCell*>(A.taby)[i] = cls_table_one(A.Ly, A.Ry, A.ny, A.ky0, A.shy, i);
   }
 }
 
@@ -757,12 +757,12 @@ int make_plan(const owm_tile_desc* td, int32_t ntiles, const BatchRun& br, Plan*
       Plan::ClsLayout& l = P->clay[t];
       auto piece = [&](size_t bytes) {
         size_t r = P->cls_misc;
-        P->cls_misc += (bytes + 15) & ~(size_t)15;
+        P->cls_misc += (bytes + 31) & ~(size_t)31;  // 32-byte table cells
         return r;
       };
       const size_t nx = (size_t)a.nx, ny = (size_t)a.ny, rows = nx * (size_t)a.ty;
-      l.tabx = piece((size_t)a.qx * 8);
-      l.taby = piece((size_t)a.qy * 8);
+      l.tabx = piece((size_t)a.qx * sizeof(ClsCell));
+      l.taby = piece((size_t)a.qy * sizeof(ClsCell));
       l.Lx = piece(nx * 8);
       l.Rx = piece(nx * 8);
       l.Ly = piece(ny * 8);
@@ -1094,8 +1094,8 @@ int BatchRun::launch(const owm_tile_desc* td, int32_t ntiles) {
     for (int32_t t = 0; t < ntiles; ++t) {
       const Plan::ClsLayout& l = P.clay[t];
       ClassArgs& a = A[t];
-      a.tabx = reinterpret_cast<const int2*>(misc + l.tabx);
-      a.taby = reinterpret_cast<const int2*>(misc + l.taby);
+      a.tabx = reinterpret_cast<const ClsCell*>(misc + l.tabx);
+      a.taby = reinterpret_cast<const ClsCell*>(misc + l.taby);
       a.Lx = reinterpret_cast<const int64_t*>(misc + l.Lx);
       a.Rx = reinterpret_cast<const int64_t*>(misc + l.Rx);
       a.Ly = reinterpret_cast<const int64_t*>(misc + l.Ly);

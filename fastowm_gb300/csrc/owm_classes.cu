@@ -42,7 +42,7 @@ __global__ void k_cls_split(const Edge* __restrict__ e, int32_t n, int64_t* __re
 }
 
 __global__ void k_cls_table(const int64_t* __restrict__ L, const int64_t* __restrict__ R, int32_t n, int64_t k0,
-                            int sh, int32_t Q, int2* __restrict__ tab) {
+                            int sh, int32_t Q, ClsCell* __restrict__ tab) {
   int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < Q) tab[q] = cls_table_one(L, R, n, k0, sh, q);
 }
@@ -121,7 +121,7 @@ bool cls_table_geometry(double lo, double hi, double step, int64_t* k0, int* sh,
 size_t classes_scratch_bytes(int64_t n, int32_t ncols, int32_t nrows) {
   const int64_t tx = 2 * (int64_t)ncols + 1, ty = 2 * (int64_t)nrows + 1;
   (void)n;  // nothing per point: the sub-cell counters are the whole state
-  return 2 * a256((size_t)kMaxTable * 8) + 2 * a256((size_t)ncols * 8) +
+  return 2 * a256((size_t)kMaxTable * sizeof(ClsCell)) + 2 * a256((size_t)ncols * 8) +
          2 * a256((size_t)nrows * 8) + 2 * a256((size_t)ncols * 4) + 2 * a256((size_t)nrows * 4) +
          a256((size_t)(tx * ty) * 4) + a256((size_t)(tx * ty) * 16) +
          2 * a256((size_t)(ncols * ty) * 4) + a256((size_t)(ncols * ty) * 8) + 1024;
@@ -141,8 +141,8 @@ int classes_prepare(const owm_params& p, const Edge* ex, const Edge* ey, void* s
     return q;
   };
   std::memset(A, 0, sizeof(*A));
-  int2* tabx = (int2*)take((size_t)kMaxTable * 8);
-  int2* taby = (int2*)take((size_t)kMaxTable * 8);
+  ClsCell* tabx = (ClsCell*)take((size_t)kMaxTable * sizeof(ClsCell));
+  ClsCell* taby = (ClsCell*)take((size_t)kMaxTable * sizeof(ClsCell));
   int64_t* Lx = (int64_t*)take((size_t)nc * 8);
   int64_t* Rx = (int64_t*)take((size_t)nc * 8);
   int64_t* Ly = (int64_t*)take((size_t)nr * 8);

@@ -13,10 +13,21 @@
 namespace owm {
 
 // Everything the per-point classification needs (device pointers).
+// Class-table cell of one axis: the left and right edges below its start
+// (a = #{L < start}, b = #{R < start}) and the first of each at or after it
+// (INT64_MAX when none).  A cell spans at most half a window step, so it
+// holds at most one edge of each kind, and a point's sub-cell index is one
+// 32-byte read away: a + b + (l < key) + (r <= key).
+struct __align__(32) ClsCell {
+  int64_t l, r;
+  int32_t a, b;
+  int32_t pad0, pad1;
+};
+
 struct ClassArgs {
   const int64_t *Lx, *Rx, *Ly, *Ry;  // edge keys per axis
   int32_t nx, ny;                     // window columns / rows
-  const int2 *tabx, *taby;            // class tables (q* == 0: none)
+  const ClsCell *tabx, *taby;         // class tables (q* == 0: none)
   int64_t kx0, ky0;
   int32_t shx, shy, qx, qy;
   int32_t tx, ty;                     // sub-cell grid: 2*nx+1 by 2*ny+1
@@ -78,25 +89,27 @@ __device__ __forceinline__ void cls_zid_min(ulonglong2* p, unsigned long long z,
   }
 }
 
+// Sub-cell index along one axis of a key that lies in table cell *e (below
+// INT64_MAX, as every key inside a table does).
+__device__ __forceinline__ int32_t cls_cell_index(const ClsCell* e, int64_t k) {
+  int64_t l, r, ab;
+  asm("ld.global.nc.v4.b64 {%0, %1, %2, _}, [%3];" : "=l"(l), "=l"(r), "=l"(ab) : "l"(e));
+  return (int32_t)(uint32_t)ab + (int32_t)(ab >> 32) + (l < k) + (r <= k);
+}
+
 // All 32 lanes call this together, each with one point (valid or not).
 // Folds the warp's points into their sub-cells: per group of lanes in one
 // sub-cell, one atomic add of the count and one (z, id) atomic min.
 __device__ __forceinline__ void cls_aggregate_warp(const ClassArgs& A, bool valid, int64_t px, int64_t py,
                                                    int64_t pz, uint32_t id, int lane) {
   int32_t sx = -1, sy = -1;
-  if (A.qx > 0) {  // table: one read + one compare per edge array
+  if (A.qx > 0) {  // table: one read
     const int64_t q = (px - A.kx0) >> A.shx;
-    if (q >= 0 && q < A.qx) {
-      const int2 a = __ldg(A.tabx + q);
-      sx = a.x + (a.x < A.nx && __ldg(A.Lx + a.x) < px) + a.y + (a.y < A.nx && __ldg(A.Rx + a.y) <= px);
-    }
+    if (q >= 0 && q < A.qx) sx = cls_cell_index(A.tabx + q, px);
   }
   if (A.qy > 0) {
     const int64_t q = (py - A.ky0) >> A.shy;
-    if (q >= 0 && q < A.qy) {
-      const int2 a = __ldg(A.taby + q);
-      sy = a.x + (a.x < A.ny && __ldg(A.Ly + a.x) < py) + a.y + (a.y < A.ny && __ldg(A.Ry + a.y) <= py);
-    }
+    if (q >= 0 && q < A.qy) sy = cls_cell_index(A.taby + q, py);
   }
   if (__any_sync(0xffffffffu, valid && (sx < 0 || sy < 0))) {
     // search: the warp's keys lie in [x0, x1] x [y0, y1], so every lane's
@@ -151,10 +164,16 @@ __device__ __forceinline__ void cls_range_one(const int64_t* L, const int64_t* R
 
 // Class-table cell q: (#{L < cell start}, #{R < cell start}) for cells of
 // 2^sh keys from k0.
-__device__ __forceinline__ int2 cls_table_one(const int64_t* L, const int64_t* R, int32_t n, int64_t k0, int sh,
+__device__ __forceinline__ ClsCell cls_table_one(const int64_t* L, const int64_t* R, int32_t n, int64_t k0, int sh,
                                               int32_t q) {
   const int64_t qs = k0 + ((int64_t)q << sh);
-  return make_int2(cls_count_less(L, n, qs), cls_count_less(R, n, qs));
+  ClsCell c;
+  c.a = cls_count_less(L, n, qs);
+  c.b = cls_count_less(R, n, qs);
+  c.l = c.a < n ? L[c.a] : INT64_MAX;
+  c.r = c.b < n ? R[c.b] : INT64_MAX;
+  c.pad0 = c.pad1 = 0;
+  return c;
 }
 
 __device__ __forceinline__ bool cls_zu_less(unsigned long long za, uint32_t ia, unsigned long long zb, uint32_t ib) {

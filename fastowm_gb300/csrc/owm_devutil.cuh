@@ -154,9 +154,8 @@ __device__ __forceinline__ bool load_point16(const double* __restrict__ xyz, uin
   if (kStride == 4) {
     // one 32-byte load; it bypasses L1, which then keeps the tables that the
     // callers look up per point (1.2% off the build gather at 100 M points)
-    double pad;
-    asm("ld.global.nc.L1::no_allocate.L2::64B.v4.f64 {%0, %1, %2, %3}, [%4];"
-        : "=d"(dx), "=d"(dy), "=d"(dz), "=d"(pad)
+    asm("ld.global.nc.L1::no_allocate.L2::64B.v4.f64 {%0, %1, %2, _}, [%3];"
+        : "=d"(dx), "=d"(dy), "=d"(dz)
         : "l"(xyz + 4 * (int64_t)src));
   } else {
     const int64_t e = 3 * (int64_t)src;
