@@ -164,14 +164,16 @@ __global__ void __maxnreg__(40) k_gather_leaves(const double* __restrict__ xyz, 
        u += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     LeafAcc acc;
     acc.init();
+    // the next chunk's permutation entry is in flight while a chunk is folded
+    uint32_t s_nxt = u * kUnit + lane < n ? __ldg(perm + u * kUnit + lane) : 0u;
 #pragma unroll
     for (int c = 0; c < kUnit; c += 32) {
       int64_t pos = u * kUnit + c + lane;
       const bool valid = pos < n;
       int64_t x = 0, y = 0, z = 0;
-      uint32_t src = 0;
+      const uint32_t src = s_nxt;
+      if (c + 32 < kUnit) s_nxt = pos + 32 < n ? __ldg(perm + pos + 32) : 0u;
       if (valid) {
-        src = __ldg(perm + pos);
         finite &= load_point16<kStride>(xyz, src, x, y, z);
         xk[pos] = x;
         yk[pos] = y;
