@@ -19,7 +19,6 @@
 //     duration and restores the caller's device before it returns;
 //   * the first call in each CUDA context of a device looks up the array's
 //     device address with cudaGetSymbolAddress (with that device current);
-//     make that first call before any stream capture;
 //   * every call shares the one array, which keeps the previous call's data:
 //     calls whose GPU work overlaps (two streams, two threads) race and
 //     corrupt each other's results -- serialise them;

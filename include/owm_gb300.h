@@ -266,9 +266,8 @@ int owm_stage3(owm_ctx* ctx, const owm_tree* tree, const owm_params* params, con
  * Working memory is one static device array of about 21.5 MB that every
  * GPU loading this library holds until exit; at most 1,048,576 windows per
  * call (OWM_ERANGE above that).  The first call in each CUDA context of a
- * device looks up the array's address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race, so serialise them. */
+ * device looks up the array's address (cudaGetSymbolAddress).  All calls
+ * share the array: calls that overlap on the GPU race, so serialise them. */
 int owm_stage2_noalloc(void* stream, const int64_t* d_win_min, int64_t ncells, double overlap,
                        int64_t npoints, int64_t* d_llp, int64_t* n_llp);
 
