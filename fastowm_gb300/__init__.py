@@ -2,11 +2,11 @@
 
 A thin layer over the C ABI (``include/owm_gb300.h``) of the in-tree native
 library.  Names follow the reference's entry points
-(CPP-TBB-CPU/include/optim3_func.hpp:73-93 and the driver
+(CPP-TBB-CPU/include/optim3_func.hpp:73-93 and the reference application
 CPP-TBB-CPU/application/owm_optim3.cpp):
 
     read_xyz        readXYZfile            (optim3_func.cpp:665-722)
-    params          driver parameter block (owm_optim3.cpp:92-132)
+    params          application parameter block (owm_optim3.cpp:92-132)
     Context.tree    parallel_qtree + storeMinAndNumPoints (optim3_func.cpp:220-307)
     Context.stage1  stage1                 (optim3_func.cpp:541-561)
     Context.stage2  std::sort + stage2     (owm_optim3.cpp:160-188, optim3_func.cpp:610-625)

@@ -1,4 +1,4 @@
-// The whole OWM path of one cloud on the device, as the reference driver
+// The whole OWM path of one cloud on the device, as the reference application
 // runs it per loop iteration (CPP-TBB-CPU/application/owm_optim3.cpp:77-230):
 // tree build, stage 1, sort + stage 2, LLP grid + stage 3, and the result
 // (stage-3 ids followed by the LLPs).  Intermediates never leave the device;

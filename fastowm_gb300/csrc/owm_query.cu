@@ -321,7 +321,7 @@ __global__ void k_s2_keys(const uint32_t* __restrict__ win, int64_t n, uint32_t 
 
 // Sorted keys -> flag of the first element of every run of length >= 2
 // (overlap > 0), or of every valid element (overlap == 0: the reference
-// counts all valid minima there, owm_optim3.cpp:185-188, and this build
+// counts all valid minima there, owm_optim3.cpp:185-188, and this kernel
 // compacts them; only the sentinel id 0 of empty windows can repeat).
 __global__ void k_s2_flags(const uint32_t* __restrict__ keys, int64_t n, uint32_t none_key, int need_dup,
                            uint32_t* __restrict__ flags) {

@@ -54,7 +54,7 @@ typedef struct {
   double min_x, min_y, max_x, max_y;
   double width, height, density, displace;
   uint32_t min_num_points; /* as stage1 receives it: (ushort) */
-  uint32_t ncols, nrows;   /* ushort-truncated like the driver */
+  uint32_t ncols, nrows;   /* ushort-truncated like the reference application */
   uint32_t ncols_grid, nrows_grid;
   int64_t ncells, ngrid;
 } oracle_params;

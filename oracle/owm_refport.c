@@ -354,7 +354,7 @@ static int cmp_int(const void* a, const void* b) {
   return (x > y) - (x < y);
 }
 
-/* Whole path like the reference driver.  xyz: n points (no sentinel);
+/* Whole path like the reference application.  xyz: n points (no sentinel);
  * policy 1 = maxNumber leaves, 0 = minRadius leaves (the -DMAXNUMBER switch).
  * seeds: stage-3 ids then LLPs; returns their count (or -1).  Times in s. */
 int64_t refport_run(const double* xyz, int64_t n, const double* bbox, uint32_t Wsize, double Overlap,
