@@ -163,6 +163,26 @@ def test_header_bbox_narrower_than_data(owm, oracle, ctx):
     np.testing.assert_array_equal(got, want)
 
 
+@pytest.mark.parametrize("xr,yr,W,Ov,B", [
+    ((1000.0, 1100.0), (3000.0, 3080.0), 10, 0.8, 20),   # x crosses 1024: no x table, y table
+    ((3000.0, 3080.0), (1000.0, 1100.0), 10, 0.8, 20),   # the same with the axes swapped
+    ((4100.0, 5600.0), (8200.0, 8260.0), 2, 0.9, 5),     # 0.2 m step: about 24,000 x-table cells
+])
+def test_class_table_axes(owm, oracle, ctx, xr, yr, W, Ov, B):
+    """Stage 1 by window classes looks a point's sub-cell up in a per-axis
+    table when the axis's keys are linear over the bbox (positive, one binary
+    exponent), and searches the edge arrays otherwise: one axis of each kind,
+    and a table of many cells, against the oracle."""
+    rng = np.random.default_rng(11)
+    n = 300_000
+    xyz = np.column_stack([xr[0] + rng.random(n) * (xr[1] - xr[0]), yr[0] + rng.random(n) * (yr[1] - yr[0]),
+                           np.round(100 + rng.random(n) * 3, 3)])
+    bb = owm.bbox_of(xyz)
+    got, want, _ = _run_both(owm, oracle, ctx, xyz, bb, W, Ov, B, 32)
+    assert len(want) > 0
+    np.testing.assert_array_equal(got, want)
+
+
 @pytest.mark.parametrize("policy,mn,mr", [(1, 32, 0.1), (1, 16, 0.1), (1, 128, 0.1), (0, 32, 0.4)])
 def test_large_cloud_policies(owm, oracle, ctx, policy, mn, mr):
     """1.5 M points (persistent pipelined sort), both leaf policies, both stage-1 algorithms."""
