@@ -141,8 +141,9 @@ __global__ void __launch_bounds__(256) k_morton_counts(const double* __restrict_
 
 // One warp per unit of max(L, 32) sorted positions.  L in {1,2,4,...,256}.
 // With kCls, every chunk of 32 gathered points is also folded into the
-// stage-1 window classes (the point is already in registers; this kernel is
-// DRAM-bound, so the classification costs next to nothing here).
+// stage-1 window classes while the point is in registers (about 0.45 ms of
+// the kernel's 2.5 ms at 100 M points, nearly all of it the sub-cell lookups
+// and the warp votes; the atomics take about 0.07 ms).
 // At most 40 registers a thread (a few bytes spill): 3 blocks of 512 (48
 // warps) per SM instead of 2 at the 63 registers the compiler would take; the
 // kernel waits on random DRAM reads, and the extra resident warps keep more of
