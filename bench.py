@@ -175,7 +175,12 @@ def kernel_bytes(name: str, n: int, p, nleaves: int) -> float | None:
     """Algorithmic bytes per launch of the main kernels (per-unit figures x units)."""
     if name == "k_query_s1":  # read sorted points once, node summaries, one result per window
         return 24.0 * n + 48.0 * nleaves + 8.0 * p.ncells
-    if name.startswith("k_gather_leaves"):  # perm + xyz in; keyed points, id and leaf out
+    if name.startswith("k_gather_leaves"):
+        # the permute step of the whole-step model (read the permutation, gather
+        # xyz, write the permuted points) and 48 B per leaf node.  With the
+        # class fold (the whole-path run) the kernel writes no permuted points:
+        # stage 3 reads its few points through the permutation instead.  The
+        # figure then exceeds what the kernel moves, which `traffic` measures.
         return (4 + 24 + 24 + 4) * n + 48.0 * nleaves
     if name == "k_rs_downsweep":
         return 16.0 * n
@@ -633,6 +638,10 @@ def main():
                                   "case of the same generator at leaf 256 (profiles/), per point x points"
                                   if traffic else None,
                 "ms_per_launch": round(per_launch_ms, 4), "bytes_per_launch": bytes_alg}
+        if name.startswith("k_gather_leaves"):
+            roof["bytes_note"] = ("bytes_per_launch is the whole-step model's permute step (56 B/pt, permuted "
+                                  "points written) + 48 B/leaf; the class-fold gather writes no permuted points "
+                                  "(28 B/pt + 48 B/leaf of its own): `traffic` is what it moves")
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         sspec, sW, sO, sB, smn, sseed = workload(args.config, args.cpu_sample)

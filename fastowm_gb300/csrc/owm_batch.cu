@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kW * 32) k_b_query_cells(const QueryJob* __res
     return;
   }
   const uint32_t r =
-      cell_min_warp(J.tree, J.ex[k % J.ncols], J.ey[k / J.ncols], stack_all + wib * kS3Stack, J.status, lane);
+      cell_min_warp<false>(J.tree, J.ex[k % J.ncols], J.ey[k / J.ncols], stack_all + wib * kS3Stack, J.status, lane);
   if (lane == 0) J.out[k] = r;
 }
 

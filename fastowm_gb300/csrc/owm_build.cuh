@@ -18,6 +18,10 @@ struct TreeStore {
   int32_t nleaves = 0, root = 0, key_bits = 0, max_leaf = 0;
   int32_t gather_block = 256;  // threads per block of the build's gather (128, 256 or 512)
   double ox = 0, oy = 0;
+  // points through the sort's permutation instead of the arrays (TreeView)
+  const uint32_t* perm = nullptr;
+  const double* rec = nullptr;
+  int32_t rec_stride = 0;
 
   TreeView view(int32_t walk_limit = 0, int32_t cell_warps = 4) const {
     TreeView v;
@@ -32,6 +36,9 @@ struct TreeStore {
     v.root = root;
     v.ox = ox;
     v.oy = oy;
+    v.perm = perm;
+    v.rec = rec;
+    v.rec_stride = rec_stride;
     return v;
   }
 };

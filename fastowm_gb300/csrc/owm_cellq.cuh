@@ -1,6 +1,7 @@
 // Stage-3 cell query by one warp per cell (single clouds and batches).
 #pragma once
 
+#include "owm_devutil.cuh"
 #include "owm_query.cuh"
 
 namespace owm {
@@ -27,8 +28,44 @@ constexpr int kS3Stack = 2304;   // node stack entries per warp (the kernels run
 
 __device__ __forceinline__ int64_t cq_shfl64(int64_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
+// Point p of the tree's sorted order as order keys and id: from the sorted
+// arrays, or (kPerm: the build kept none) from record perm[p] of its points.
+template <bool kPerm>
+__device__ __forceinline__ void cq_point(const TreeView& T, int64_t p, int64_t& x, int64_t& y, int64_t& z,
+                                         uint32_t& id) {
+  if (kPerm) {
+    const uint32_t src = __ldg(T.perm + p);
+    if (T.rec_stride == 4)
+      load_point16<4>(T.rec, src, x, y, z);
+    else
+      load_point16<3>(T.rec, src, x, y, z);
+    id = src + 1;
+  } else {
+    x = __ldg(T.xk + p);
+    y = __ldg(T.yk + p);
+    z = __ldg(T.zk + p);
+    id = __ldg(T.pid + p);
+  }
+}
+// x, y of a node's min point: sorted position p, id `id` (its record + 1).
+template <bool kPerm>
+__device__ __forceinline__ void cq_min_point_xy(const TreeView& T, int64_t p, uint32_t id, int64_t& x, int64_t& y) {
+  if (kPerm) {  // the id names the record: no permutation read
+    int64_t z;
+    if (T.rec_stride == 4)
+      load_point16<4>(T.rec, id - 1u, x, y, z);
+    else
+      load_point16<3>(T.rec, id - 1u, x, y, z);
+  } else {
+    x = __ldg(T.xk + p);
+    y = __ldg(T.yk + p);
+  }
+}
+
 // The whole warp answers the cell with edge tables ex, ey over tree T; st is
 // this warp's kS3Stack-entry shared stack.  Returns the result on every lane.
+// kPerm: T keeps no point arrays (T.perm is set).
+template <bool kPerm>
 __device__ __forceinline__ uint32_t cell_min_warp(const TreeView& T, const Edge& ex, const Edge& ey, int32_t* st,
                                                   uint32_t* status, int lane) {
   const uint32_t lt = (1u << lane) - 1u;
@@ -67,7 +104,8 @@ __device__ __forceinline__ uint32_t cell_min_warp(const TreeView& T, const Edge&
       if (inside) {
         cand = true;
       } else if (!outside && (improve || !any)) {
-        const int64_t mx = __ldg(T.xk + npos), my = __ldg(T.yk + npos);
+        int64_t mx, my;
+        cq_min_point_xy<kPerm>(T, npos, nid, mx, my);
         if (mx > ex.lo_k && mx < ex.hi_k && my > ey.lo_k && my < ey.hi_k) {
           cand = true;
         } else if (nodei >= first_leaf) {
@@ -112,28 +150,49 @@ __device__ __forceinline__ uint32_t cell_min_warp(const TreeView& T, const Edge&
       int64_t mz = 0x7FFFFFFFFFFFFFFFll;
       uint32_t mid = 0xFFFFFFFFu;
       bool seen = false;
-      // 128 points per chunk, every load issued before any test: one memory
-      // latency per chunk
-      for (uint32_t o = 0; o < c; o += 128) {
-        int64_t x[4], y[4], z[4];
-        uint32_t id[4];
+      // kU * 32 points per chunk, every load issued before any test: one
+      // memory latency per chunk (with kPerm two, the permutation entries
+      // first; 256 points a chunk, so a leaf of up to 256 points takes one)
+      constexpr int kU = kPerm ? 8 : 4;
+      for (uint32_t o = 0; o < c; o += 32 * kU) {
+        int64_t x[kU], y[kU], z[kU];
+        uint32_t id[kU];
+        if (kPerm) {
+          uint32_t src[kU];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const uint32_t k = o + u * 32 + lane;
-          if (k < c) {
-            const int64_t q = (int64_t)first + k;
-            x[u] = __ldg(T.xk + q);
-            y[u] = __ldg(T.yk + q);
-            z[u] = __ldg(T.zk + q);
-            id[u] = __ldg(T.pid + q);
-          } else {
-            x[u] = ex.lo_k;  // fails the strict test
-            y[u] = z[u] = 0;
-            id[u] = 0;
+          for (int u = 0; u < kU; ++u) {
+            const uint32_t k = o + u * 32 + lane;
+            src[u] = k < c ? __ldg(T.perm + (int64_t)first + k) : 0xFFFFFFFFu;  // positions < 2^31
+          }
+#pragma unroll
+          for (int u = 0; u < kU; ++u) {
+            if (src[u] != 0xFFFFFFFFu) {
+              if (T.rec_stride == 4)
+                load_point16<4>(T.rec, src[u], x[u], y[u], z[u]);
+              else
+                load_point16<3>(T.rec, src[u], x[u], y[u], z[u]);
+              id[u] = src[u] + 1u;
+            } else {
+              x[u] = ex.lo_k;  // fails the strict test
+              y[u] = z[u] = 0;
+              id[u] = 0;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < kU; ++u) {
+            const uint32_t k = o + u * 32 + lane;
+            if (k < c) {
+              cq_point<false>(T, (int64_t)first + k, x[u], y[u], z[u], id[u]);
+            } else {
+              x[u] = ex.lo_k;  // fails the strict test
+              y[u] = z[u] = 0;
+              id[u] = 0;
+            }
           }
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kU; ++u) {
           if (x[u] > ex.lo_k && x[u] < ex.hi_k && y[u] > ey.lo_k && y[u] < ey.hi_k) {
             seen = true;
             if (zid_less(z[u], id[u], mz, mid)) {

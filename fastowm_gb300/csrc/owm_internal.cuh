@@ -90,6 +90,14 @@ struct TreeView {
   // a walk give up on a well-formed tree (owm_ctx_set_walk_limit)
   int32_t walk_limit = 0;
   int32_t cell_warps = 4;  // stage-3 cell walk: cells (warps) per block, 2, 4 or 8
+  // Set when the build kept no sorted point arrays (xk, yk, zk and pid then
+  // hold nothing): point p of the sorted order is record perm[p] of `rec`
+  // (records of rec_stride doubles, x y z first), with id perm[p] + 1.  Only
+  // the stage-3 cell walk reads points this way; builds for anything else
+  // keep the arrays.
+  const uint32_t* perm = nullptr;
+  const double* rec = nullptr;
+  int32_t rec_stride = 0;
 };
 
 // ---------------------------------------------------------------------------

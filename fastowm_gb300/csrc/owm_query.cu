@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kQBlock) k_query_persistent(const QueryJob* __
 }
 
 // ---- stage 3: one warp per cell (owm_cellq.cuh) ---------------------------------
-template <int kW>
+template <int kW, bool kPerm>
 __global__ void __launch_bounds__(kW * 32) k_query_cells(TreeView T, const Edge* __restrict__ exs,
                                                            const Edge* __restrict__ eys, int32_t ncols,
                                                            int64_t ncells, const uint8_t* __restrict__ skip,
@@ -292,23 +292,32 @@ __global__ void __launch_bounds__(kW * 32) k_query_cells(TreeView T, const Edge*
     if (lane == 0) out[cell] = kNone;
     return;
   }
-  const uint32_t r = cell_min_warp(T, exs[cell % ncols], eys[cell / ncols], stack_all + wib * kS3Stack, status, lane);
+  const uint32_t r =
+      cell_min_warp<kPerm>(T, exs[cell % ncols], eys[cell / ncols], stack_all + wib * kS3Stack, status, lane);
   if (lane == 0) out[cell] = r;
 }
 
-template <int kW>
-cudaError_t launch_query_cells(const TreeView& t, const Edge* ex, const Edge* ey, int32_t ncols, int64_t ng,
-                               const uint8_t* skip, uint32_t* out, uint32_t* status, cudaStream_t s) {
+template <int kW, bool kPerm>
+cudaError_t launch_query_cells_as(const TreeView& t, const Edge* ex, const Edge* ey, int32_t ncols, int64_t ng,
+                                  const uint8_t* skip, uint32_t* out, uint32_t* status, cudaStream_t s) {
   static bool configured = false;  // per template instance
   const size_t smem = (size_t)kW * kS3Stack * sizeof(int32_t);
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_query_cells<kW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_query_cells<kW, kPerm>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  OWM_LAUNCH("k_query_s3", s, (k_query_cells<kW><<<(unsigned)((ng + kW - 1) / kW), kW * 32, smem, s>>>(
+  OWM_LAUNCH("k_query_s3", s, (k_query_cells<kW, kPerm><<<(unsigned)((ng + kW - 1) / kW), kW * 32, smem, s>>>(
       t, ex, ey, ncols, ng, skip, out, status)));
   return cudaGetLastError();
+}
+// Trees without point arrays (t.perm set) read points through the permutation.
+template <int kW>
+cudaError_t launch_query_cells(const TreeView& t, const Edge* ex, const Edge* ey, int32_t ncols, int64_t ng,
+                               const uint8_t* skip, uint32_t* out, uint32_t* status, cudaStream_t s) {
+  return t.perm ? launch_query_cells_as<kW, true>(t, ex, ey, ncols, ng, skip, out, status, s)
+                : launch_query_cells_as<kW, false>(t, ex, ey, ncols, ng, skip, out, status, s);
 }
 
 // ---- stage 2 -----------------------------------------------------------------
