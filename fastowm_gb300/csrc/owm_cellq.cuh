@@ -28,34 +28,20 @@ constexpr int kS3Stack = 2304;   // node stack entries per warp (the kernels run
 
 __device__ __forceinline__ int64_t cq_shfl64(int64_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-// Point p of the tree's sorted order as order keys and id: from the sorted
-// arrays, or (kPerm: the build kept none) from record perm[p] of its points.
-template <bool kPerm>
-__device__ __forceinline__ void cq_point(const TreeView& T, int64_t p, int64_t& x, int64_t& y, int64_t& z,
-                                         uint32_t& id) {
-  if (kPerm) {
-    const uint32_t src = __ldg(T.perm + p);
-    if (T.rec_stride == 4)
-      load_point16<4>(T.rec, src, x, y, z);
-    else
-      load_point16<3>(T.rec, src, x, y, z);
-    id = src + 1;
-  } else {
-    x = __ldg(T.xk + p);
-    y = __ldg(T.yk + p);
-    z = __ldg(T.zk + p);
-    id = __ldg(T.pid + p);
-  }
+// Record r of the points a tree without point arrays was built from, as
+// order keys (T.perm set: point p of the sorted order is record T.perm[p]).
+__device__ __forceinline__ void cq_record(const TreeView& T, uint32_t r, int64_t& x, int64_t& y, int64_t& z) {
+  if (T.rec_stride == 4)
+    load_point16<4>(T.rec, r, x, y, z);
+  else
+    load_point16<3>(T.rec, r, x, y, z);
 }
 // x, y of a node's min point: sorted position p, id `id` (its record + 1).
 template <bool kPerm>
 __device__ __forceinline__ void cq_min_point_xy(const TreeView& T, int64_t p, uint32_t id, int64_t& x, int64_t& y) {
   if (kPerm) {  // the id names the record: no permutation read
     int64_t z;
-    if (T.rec_stride == 4)
-      load_point16<4>(T.rec, id - 1u, x, y, z);
-    else
-      load_point16<3>(T.rec, id - 1u, x, y, z);
+    cq_record(T, id - 1u, x, y, z);
   } else {
     x = __ldg(T.xk + p);
     y = __ldg(T.yk + p);
@@ -167,10 +153,7 @@ __device__ __forceinline__ uint32_t cell_min_warp(const TreeView& T, const Edge&
 #pragma unroll
           for (int u = 0; u < kU; ++u) {
             if (src[u] != 0xFFFFFFFFu) {
-              if (T.rec_stride == 4)
-                load_point16<4>(T.rec, src[u], x[u], y[u], z[u]);
-              else
-                load_point16<3>(T.rec, src[u], x[u], y[u], z[u]);
+              cq_record(T, src[u], x[u], y[u], z[u]);
               id[u] = src[u] + 1u;
             } else {
               x[u] = ex.lo_k;  // fails the strict test
@@ -183,7 +166,11 @@ __device__ __forceinline__ uint32_t cell_min_warp(const TreeView& T, const Edge&
           for (int u = 0; u < kU; ++u) {
             const uint32_t k = o + u * 32 + lane;
             if (k < c) {
-              cq_point<false>(T, (int64_t)first + k, x[u], y[u], z[u], id[u]);
+              const int64_t q = (int64_t)first + k;
+              x[u] = __ldg(T.xk + q);
+              y[u] = __ldg(T.yk + q);
+              z[u] = __ldg(T.zk + q);
+              id[u] = __ldg(T.pid + q);
             } else {
               x[u] = ex.lo_k;  // fails the strict test
               y[u] = z[u] = 0;
